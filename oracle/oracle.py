@@ -1,0 +1,221 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes access to the CPU oracle.
+
+* ``liboracle.so`` (oracle/fastcc_oracle.cpp): the restatement of the
+  reference's ``Tensor<DT>::fastcc_multiply`` (contract.hpp:824-912), plus a
+  brute-force join and the 64-bit product count.
+* ``libfastcc_ref.so`` (oracle/ref_harness.cpp): the reference's own code,
+  compiled from its sources by ``make -C oracle ref``; it exists only where the
+  reference sources are present, and is used to pin the restatement.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module, as the checker or the timed CPU baseline.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libfastcc_ref.so")
+
+
+class _Tensor(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int32), ("nnz", ctypes.c_int64),
+                ("coords", ctypes.c_void_p), ("values", ctypes.c_void_p),
+                ("max_index", ctypes.c_void_p)]
+
+
+class _Result(ctypes.Structure):
+    _fields_ = [("nnz", ctypes.c_int64), ("order", ctypes.c_int32),
+                ("left", ctypes.POINTER(ctypes.c_uint64)),
+                ("right", ctypes.POINTER(ctypes.c_uint64)),
+                ("coords", ctypes.POINTER(ctypes.c_int32)),
+                ("values", ctypes.POINTER(ctypes.c_double)),
+                ("abs_sum", ctypes.POINTER(ctypes.c_double)),
+                ("products", ctypes.c_int64),
+                ("index_ms", ctypes.c_double), ("compute_ms", ctypes.c_double)]
+
+
+def build(ref=False):
+    """Compile liboracle.so (and the reference harness when ref=True)."""
+    subprocess.check_call(["make", "-s", "-C", HERE] + (["ref"] if ref else ["all"]))
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        _lib.orc_fastcc_multiply.restype = ctypes.c_int
+        _lib.orc_bruteforce.restype = ctypes.c_int
+        _lib.orc_count_products.restype = ctypes.c_int64
+        _lib.orc_infer_shape.restype = ctypes.c_int
+    return _lib
+
+
+def ref_available():
+    return os.path.exists(REF_PATH)
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        _ref = ctypes.CDLL(REF_PATH)
+        _ref.ref_fastcc_multiply.restype = ctypes.c_int
+    return _ref
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else ctypes.c_void_p(0)
+
+
+class _Keep:
+    """Holds numpy arrays alive while a ctypes struct points at them."""
+
+    def __init__(self, coords, values, max_index):
+        self.coords = np.ascontiguousarray(coords, dtype=np.int32)
+        self.values = np.ascontiguousarray(values, dtype=np.float64)
+        self.max_index = np.ascontiguousarray(max_index, dtype=np.int32)
+        order = self.coords.shape[1] if self.coords.ndim == 2 else len(self.max_index)
+        self.t = _Tensor(order, self.values.shape[0], _ptr(self.coords), _ptr(self.values),
+                         _ptr(self.max_index))
+
+
+def infer_shape(coords):
+    """Per-mode max index (Tensor::_infer_shape, contract.hpp:124-144)."""
+    coords = np.asarray(coords)
+    if coords.shape[0] == 0:
+        return np.zeros(coords.shape[1], np.int32)
+    return coords.max(axis=0).astype(np.int32)
+
+
+def _take(res, want_abs):
+    n, d = res.nnz, res.order
+    out = {
+        "order": d,
+        "products": res.products,
+        "index_ms": res.index_ms,
+        "compute_ms": res.compute_ms,
+        "left": np.ctypeslib.as_array(res.left, (max(n, 1),))[:n].copy(),
+        "right": np.ctypeslib.as_array(res.right, (max(n, 1),))[:n].copy(),
+        "values": np.ctypeslib.as_array(res.values, (max(n, 1),))[:n].copy(),
+        "coords": np.ctypeslib.as_array(res.coords, (max(n * d, 1),))[: n * d].reshape(n, d).copy(),
+    }
+    if want_abs:
+        out["abs_sum"] = np.ctypeslib.as_array(res.abs_sum, (max(n, 1),))[:n].copy()
+    lib().orc_free(ctypes.byref(res))
+    return out
+
+
+def fastcc_multiply(a_coords, a_vals, a_max, b_coords, b_vals, b_max, ctr_a, ctr_b,
+                    tile_size=100, nthreads=0, want_abs=False):
+    """The restatement; returns dict of numpy arrays (unsorted, reference order)."""
+    ka, kb = _Keep(a_coords, a_vals, a_max), _Keep(b_coords, b_vals, b_max)
+    ca = np.ascontiguousarray(ctr_a, np.int32)
+    cb = np.ascontiguousarray(ctr_b, np.int32)
+    res = _Result()
+    rc = lib().orc_fastcc_multiply(ctypes.byref(ka.t), ctypes.byref(kb.t), _ptr(ca), _ptr(cb),
+                                   ctypes.c_int32(len(ca)), ctypes.c_int32(tile_size),
+                                   ctypes.c_int32(nthreads), ctypes.c_int32(1 if want_abs else 0),
+                                   ctypes.byref(res))
+    if rc != 0:
+        raise ValueError("oracle rejected the arguments")
+    return _take(res, want_abs)
+
+
+def bruteforce(a_coords, a_vals, a_max, b_coords, b_vals, b_max, ctr_a, ctr_b):
+    ka, kb = _Keep(a_coords, a_vals, a_max), _Keep(b_coords, b_vals, b_max)
+    ca = np.ascontiguousarray(ctr_a, np.int32)
+    cb = np.ascontiguousarray(ctr_b, np.int32)
+    res = _Result()
+    rc = lib().orc_bruteforce(ctypes.byref(ka.t), ctypes.byref(kb.t), _ptr(ca), _ptr(cb),
+                              ctypes.c_int32(len(ca)), ctypes.byref(res))
+    if rc != 0:
+        raise ValueError("oracle rejected the arguments")
+    return _take(res, True)
+
+
+def count_products(a_coords, a_vals, a_max, b_coords, b_vals, b_max, ctr_a, ctr_b):
+    ka, kb = _Keep(a_coords, a_vals, a_max), _Keep(b_coords, b_vals, b_max)
+    ca = np.ascontiguousarray(ctr_a, np.int32)
+    cb = np.ascontiguousarray(ctr_b, np.int32)
+    return int(lib().orc_count_products(ctypes.byref(ka.t), ctypes.byref(kb.t), _ptr(ca), _ptr(cb),
+                                        ctypes.c_int32(len(ca))))
+
+
+def reference_multiply(a_coords, a_vals, a_max, b_coords, b_vals, b_max, ctr_a, ctr_b,
+                       tile_size=100, shipped=False):
+    """The reference's own fastcc_multiply (needs oracle/_ref). shipped=False plugs
+    in the recording accumulator; shipped=True runs TileAccumulator<double>."""
+    r = ref_lib()
+    ac = np.ascontiguousarray(a_coords, np.int32)
+    bc = np.ascontiguousarray(b_coords, np.int32)
+    av = np.ascontiguousarray(a_vals, np.float64)
+    bv = np.ascontiguousarray(b_vals, np.float64)
+    am = np.ascontiguousarray(a_max, np.int32)
+    bm = np.ascontiguousarray(b_max, np.int32)
+    ca = np.ascontiguousarray(ctr_a, np.int32)
+    cb = np.ascontiguousarray(ctr_b, np.int32)
+    n = ctypes.c_int64()
+    left = ctypes.POINTER(ctypes.c_uint64)()
+    right = ctypes.POINTER(ctypes.c_uint64)()
+    vals = ctypes.POINTER(ctypes.c_double)()
+    coords = ctypes.POINTER(ctypes.c_int32)()
+    order = ctypes.c_int32()
+    ms = ctypes.c_double()
+    rc = r.ref_fastcc_multiply(ac.shape[1], ac.shape[0], _ptr(ac), _ptr(av), _ptr(am),
+                               bc.shape[1], bc.shape[0], _ptr(bc), _ptr(bv), _ptr(bm),
+                               _ptr(ca), _ptr(cb), ctypes.c_int32(len(ca)),
+                               ctypes.c_int32(tile_size), ctypes.c_int32(1 if shipped else 0),
+                               ctypes.byref(n), ctypes.byref(left), ctypes.byref(right),
+                               ctypes.byref(vals), ctypes.byref(coords), ctypes.byref(order),
+                               ctypes.byref(ms))
+    if rc != 0:
+        raise ValueError("reference harness rejected the arguments")
+    k = n.value
+    out = {"order": order.value, "ms": ms.value,
+           "values": np.ctypeslib.as_array(vals, (k + 1,))[:k].copy()}
+    if shipped:
+        d = order.value
+        out["coords"] = np.ctypeslib.as_array(coords, (k * d + 1,))[: k * d].reshape(k, d).copy()
+        r.ref_free(coords)
+    else:
+        out["left"] = np.ctypeslib.as_array(left, (k + 1,))[:k].copy()
+        out["right"] = np.ctypeslib.as_array(right, (k + 1,))[:k].copy()
+        r.ref_free(left)
+        r.ref_free(right)
+    r.ref_free(vals)
+    return out
+
+
+def external_radices(max_index, ctr):
+    """Radices (max+1) of the non-contracted modes in ascending mode order."""
+    ctr = set(int(c) for c in ctr)
+    return [int(max_index[m]) + 1 for m in range(len(max_index)) if m not in ctr]
+
+
+def decode(lin, radices):
+    """Mixed-radix decode, last mode least significant."""
+    lin = np.asarray(lin, dtype=np.uint64).copy()
+    out = np.zeros((lin.shape[0], len(radices)), np.int64)
+    for e in range(len(radices) - 1, -1, -1):
+        r = np.uint64(radices[e])
+        out[:, e] = (lin % r).astype(np.int64)
+        lin //= r
+    return out
+
+
+def sort_output(coords, values, *extra):
+    """Lexicographic sort of output coordinates (for order-free comparison)."""
+    coords = np.asarray(coords)
+    if coords.shape[0] == 0 or coords.shape[1] == 0:
+        return (coords, values) + tuple(extra)
+    idx = np.lexsort(coords.T[::-1])
+    return (coords[idx], values[idx]) + tuple(e[idx] for e in extra)
