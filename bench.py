@@ -1,0 +1,306 @@
+#!/usr/bin/env python
+"""Benchmark: FaSTCC sparse x sparse contraction on one GB300.
+
+One step = one full contraction (index build, plan, tile contraction, output
+compaction) of the Zipf 3-way self-contraction A(i,c0,c1) * A(j,c0,c1):
+A 20,000 x 20,000 x 500,000 with 10M distinct nonzeros, every mode Zipf(1.2),
+sign-random lognormal values, contracted over modes {1,2}.
+
+  value  = FP64 multiply-adds per second, inputs resident on the device
+  e2e    = the same through the C ABI with host (pinned) operands and the full
+           output copied back to the host inside the timed region
+  roofline: the tile contraction kernel (k_contract_dense); algorithmic bytes
+           = inputs read once + outputs written once
+  cpu_baseline: the CPU oracle (restatement of the reference's OpenMP
+           fastcc_multiply) on a bounded sample of the same workload
+
+--impl reference times that CPU implementation alone (all host threads).
+Multi-GPU runs (torchrun) are replicas: every rank contracts its own copy.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "fastcc-benchmark_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "FP64 multiply-adds/s & ms/contraction: learned+batched vs plain, 1 GB300"
+UNIT = "multiply-adds/s"
+WORKLOAD = "zipf3: A 20000x20000x500000, 10M nnz, Zipf(1.2) per mode, lognormal values; A x A over modes {1,2}"
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_contract_dense launch on
+# this workload, from the ncu capture summarised in profiles/ (None until taken).
+MEASURED_TRAFFIC = None
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        def run():
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits"], capture_output=True,
+                                         text=True, timeout=5).stdout.strip()
+                    if out:
+                        self.rows.append([x.strip() for x in out.split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("FCC_BACKEND", "nccl") == "nccl" else "gloo")
+    return ws, rank, local
+
+
+def dist_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_sample(w, every, phase):
+    """The left operand restricted to rows i with i % every == phase; the right
+    operand is the whole tensor."""
+    a = w["a"]
+    sel = (a.coords[:, 0] % every) == phase
+    return a.coords[sel], a.values[sel]
+
+
+def time_cpu_oracle(w, every, nthreads):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    ac, av = cpu_sample(w, every, 0)
+    b = w["b"]
+    t0 = time.perf_counter()
+    o = oracle.fastcc_multiply(ac, av, w["a"].max_index, b.coords, b.values, b.max_index,
+                               w["ctr_a"], w["ctr_b"], tile_size=128, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return o["products"], dt, len(o["values"])
+
+
+def run_reference(args, ws, rank):
+    """--impl reference: the reference's CPU algorithm (the oracle restatement,
+    compiled here; the reference's own sources are not on this machine) on all
+    host threads, one bounded sample of the workload per step."""
+    if rank != 0:
+        return
+    import workloads
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    w = workloads.zipf3(seed=1)
+    ncores = os.cpu_count() or 1
+    every = 64
+    prods, secs = [], []
+    for s in range(args.warmup + args.steps):
+        p, dt, _ = time_cpu_oracle(w, every, ncores)
+        if s >= args.warmup:
+            prods.append(p)
+            secs.append(dt)
+    value = sum(prods) / sum(secs)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(secs) / len(secs),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": f"left operand rows i % {every} == 0, right operand whole",
+                       "products_per_step": prods[0]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port",
+                             "sample": f"rows i % {every} == 0 of the left operand ({prods[0]} multiply-adds)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+
+    import numpy as np
+    import torch
+
+    import build_lib
+    build_lib.build_all()
+    import fastcc_gpu as F
+    import workloads
+
+    torch.cuda.set_device(local)
+    w = workloads.zipf3(seed=1)
+    a = w["a"]
+    nnz = a.nnz
+    dev_c = torch.from_numpy(a.coords).cuda()
+    dev_v = torch.from_numpy(a.values).cuda()
+    A = F.Tensor(dev_c, dev_v, a.max_index)
+    torch.cuda.synchronize()
+    ctx = F.Context(local)
+    # a dedicated (non-default) stream: the library and the timing events share it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    opts = F.Options(timing=1)
+
+    res = None
+    for _ in range(args.warmup):
+        r = ctx.contract(A, A, w["ctr_a"], w["ctr_b"], opts)
+        res = (r.nnz, r.products, r.order)
+        r.free()
+    out_nnz, products, out_order = res
+
+    clocks = Clocks(local)
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks.start()
+    l0 = F.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    contract_ms = []
+    ev0.record(stream)
+    for _ in range(args.steps):
+        r = ctx.contract(A, A, w["ctr_a"], w["ctr_b"], opts)
+        contract_ms.append(ctx.timings()["contract"])
+        r.free()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = F.launch_count() - l0
+    barrier(ws)
+    clk = clocks.stop()
+    ms = dist_max(ev0.elapsed_time(ev1) / args.steps, ws)
+    phases = ctx.timings()
+    value = products * ws / (ms / 1000.0)
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    pin_c = torch.from_numpy(a.coords).pin_memory()
+    pin_v = torch.from_numpy(a.values).pin_memory()
+    H = F.Tensor(pin_c.numpy(), pin_v.numpy(), a.max_index)
+    out_c = torch.empty((out_order, out_nnz), dtype=torch.int32).pin_memory()
+    out_v = torch.empty(out_nnz, dtype=torch.float64).pin_memory()
+    e2e_opts = F.Options()
+    for _ in range(1):
+        r = ctx.contract(H, H, w["ctr_a"], w["ctr_b"], e2e_opts)
+        r.to_numpy_soa(out_c.numpy(), out_v.numpy())
+        r.free()
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.e2e_steps):
+        r = ctx.contract(H, H, w["ctr_a"], w["ctr_b"], e2e_opts)
+        r.to_numpy_soa(out_c.numpy(), out_v.numpy())
+        r.free()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = dist_max(e0.elapsed_time(e1) / args.e2e_steps, ws)
+    h2d = 2 * (pin_c.numel() * 4 + pin_v.numel() * 8)
+    d2h = out_nnz * (4 * out_order + 8)
+
+    peak, peak_kind = load_peaks()
+    alg_bytes = 2 * nnz * (4 * 3 + 8) + out_nnz * (4 * out_order + 8)
+    kms = statistics.mean(contract_ms)
+    achieved = alg_bytes / (kms / 1000.0) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nnz": nnz, "multiply_adds": products, "outputs": out_nnz,
+                   "l2": "inputs 200 MB and outputs 6.4 GB exceed the 129 MB L2; no flush",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": MEASURED_TRAFFIC,
+                     "kernel": "k_contract_dense", "kernel_ms": kms, "algorithmic_bytes": alg_bytes,
+                     "peak_kind": peak_kind},
+        "e2e": {"value": products * ws / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "phases_ms": {k: round(v, 4) for k, v in phases.items()},
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        # bounded sample: grow it (halve `every`) until one run takes >= 8 s
+        every = 256
+        while True:
+            p, dt, _ = time_cpu_oracle(w, every, os.cpu_count() or 1)
+            if dt >= 8.0 or every == 1:
+                break
+            grow = 2
+            while grow < 16 and dt * grow * 2 < 12.0:
+                grow *= 2
+            every = max(1, every // grow)
+        line["cpu_baseline"] = {"value": p / dt, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": f"left operand rows i % {every} == 0 ({p} multiply-adds, {dt:.1f} s)"}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,228 @@
+// C ABI of libfastcc_gpu.so (include/fastcc_gpu.h): contexts, the contraction
+// entry point and result access. Exceptions never cross this boundary; each
+// entry point returns an fcc_status and keeps the message for fcc_last_error.
+
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "fcc_internal.cuh"
+
+namespace fcc {
+void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+              const int32_t *ctrB, int k, const fcc_options &opt, fcc_result **out, i64 *products,
+              bool count_only);
+}
+
+namespace {
+
+thread_local std::string g_last_error;  // errors without a context
+
+template <class F>
+int guarded(fcc_ctx *ctx, F &&f) {
+  try {
+    if (ctx) FCC_CUDA(cudaSetDevice(ctx->device));
+    f();
+    return FCC_OK;
+  } catch (const fcc::Error &e) {
+    (ctx ? ctx->last_error : g_last_error) = e.msg;
+    return e.status;
+  } catch (const std::bad_alloc &) {
+    (ctx ? ctx->last_error : g_last_error) = "host allocation failed";
+    return FCC_ERR_OOM;
+  } catch (...) {
+    (ctx ? ctx->last_error : g_last_error) = "unexpected exception";
+    return FCC_ERR_CUDA;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int fcc_abi_version(void) { return FCC_ABI_VERSION; }
+
+int64_t fcc_launch_count(void) { return fcc::g_launches.load(); }
+
+const char *fcc_status_string(int32_t s) {
+  switch (s) {
+    case FCC_OK: return "ok";
+    case FCC_ERR_ARG: return "invalid argument";
+    case FCC_ERR_OOM: return "out of memory";
+    case FCC_ERR_HASH_FULL: return "hash accumulator full";
+    case FCC_ERR_TIMEOUT: return "bounded device wait timed out";
+    case FCC_ERR_CUDA: return "CUDA error";
+    case FCC_ERR_OVERFLOW: return "index space exceeds 64 bits";
+    case FCC_ERR_NO_DEVICE: return "no usable sm_103 device";
+    case FCC_ERR_CAPACITY: return "output buffer too small";
+    default: return "unknown status";
+  }
+}
+
+int fcc_options_default(fcc_options *o) {
+  if (!o) return FCC_ERR_ARG;
+  std::memset(o, 0, sizeof(*o));
+  o->tile_size = 100;
+  return FCC_OK;
+}
+
+const char *fcc_last_error(const fcc_ctx *ctx) {
+  return ctx ? ctx->last_error.c_str() : g_last_error.c_str();
+}
+
+int fcc_ctx_create(int32_t device, fcc_ctx **out) {
+  if (!out) return FCC_ERR_ARG;
+  *out = nullptr;
+  fcc_ctx *ctx = nullptr;
+  int st = guarded(nullptr, [&] {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+      cudaGetLastError();
+      throw fcc::Error{FCC_ERR_NO_DEVICE, "no CUDA device"};
+    }
+    int dev = device;
+    if (dev < 0) FCC_CUDA(cudaGetDevice(&dev));
+    if (dev >= n) throw fcc::Error{FCC_ERR_ARG, "device index out of range"};
+    FCC_CUDA(cudaSetDevice(dev));
+    cudaDeviceProp p{};
+    FCC_CUDA(cudaGetDeviceProperties(&p, dev));
+    if (!(p.major == 10 && p.minor == 3))
+      throw fcc::Error{FCC_ERR_NO_DEVICE, "this library is built for sm_103a (GB300) only"};
+    ctx = new fcc_ctx();
+    ctx->device = dev;
+    ctx->num_sms = p.multiProcessorCount;
+    int optin = 0;
+    FCC_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    ctx->smem_optin = size_t(optin);
+    FCC_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+    ctx->stream = ctx->own_stream;
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    FCC_CUDA(cudaMemPoolCreate(&ctx->pool, &props));
+    uint64_t keep = ~0ull;
+    FCC_CUDA(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    ctx->arena.init(ctx->pool);
+    FCC_CUDA(cudaMalloc(reinterpret_cast<void **>(&ctx->d_err), sizeof(fcc::u32)));
+    FCC_CUDA(cudaMallocHost(reinterpret_cast<void **>(&ctx->h_scalars), sizeof(fcc::u64) * 32));
+    for (auto &e : ctx->ev) FCC_CUDA(cudaEventCreate(&e));
+  });
+  if (st != FCC_OK) {
+    if (ctx) fcc_ctx_destroy(ctx);
+    return st;
+  }
+  *out = ctx;
+  return FCC_OK;
+}
+
+int fcc_ctx_destroy(fcc_ctx *ctx) {
+  if (!ctx) return FCC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->stream) ctx->arena.release_all(ctx->stream);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (auto &e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->d_err) cudaFree(ctx->d_err);
+  if (ctx->h_scalars) cudaFreeHost(ctx->h_scalars);
+  if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return FCC_OK;
+}
+
+int fcc_ctx_set_stream(fcc_ctx *ctx, void *stream) {
+  if (!ctx) return FCC_ERR_ARG;
+  return guarded(ctx, [&] {
+    // workspace frees are ordered on the previous stream: drain it first
+    FCC_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  });
+}
+
+int fcc_contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                 const int32_t *ctrB, int32_t k, const fcc_options *opts, fcc_result **out) {
+  if (!ctx || !out) return FCC_ERR_ARG;
+  *out = nullptr;
+  fcc_options o;
+  if (opts) o = *opts; else fcc_options_default(&o);
+  return guarded(ctx, [&] { fcc::contract(ctx, A, B, ctrA, ctrB, k, o, out, nullptr, false); });
+}
+
+int fcc_count_products(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                       const int32_t *ctrB, int32_t k, const fcc_options *opts, int64_t *products) {
+  if (!ctx || !products) return FCC_ERR_ARG;
+  fcc_options o;
+  if (opts) o = *opts; else fcc_options_default(&o);
+  return guarded(ctx, [&] { fcc::contract(ctx, A, B, ctrA, ctrB, k, o, nullptr, products, true); });
+}
+
+int fcc_result_info(const fcc_result *r, int32_t *order, int64_t *nnz, int64_t *products) {
+  if (!r) return FCC_ERR_ARG;
+  if (order) *order = r->order;
+  if (nnz) *nnz = r->nnz;
+  if (products) *products = r->products;
+  return FCC_OK;
+}
+
+int fcc_result_device(const fcc_result *r, const uint32_t **coords, int64_t *mode_stride,
+                      const double **values) {
+  if (!r) return FCC_ERR_ARG;
+  if (coords) *coords = r->d_coords;
+  if (mode_stride) *mode_stride = r->cap;
+  if (values) *values = r->d_vals;
+  return FCC_OK;
+}
+
+int fcc_result_copy_to_host(const fcc_result *r, int32_t *coords, int64_t stride_nnz,
+                            int64_t stride_mode, double *values) {
+  if (!r || !r->ctx) return FCC_ERR_ARG;
+  fcc_ctx *ctx = r->ctx;
+  return guarded(ctx, [&] {
+    const int64_t n = r->nnz;
+    if (n == 0) return;
+    cudaStream_t s = ctx->stream;
+    if (values) FCC_CUDA(cudaMemcpyAsync(values, r->d_vals, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    if (coords && r->order > 0) {
+      if (stride_nnz == 1) {
+        for (int m = 0; m < r->order; m++)
+          FCC_CUDA(cudaMemcpyAsync(coords + m * stride_mode, r->d_coords + m * r->cap, sizeof(uint32_t) * n,
+                                   cudaMemcpyDeviceToHost, s));
+        FCC_CUDA(cudaStreamSynchronize(s));
+      } else {
+        std::vector<uint32_t> tmp(size_t(n) * r->order);
+        for (int m = 0; m < r->order; m++)
+          FCC_CUDA(cudaMemcpyAsync(tmp.data() + size_t(m) * n, r->d_coords + m * r->cap, sizeof(uint32_t) * n,
+                                   cudaMemcpyDeviceToHost, s));
+        FCC_CUDA(cudaStreamSynchronize(s));
+        for (int m = 0; m < r->order; m++) {
+          const uint32_t *src = tmp.data() + size_t(m) * n;
+          int32_t *dst = coords + m * stride_mode;
+          for (int64_t i = 0; i < n; i++) dst[i * stride_nnz] = int32_t(src[i]);
+        }
+      }
+    }
+    FCC_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int fcc_result_free(fcc_result *r) {
+  if (!r) return FCC_ERR_ARG;
+  if (r->ctx) {
+    cudaSetDevice(r->ctx->device);
+    if (r->d_vals) cudaFreeAsync(r->d_vals, r->ctx->stream);
+    if (r->d_coords) cudaFreeAsync(r->d_coords, r->ctx->stream);
+  }
+  delete r;
+  return FCC_OK;
+}
+
+int fcc_last_timings(const fcc_ctx *ctx, double *ms, int32_t n) {
+  if (!ctx || !ms || n < 0) return FCC_ERR_ARG;
+  for (int i = 0; i < n && i < FCC_NUM_PHASES; i++) ms[i] = ctx->phase_ms[i];
+  return FCC_OK;
+}
+
+}  // extern "C"

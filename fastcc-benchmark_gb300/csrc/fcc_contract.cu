@@ -1,0 +1,1068 @@
+// The GB300 contraction pipeline behind fcc_contract (include/fastcc_gpu.h),
+// the device replacement of Tensor<DT>::fastcc_multiply (contract.hpp:824-912).
+//
+// Reference step                                  -> here
+//  TileIndexedTensor over B (index_tensors.hpp:506-547): per tile, hash map
+//    contraction key -> (external % T, value)     -> k_linearize + radix sort of
+//    B by 64-bit contraction key + segment build (ukey / segbeg): CSF-style
+//    segments, one per distinct key, in HBM
+//  TileIndexedTensor over A                       -> radix sort of A by its
+//    external (row) index; each A nonzero looks up its B segment once
+//    (k_lookup) instead of once per B tile (contract.hpp:887)
+//  tile-pair loop (contract.hpp:876-897)          -> output tiles of TL A rows
+//    x the whole B external span; a tile's multiply-adds are cut into work
+//    items of at most `products_per_item`, scheduled dynamically over
+//    persistent CTAs
+//  TileAccumulator (index_tensors.hpp:994-1060)   -> k_contract_dense: the tile
+//    lives in shared memory as doubles plus a touched bitmask; drain emits
+//    every touched position (exact zero sums included)
+//  TileAccumulatorMap (index_tensors.hpp:843-883) -> k_contract_hash: shared-
+//    memory open addressing, for B external spans too wide for a dense tile
+//  drain + ListTensor push/concatenate (index_tensors.hpp:90-125,1039-1060)
+//    -> block prefix sums reserve an output range with one atomic per tile;
+//    warps write coordinates (SoA, uint32) and values coalesced
+//  tiles cut into several items                   -> partial tiles are added
+//    into a global dense tile or a global per-tile hash region (FP64 atomics)
+//    and drained by k_merge_*.
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <type_traits>
+
+#include "fcc_internal.cuh"
+
+namespace fcc {
+
+struct LinSpec {
+  int order, n_ext, n_ctr;
+  int ext_mode[FCC_MAX_ORDER];
+  int ctr_mode[FCC_MAX_ORDER];
+  u64 ext_radix[FCC_MAX_ORDER];
+  u64 ctr_radix[FCC_MAX_ORDER];
+  int32_t max_index[FCC_MAX_ORDER];
+};
+
+struct Decode {
+  int na, nb;
+  int narrow;  // every radix and both spans < 2^32
+  u64 ra[FCC_MAX_ORDER], rb[FCC_MAX_ORDER];
+};
+
+struct Out {
+  u32 *coords;  // SoA, mode m at coords[m * stride]
+  i64 stride;
+  double *vals;
+  u64 cap;
+  u64 *cursor;
+};
+
+struct Item {
+  u64 p0, p1;
+  u32 tile, pad;
+};
+
+// ------------------------------------------------------------ helpers ----
+
+__device__ __forceinline__ u32 warp_incl_u32(u32 x) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    u32 y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  return x;
+}
+
+__device__ __forceinline__ u32 hash_slot(u64 key) {
+  return u32((key * 0x9E3779B97F4A7C15ull) >> 32) ^ u32(key >> 29);
+}
+
+__device__ __forceinline__ void emit(const Out &o, const Decode &d, u64 idx, u64 row, u64 col,
+                                     double v) {
+  u32 *c = o.coords;
+  if (d.narrow) {
+    u32 r = u32(row);
+    for (int e = d.na - 1; e > 0; --e) {
+      u32 rad = u32(d.ra[e]), q = r / rad;
+      c[e * o.stride + idx] = r - q * rad;
+      r = q;
+    }
+    if (d.na > 0) c[idx] = r;
+    u32 s = u32(col);
+    for (int e = d.nb - 1; e > 0; --e) {
+      u32 rad = u32(d.rb[e]), q = s / rad;
+      c[(d.na + e) * o.stride + idx] = s - q * rad;
+      s = q;
+    }
+    if (d.nb > 0) c[d.na * o.stride + idx] = s;
+  } else {
+    u64 r = row;
+    for (int e = d.na - 1; e > 0; --e) {
+      u64 q = r / d.ra[e];
+      c[e * o.stride + idx] = u32(r - q * d.ra[e]);
+      r = q;
+    }
+    if (d.na > 0) c[idx] = u32(r);
+    u64 s = col;
+    for (int e = d.nb - 1; e > 0; --e) {
+      u64 q = s / d.rb[e];
+      c[(d.na + e) * o.stride + idx] = u32(s - q * d.rb[e]);
+      s = q;
+    }
+    if (d.nb > 0) c[d.na * o.stride + idx] = u32(s);
+  }
+  o.vals[idx] = v;
+}
+
+// Reserves `total` outputs with one atomic; ~0 marks "over capacity".
+__device__ __forceinline__ u64 reserve(const Out &o, u64 total, u32 *err) {
+  if (total == 0) return 0;
+  u64 b = atomicAdd(reinterpret_cast<unsigned long long *>(o.cursor), (unsigned long long)total);
+  if (b + total > o.cap) {
+    atomicOr(err, ERRB_OVERFLOW);
+    return ~0ull;
+  }
+  return b;
+}
+
+// ------------------------------------------------------ index building ----
+
+__global__ void k_linearize(const int32_t *__restrict__ coords, i64 sn, i64 sm, i64 nnz, LinSpec s,
+                            u64 *__restrict__ ext, u64 *__restrict__ key, u32 *__restrict__ iota,
+                            u32 *err) {
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < nnz; i += i64(gridDim.x) * blockDim.x) {
+    const int32_t *c = coords + i * sn;
+    bool bad = false;
+    u64 e = 0, k = 0;
+    for (int q = 0; q < s.n_ext; q++) {
+      int32_t v = c[i64(s.ext_mode[q]) * sm];
+      bad |= v < 0 || v > s.max_index[s.ext_mode[q]];
+      e = e * s.ext_radix[q] + u64(u32(v));
+    }
+    for (int q = 0; q < s.n_ctr; q++) {
+      int32_t v = c[i64(s.ctr_mode[q]) * sm];
+      bad |= v < 0 || v > s.max_index[s.ctr_mode[q]];
+      k = k * s.ctr_radix[q] + u64(u32(v));
+    }
+    if (bad) atomicOr(err, ERRB_COORD);
+    ext[i] = e;
+    key[i] = k;
+    iota[i] = u32(i);
+  }
+}
+
+template <class ColT>
+__global__ void k_gather_b(const u32 *__restrict__ perm, const u64 *__restrict__ ext,
+                           const double *__restrict__ vals, i64 n, ColT *__restrict__ col,
+                           double *__restrict__ val) {
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
+    u32 p = perm[i];
+    col[i] = ColT(ext[p]);
+    val[i] = vals[p];
+  }
+}
+
+__global__ void k_flag_change(const u64 *__restrict__ key, i64 n, u32 *__restrict__ flag) {
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x)
+    flag[i] = (i == 0 || key[i] != key[i - 1]) ? 1u : 0u;
+}
+
+__global__ void k_seg_write(const u64 *__restrict__ key, const u32 *__restrict__ flag,
+                            const u32 *__restrict__ idx, i64 n, u64 *__restrict__ ukey,
+                            u32 *__restrict__ segbeg) {
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
+    if (flag[i]) {
+      ukey[idx[i]] = key[i];
+      segbeg[idx[i]] = u32(i);
+    }
+    if (i == n - 1) segbeg[idx[i] + flag[i]] = u32(n);
+  }
+}
+
+// For each A nonzero (in row-sorted order) find the B segment of its key.
+__global__ void k_lookup(const u64 *__restrict__ keyA, const u32 *__restrict__ permA, i64 n,
+                         const u64 *__restrict__ ukey, const u32 *__restrict__ nseg_p,
+                         u32 *__restrict__ seg, u32 *__restrict__ flag) {
+  const u32 nseg = *nseg_p;
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
+    const u64 k = keyA[permA[i]];
+    u32 lo = 0, hi = nseg;  // first index with ukey >= k
+    while (lo < hi) {
+      u32 mid = (lo + hi) >> 1;
+      if (ukey[mid] < k) lo = mid + 1; else hi = mid;
+    }
+    bool hit = lo < nseg && ukey[lo] == k;
+    seg[i] = lo;
+    flag[i] = hit ? 1u : 0u;
+  }
+}
+
+__global__ void k_compact_a(const u32 *__restrict__ flag, const u32 *__restrict__ idx, i64 n,
+                            const u32 *__restrict__ permA, const u64 *__restrict__ rowSorted,
+                            const u32 *__restrict__ segTmp, const double *__restrict__ valsA,
+                            const u32 *__restrict__ segbeg, u64 *__restrict__ rowA,
+                            u32 *__restrict__ segA, double *__restrict__ valA, u32 *__restrict__ len) {
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
+    if (!flag[i]) continue;
+    const u32 d = idx[i], s = segTmp[i];
+    rowA[d] = rowSorted[i];
+    segA[d] = s;
+    valA[d] = valsA[permA[i]];
+    len[d] = segbeg[s + 1] - segbeg[s];
+  }
+}
+
+// ------------------------------------------------------------ planning ----
+
+__global__ void k_tile_flags(const u64 *__restrict__ rowA, i64 n, u64 TL, u32 *__restrict__ flag) {
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x)
+    flag[i] = (i == 0 || rowA[i] / TL != rowA[i - 1] / TL) ? 1u : 0u;
+}
+
+__global__ void k_tile_write(const u64 *__restrict__ rowA, const u32 *__restrict__ flag,
+                             const u32 *__restrict__ idx, i64 n, u64 TL, u64 *__restrict__ row0,
+                             u32 *__restrict__ abeg) {
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
+    if (flag[i]) {
+      row0[idx[i]] = (rowA[i] / TL) * TL;
+      abeg[idx[i]] = u32(i);
+    }
+    if (i == n - 1) abeg[idx[i] + flag[i]] = u32(n);
+  }
+}
+
+// Per tile: work items, split flag, output bound and (hash) region size.
+__global__ void k_tile_items(const u32 *__restrict__ ntiles_p, i64 nmax, const u32 *__restrict__ abeg,
+                             const u64 *__restrict__ P, u64 pmax, u64 area, int hash_mode,
+                             u32 *__restrict__ nitems, u32 *__restrict__ split, u64 *__restrict__ cap,
+                             u64 *__restrict__ hsz) {
+  const u32 ntiles = *ntiles_p;
+  for (i64 t = i64(blockIdx.x) * blockDim.x + threadIdx.x; t < nmax; t += i64(gridDim.x) * blockDim.x) {
+    if (t >= ntiles) {
+      nitems[t] = 0; split[t] = 0; cap[t] = 0; hsz[t] = 0;
+      continue;
+    }
+    const u64 prod = P[abeg[t + 1]] - P[abeg[t]];
+    const u64 items = (prod + pmax - 1) / pmax;
+    const u64 bound = prod < area ? prod : area;
+    nitems[t] = u32(items);
+    split[t] = items > 1 ? 1u : 0u;
+    cap[t] = bound;
+    u64 h = 0;
+    if (hash_mode && items > 1) {
+      h = 64;
+      while (h < 2 * bound) h <<= 1;
+    }
+    hsz[t] = h;
+  }
+}
+
+__global__ void k_item_write(const u32 *__restrict__ ntiles_p, const u32 *__restrict__ abeg,
+                             const u64 *__restrict__ P, const u32 *__restrict__ item_off, u64 pmax,
+                             Item *__restrict__ items, const u32 *__restrict__ split,
+                             const u32 *__restrict__ split_idx, int *__restrict__ split_of_tile,
+                             u32 *__restrict__ split_tiles) {
+  const u32 ntiles = *ntiles_p;
+  for (i64 t = i64(blockIdx.x) * blockDim.x + threadIdx.x; t < ntiles; t += i64(gridDim.x) * blockDim.x) {
+    const u64 b = P[abeg[t]], e = P[abeg[t + 1]];
+    u32 o = item_off[t];
+    for (u64 p = b; p < e; p += pmax) {
+      Item it;
+      it.p0 = p;
+      it.p1 = (e - p > pmax) ? p + pmax : e;
+      it.tile = u32(t);
+      it.pad = 0;
+      items[o++] = it;
+    }
+    if (split[t]) {
+      split_of_tile[t] = int(split_idx[t]);
+      split_tiles[split_idx[t]] = u32(t);
+    } else {
+      split_of_tile[t] = -1;
+    }
+  }
+}
+
+// --------------------------------------------------------- dense tiles ----
+
+constexpr int kTileThreads = 512;
+constexpr u32 kUnit = 256;  // multiply-adds per warp work unit
+
+struct DenseArgs {
+  const Item *items;
+  u32 nitems;
+  u32 *counter;
+  const u64 *tile_row0;
+  const u32 *tile_abeg;
+  const int *split_of_tile;
+  const u32 *split_tiles;
+  u32 nsplit;
+  const u64 *P;
+  const u64 *rowA;
+  const u32 *segA;
+  const double *valA;
+  const u32 *segbeg;
+  const u32 *colB;
+  const double *valB;
+  u32 LB, area, words;
+  double *gacc;
+  u32 *gmask;
+  Out out;
+  Decode dec;
+  u32 *err;
+};
+
+// Emits every set bit of `mask` (the touched positions of a dense tile) with
+// its accumulated value, coalesced per warp, and clears both.
+__device__ void drain_dense(double *acc, u32 *mask, u32 words, u32 LB, u64 row0, const Out &out,
+                            const Decode &dec, u32 *err, u32 *s_wcnt, u64 *s_base) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const u32 wpw = (words + nwarps - 1) / nwarps;
+  const u32 w0 = min(words, u32(warp) * wpw), w1 = min(words, w0 + wpw);
+  u32 c = 0;
+  for (u32 w = w0 + lane; w < w1; w += 32) c += __popc(mask[w]);
+  c = __reduce_add_sync(kFull, c);
+  if (lane == 0) s_wcnt[warp] = c;
+  __syncthreads();
+  if (tid == 0) {
+    u32 run = 0;
+    for (int w = 0; w < nwarps; w++) {
+      u32 x = s_wcnt[w];
+      s_wcnt[w] = run;
+      run += x;
+    }
+    *s_base = reserve(out, run, err);
+  }
+  __syncthreads();
+  const u64 base = *s_base;
+  const bool write = base != ~0ull;
+  u64 run = write ? base + s_wcnt[warp] : 0;
+  for (u32 cw = w0; cw < w1; cw += 32) {
+    const u32 w = cw + lane;
+    const u32 word = w < w1 ? mask[w] : 0u;
+    const u32 incl = warp_incl_u32(__popc(word));
+    const u32 tot = __shfl_sync(kFull, incl, 31);
+    for (u32 kk = 0; kk < tot; kk += 32) {
+      const u32 k = kk + lane;
+      u32 lo = 0;
+#pragma unroll
+      for (u32 step = 16; step >= 1; step >>= 1) {
+        u32 v = __shfl_sync(kFull, incl, lo + step - 1);
+        if (v <= k) lo += step;
+      }
+      const u32 wsrc = __shfl_sync(kFull, word, lo);
+      const u32 isrc = __shfl_sync(kFull, incl, lo);
+      if (k < tot) {
+        const u32 nth = k - (isrc - __popc(wsrc));
+        const u32 bit = __fns(wsrc, 0, int(nth) + 1);
+        const u32 pos = (cw + lo) * 32 + bit;
+        const double v = acc[pos];
+        acc[pos] = 0.0;
+        if (write) emit(out, dec, run + k, row0 + pos / LB, pos % LB, v);
+      }
+    }
+    if (w < w1) mask[w] = 0u;
+    run += tot;
+  }
+}
+
+__device__ void flush_dense(double *acc, u32 *mask, u32 words, double *gacc, u32 *gmask) {
+  for (u32 w = threadIdx.x; w < words; w += blockDim.x) {
+    u32 word = mask[w];
+    if (!word) continue;
+    atomicOr(&gmask[w], word);
+    mask[w] = 0u;
+    while (word) {
+      const u32 pos = w * 32 + u32(__ffs(word) - 1);
+      word &= word - 1;
+      atomicAdd(&gacc[pos], acc[pos]);
+      acc[pos] = 0.0;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kTileThreads, 1) k_contract_dense(DenseArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  double *acc = reinterpret_cast<double *>(smem);
+  u32 *mask = reinterpret_cast<u32 *>(acc + a.area);
+  __shared__ u32 s_item;
+  __shared__ u32 s_wcnt[32];
+  __shared__ u64 s_base;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  for (u32 i = tid; i < a.area; i += blockDim.x) acc[i] = 0.0;
+  for (u32 i = tid; i < a.words; i += blockDim.x) mask[i] = 0u;
+  __syncthreads();
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(a.counter, 1u);
+    __syncthreads();
+    const u32 it = s_item;
+    if (it >= a.nitems) break;
+    const Item item = a.items[it];
+    const u32 t = item.tile;
+    const u32 alo = a.tile_abeg[t], ahi = a.tile_abeg[t + 1];
+    const u64 row0 = a.tile_row0[t];
+    const u64 nunits = (item.p1 - item.p0 + kUnit - 1) / kUnit;
+    for (u64 u = warp; u < nunits; u += nwarps) {
+      const u64 q0 = item.p0 + u * kUnit;
+      const u64 q1 = min(q0 + kUnit, item.p1);
+      u32 lo = alo, hi = ahi;  // P[lo] <= q0 < P[hi]
+      while (hi - lo > 1) {
+        const u32 mid = (lo + hi) >> 1;
+        if (a.P[mid] <= q0) lo = mid; else hi = mid;
+      }
+      u32 ai = lo;
+      u64 pa = a.P[ai];
+      while (pa < q1) {
+        const u64 pe = a.P[ai + 1];
+        const u64 s0 = max(q0, pa), s1 = min(q1, pe);
+        const double va = a.valA[ai];
+        const u32 base = u32(a.rowA[ai] - row0) * a.LB;
+        const u32 sb = a.segbeg[a.segA[ai]] + u32(s0 - pa);
+        const u32 cnt = u32(s1 - s0);
+        for (u32 o = lane; o < cnt; o += 32) {
+          const u32 b = sb + o;
+          const u32 pos = base + a.colB[b];
+          atomicAdd(&acc[pos], va * a.valB[b]);
+          atomicOr(&mask[pos >> 5], 1u << (pos & 31));
+        }
+        ++ai;
+        pa = pe;
+      }
+    }
+    __syncthreads();
+    const int sidx = a.split_of_tile[t];
+    if (sidx < 0)
+      drain_dense(acc, mask, a.words, a.LB, row0, a.out, a.dec, a.err, s_wcnt, &s_base);
+    else
+      flush_dense(acc, mask, a.words, a.gacc + u64(sidx) * a.area, a.gmask + u64(sidx) * a.words);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_merge_dense(DenseArgs a) {
+  __shared__ u32 s_wcnt[32];
+  __shared__ u64 s_base;
+  for (u32 s = blockIdx.x; s < a.nsplit; s += gridDim.x) {
+    const u64 row0 = a.tile_row0[a.split_tiles[s]];
+    drain_dense(a.gacc + u64(s) * a.area, a.gmask + u64(s) * a.words, a.words, a.LB, row0, a.out,
+                a.dec, a.err, s_wcnt, &s_base);
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------- hash tiles ----
+
+template <class ColT>
+struct HashArgs {
+  const Item *items;
+  u32 nitems;
+  u32 *counter;
+  const u64 *tile_row0;
+  const u32 *tile_abeg;
+  const int *split_of_tile;
+  const u32 *split_tiles;
+  u32 nsplit;
+  const u64 *P;
+  const u64 *rowA;
+  const u32 *segA;
+  const double *valA;
+  const u32 *segbeg;
+  const ColT *colB;
+  const double *valB;
+  u64 LB;
+  u32 TL;
+  u32 slots;  // shared-memory slots (power of two)
+  const u64 *hoff;  // per tile: first slot of its global region (split tiles)
+  const u64 *hsz;   // per tile: global region size, a power of two (split tiles)
+  u64 *gkeys;
+  double *gvals;
+  Out out;
+  Decode dec;
+  u32 *err;
+};
+
+// Emits occupied slots of an open-addressing table, coalesced per warp, and
+// resets them.
+__device__ void drain_hash(u64 *keys, double *vals, u64 nslots, u64 LB, u32 TL, u64 row0,
+                           const Out &out, const Decode &dec, u32 *err, u32 *s_wcnt, u64 *s_base) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const u64 spw = ((nslots + nwarps - 1) / nwarps + 31) & ~u64(31);
+  const u64 s0 = min(nslots, u64(warp) * spw), s1 = min(nslots, s0 + spw);
+  u32 c = 0;
+  for (u64 s = s0 + lane; s < s1; s += 32) c += keys[s] != kEmptyKey ? 1u : 0u;
+  c = __reduce_add_sync(kFull, c);
+  if (lane == 0) s_wcnt[warp] = c;
+  __syncthreads();
+  if (tid == 0) {
+    u32 run = 0;
+    for (int w = 0; w < nwarps; w++) {
+      u32 x = s_wcnt[w];
+      s_wcnt[w] = run;
+      run += x;
+    }
+    *s_base = reserve(out, run, err);
+  }
+  __syncthreads();
+  const u64 base = *s_base;
+  const bool write = base != ~0ull;
+  u64 run = write ? base + s_wcnt[warp] : 0;
+  const u32 lt = (1u << lane) - 1u;
+  for (u64 cs = s0; cs < s1; cs += 32) {
+    const u64 s = cs + lane;
+    const u64 key = s < s1 ? keys[s] : kEmptyKey;
+    const bool occ = key != kEmptyKey;
+    const u32 bal = __ballot_sync(kFull, occ);
+    if (occ) {
+      const double v = vals[s];
+      u64 row = row0, col = key;
+      if (TL > 1) { row = row0 + key / LB; col = key % LB; }
+      if (write) emit(out, dec, run + __popc(bal & lt), row, col, v);
+    }
+    if (s < s1) { keys[s] = kEmptyKey; vals[s] = 0.0; }
+    run += __popc(bal);
+  }
+}
+
+__device__ __forceinline__ void global_hash_add(u64 *gk, double *gv, u64 hs, u64 key, double v, u32 *err) {
+  u64 h = u64(hash_slot(key)) & (hs - 1);
+  for (u64 probe = 0; probe < hs; probe++) {
+    u64 cur = atomicCAS(reinterpret_cast<unsigned long long *>(&gk[h]), kEmptyKey, key);
+    if (cur == kEmptyKey || cur == key) {
+      atomicAdd(&gv[h], v);
+      return;
+    }
+    h = (h + 1) & (hs - 1);
+  }
+  atomicOr(err, ERRB_HASH);
+}
+
+template <class ColT>
+__global__ void __launch_bounds__(kTileThreads, 1) k_contract_hash(HashArgs<ColT> a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  u64 *hk = reinterpret_cast<u64 *>(smem);
+  double *hv = reinterpret_cast<double *>(hk + a.slots);
+  __shared__ u32 s_item;
+  __shared__ u32 s_wcnt[32];
+  __shared__ u64 s_base;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  for (u32 i = tid; i < a.slots; i += blockDim.x) { hk[i] = kEmptyKey; hv[i] = 0.0; }
+  __syncthreads();
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(a.counter, 1u);
+    __syncthreads();
+    const u32 it = s_item;
+    if (it >= a.nitems) break;
+    const Item item = a.items[it];
+    const u32 t = item.tile;
+    const u32 alo = a.tile_abeg[t], ahi = a.tile_abeg[t + 1];
+    const u64 row0 = a.tile_row0[t];
+    const u64 np = item.p1 - item.p0;
+    u32 hsl = 64;
+    while (u64(hsl) < 2 * np && hsl < a.slots) hsl <<= 1;
+    const u32 hmask = hsl - 1;
+    const u64 nunits = (np + kUnit - 1) / kUnit;
+    for (u64 u = warp; u < nunits; u += nwarps) {
+      const u64 q0 = item.p0 + u * kUnit;
+      const u64 q1 = min(q0 + kUnit, item.p1);
+      u32 lo = alo, hi = ahi;
+      while (hi - lo > 1) {
+        const u32 mid = (lo + hi) >> 1;
+        if (a.P[mid] <= q0) lo = mid; else hi = mid;
+      }
+      u32 ai = lo;
+      u64 pa = a.P[ai];
+      while (pa < q1) {
+        const u64 pe = a.P[ai + 1];
+        const u64 s0 = max(q0, pa), s1 = min(q1, pe);
+        const double va = a.valA[ai];
+        const u64 kbase = (a.rowA[ai] - row0) * a.LB;
+        const u32 sb = a.segbeg[a.segA[ai]] + u32(s0 - pa);
+        const u32 cnt = u32(s1 - s0);
+        for (u32 o = lane; o < cnt; o += 32) {
+          const u32 b = sb + o;
+          const u64 key = kbase + u64(a.colB[b]);
+          const double p = va * a.valB[b];
+          u32 h = hash_slot(key) & hmask;
+          u32 probe = 0;
+          for (;; ++probe) {
+            if (probe > hmask) { atomicOr(a.err, ERRB_HASH); break; }
+            const u64 cur = *reinterpret_cast<volatile u64 *>(&hk[h]);
+            if (cur == key) break;
+            if (cur == kEmptyKey) {
+              const u64 old = atomicCAS(reinterpret_cast<unsigned long long *>(&hk[h]), kEmptyKey, key);
+              if (old == kEmptyKey || old == key) break;
+            }
+            h = (h + 1) & hmask;
+          }
+          if (probe <= hmask) atomicAdd(&hv[h], p);
+        }
+        ++ai;
+        pa = pe;
+      }
+    }
+    __syncthreads();
+    const int sidx = a.split_of_tile[t];
+    if (sidx < 0) {
+      drain_hash(hk, hv, hsl, a.LB, a.TL, row0, a.out, a.dec, a.err, s_wcnt, &s_base);
+    } else {
+      const u64 off = a.hoff[t], hs = a.hsz[t];
+      for (u32 s = tid; s < hsl; s += blockDim.x) {
+        const u64 key = hk[s];
+        if (key != kEmptyKey) {
+          global_hash_add(a.gkeys + off, a.gvals + off, hs, key, hv[s], a.err);
+          hk[s] = kEmptyKey;
+          hv[s] = 0.0;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <class ColT>
+__global__ void __launch_bounds__(kTileThreads) k_merge_hash(HashArgs<ColT> a) {
+  __shared__ u32 s_wcnt[32];
+  __shared__ u64 s_base;
+  for (u32 s = blockIdx.x; s < a.nsplit; s += gridDim.x) {
+    const u32 t = a.split_tiles[s];
+    const u64 off = a.hoff[t];
+    drain_hash(a.gkeys + off, a.gvals + off, a.hsz[t], a.LB, a.TL, a.tile_row0[t], a.out, a.dec,
+               a.err, s_wcnt, &s_base);
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------- host pipeline ----
+
+namespace {
+
+struct Side {
+  int order = 0;
+  i64 nnz = 0;
+  LinSpec lin{};
+  u64 span = 1;      // external index space
+  u64 keyspace = 1;  // contraction key space
+  const int32_t *coords = nullptr;
+  i64 sn = 0, sm = 0;
+  const double *vals = nullptr;
+};
+
+u64 mul_checked(u64 a, u64 b, const char *what) {
+  unsigned __int128 p = (unsigned __int128)a * b;
+  if (p > (unsigned __int128)(~0ull) - 1)
+    throw Error{FCC_ERR_OVERFLOW, std::string(what) + " exceeds 64 bits"};
+  return u64(p);
+}
+
+void check_tensor(const fcc_tensor *t, const char *name) {
+  std::string n(name);
+  if (!t) throw Error{FCC_ERR_ARG, n + " is NULL"};
+  if (t->order < 0 || t->order > FCC_MAX_ORDER) throw Error{FCC_ERR_ARG, n + ": order must be in 0..8"};
+  if (t->nnz < 0 || t->nnz > 0x7FFFFFFFll) throw Error{FCC_ERR_ARG, n + ": nnz must be in 0..2^31-1"};
+  if (t->order > 0 && !t->max_index) throw Error{FCC_ERR_ARG, n + ": max_index is NULL"};
+  for (int m = 0; m < t->order; m++)
+    if (t->max_index[m] < 0) throw Error{FCC_ERR_ARG, n + ": negative max_index"};
+  if (t->nnz > 0 && ((t->order > 0 && !t->coords) || !t->values))
+    throw Error{FCC_ERR_ARG, n + ": coords or values is NULL"};
+  if (t->location != FCC_HOST && t->location != FCC_DEVICE) throw Error{FCC_ERR_ARG, n + ": bad location"};
+  if (t->nnz > 0 && t->order > 0 && (t->stride_nnz < 0 || t->stride_mode < 0))
+    throw Error{FCC_ERR_ARG, n + ": negative stride"};
+}
+
+void check_ctr(const fcc_tensor *t, const int32_t *ctr, int k, const char *name) {
+  if (k > 0 && !ctr) throw Error{FCC_ERR_ARG, std::string(name) + " is NULL"};
+  for (int i = 0; i < k; i++) {
+    if (ctr[i] < 0 || ctr[i] >= t->order)
+      throw Error{FCC_ERR_ARG, std::string(name) + ": contracted mode out of range"};
+    for (int j = 0; j < i; j++)
+      if (ctr[j] == ctr[i]) throw Error{FCC_ERR_ARG, std::string(name) + ": repeated contracted mode"};
+  }
+}
+
+void build_side(const fcc_tensor *t, const int32_t *ctr, const int32_t *other_max,
+                const int32_t *other_ctr, int k, int radix_mode, Side &s) {
+  s.order = t->order;
+  s.nnz = t->nnz;
+  LinSpec &l = s.lin;
+  std::memset(&l, 0, sizeof(l));
+  l.order = t->order;
+  bool is_ctr[FCC_MAX_ORDER] = {};
+  for (int i = 0; i < k; i++) is_ctr[ctr[i]] = true;
+  for (int m = 0; m < t->order; m++) {
+    l.max_index[m] = t->max_index[m];
+    if (!is_ctr[m]) {
+      l.ext_mode[l.n_ext] = m;
+      l.ext_radix[l.n_ext] = u64(t->max_index[m]) + 1;
+      s.span = mul_checked(s.span, l.ext_radix[l.n_ext], "external index space");
+      l.n_ext++;
+    }
+  }
+  l.n_ctr = k;
+  for (int i = 0; i < k; i++) {
+    u64 r = u64(t->max_index[ctr[i]]) + 1;
+    if (radix_mode == FCC_RADIX_SHARED) r = std::max<u64>(r, u64(other_max[other_ctr[i]]) + 1);
+    l.ctr_mode[i] = ctr[i];
+    l.ctr_radix[i] = r;
+    s.keyspace = mul_checked(s.keyspace, r, "contraction key space");
+  }
+}
+
+const int32_t *upload_coords(fcc_ctx *ctx, const fcc_tensor *t) {
+  if (t->nnz == 0 || t->order == 0 || t->location == FCC_DEVICE) return t->coords;
+  const i64 extent = (t->nnz - 1) * t->stride_nnz + i64(t->order - 1) * t->stride_mode + 1;
+  int32_t *d = ctx->arena.get_n<int32_t>(size_t(extent));
+  FCC_CUDA(cudaMemcpyAsync(d, t->coords, sizeof(int32_t) * size_t(extent), cudaMemcpyHostToDevice,
+                           ctx->stream));
+  return d;
+}
+
+const double *upload_values(fcc_ctx *ctx, const fcc_tensor *t) {
+  if (t->nnz == 0 || t->location == FCC_DEVICE) return t->values;
+  double *d = ctx->arena.get_n<double>(size_t(t->nnz));
+  FCC_CUDA(cudaMemcpyAsync(d, t->values, sizeof(double) * size_t(t->nnz), cudaMemcpyHostToDevice,
+                           ctx->stream));
+  return d;
+}
+
+// Device scalar block: slot numbers in a u64 array.
+enum Scalar { S_NSEG = 0, S_NA2, S_NTILES, S_NITEMS, S_NSPLIT, S_CAP, S_HASH, S_CURSOR, S_COUNTER,
+              S_PTOTAL, S_ERR, S_COUNT };
+
+// Copies the scalar block and the error word to pinned host memory, waits,
+// and raises the error bits that are not recoverable.
+void read_scalars(fcc_ctx *ctx, u64 *d_sc) {
+  FCC_CUDA(cudaMemcpyAsync(d_sc + S_ERR, ctx->d_err, sizeof(u32), cudaMemcpyDeviceToDevice, ctx->stream));
+  FCC_CUDA(cudaMemcpyAsync(ctx->h_scalars, d_sc, sizeof(u64) * S_COUNT, cudaMemcpyDeviceToHost, ctx->stream));
+  FCC_CUDA(cudaStreamSynchronize(ctx->stream));
+  const u32 err = u32(ctx->h_scalars[S_ERR]);
+  if (err & ERRB_COORD) throw Error{FCC_ERR_ARG, "a coordinate lies outside [0, max_index]"};
+  if (err & ERRB_HASH) throw Error{FCC_ERR_HASH_FULL, "hash accumulator probe limit reached"};
+  if (err & ERRB_INTERNAL) throw Error{FCC_ERR_CUDA, "internal plan invariant violated"};
+}
+
+u32 scalar32(fcc_ctx *ctx, int s) { return u32(ctx->h_scalars[s] & 0xFFFFFFFFu); }
+
+int grid_tiles(fcc_ctx *ctx, const void *kernel, size_t smem, u32 nitems) {
+  int per_sm = 0;
+  FCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTileThreads, smem));
+  if (per_sm < 1) throw Error{FCC_ERR_CUDA, "tile kernel does not fit on an SM"};
+  i64 g = i64(per_sm) * ctx->num_sms;
+  if (g > i64(nitems)) g = nitems;
+  return int(std::max<i64>(g, 1));
+}
+
+void free_result_buffers(fcc_result *r, cudaStream_t s) {
+  if (r->d_vals) cudaFreeAsync(r->d_vals, s);
+  if (r->d_coords) cudaFreeAsync(r->d_coords, s);
+  r->d_vals = nullptr;
+  r->d_coords = nullptr;
+}
+
+struct Timing {
+  fcc_ctx *ctx;
+  bool on;
+  int next = 0;
+  void mark(int slot) {  // records every slot up to `slot`
+    if (!on) return;
+    while (next <= slot) FCC_CUDA(cudaEventRecord(ctx->ev[next++], ctx->stream));
+  }
+  void finish() {
+    if (!on) return;
+    mark(5);
+    FCC_CUDA(cudaEventSynchronize(ctx->ev[5]));
+    const int map[FCC_NUM_PHASES][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 4}, {4, 5}, {0, 5}};
+    for (int p = 0; p < FCC_NUM_PHASES; p++) {
+      float ms = 0;
+      FCC_CUDA(cudaEventElapsedTime(&ms, ctx->ev[map[p][0]], ctx->ev[map[p][1]]));
+      ctx->phase_ms[p] = ms;
+    }
+  }
+};
+
+}  // namespace
+
+// The whole contraction. count_only stops after the segment lookup and
+// returns the multiply-add count in *products.
+void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+              const int32_t *ctrB, int k, const fcc_options &opt, fcc_result **out, i64 *products,
+              bool count_only) {
+  check_tensor(A, "A");
+  check_tensor(B, "B");
+  if (k < 0 || k > A->order || k > B->order) throw Error{FCC_ERR_ARG, "bad number of contracted modes"};
+  check_ctr(A, ctrA, k, "ctrA");
+  check_ctr(B, ctrB, k, "ctrB");
+  if (opt.radix_mode != FCC_RADIX_PER_OPERAND && opt.radix_mode != FCC_RADIX_SHARED)
+    throw Error{FCC_ERR_ARG, "bad radix_mode"};
+  if (opt.accumulator < FCC_ACC_AUTO || opt.accumulator > FCC_ACC_HASH) throw Error{FCC_ERR_ARG, "bad accumulator"};
+  if (opt.rows_per_tile < 0 || opt.products_per_item < 0 || opt.dense_cap < 0 || opt.hash_slots < 0 ||
+      opt.capacity_hint < 0)
+    throw Error{FCC_ERR_ARG, "negative tuning option"};
+
+  Side sa, sb;
+  build_side(A, ctrA, B->max_index, ctrB, k, opt.radix_mode, sa);
+  build_side(B, ctrB, A->max_index, ctrA, k, opt.radix_mode, sb);
+  const int out_order = sa.lin.n_ext + sb.lin.n_ext;
+  cudaStream_t st = ctx->stream;
+  Timing tm{ctx, opt.timing != 0};
+  for (int i = 0; i < FCC_NUM_PHASES; i++) ctx->phase_ms[i] = 0;
+
+  std::unique_ptr<fcc_result> res;
+  if (!count_only) {
+    res.reset(new fcc_result());
+    res->order = out_order;
+    res->ctx = ctx;
+  }
+  struct Cleanup {
+    std::unique_ptr<fcc_result> &r;
+    cudaStream_t s;
+    ~Cleanup() { if (r) free_result_buffers(r.get(), s); }
+  } cleanup{res, st};
+
+  ctx->arena.begin(st);
+  tm.mark(0);
+  if (A->nnz == 0 || B->nnz == 0) {
+    if (products) *products = 0;
+    tm.finish();
+    if (out) *out = res.release();
+    return;
+  }
+
+  // ---- upload (host operands) ----
+  Arena &ar = ctx->arena;
+  sa.coords = upload_coords(ctx, A);
+  sa.sn = A->stride_nnz;
+  sa.sm = A->stride_mode;
+  sa.vals = upload_values(ctx, A);
+  sb.coords = upload_coords(ctx, B);
+  sb.sn = B->stride_nnz;
+  sb.sm = B->stride_mode;
+  sb.vals = upload_values(ctx, B);
+  tm.mark(1);
+
+  const i64 nA = sa.nnz, nB = sb.nnz;
+  u64 *d_sc = ar.get_n<u64>(S_COUNT);
+  FCC_CUDA(cudaMemsetAsync(d_sc, 0, sizeof(u64) * S_COUNT, st));
+  FCC_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(u32), st));
+  auto sc32 = [&](int s) { return reinterpret_cast<u32 *>(d_sc + s); };
+
+  // ---- index: linearise, sort B by key, segments ----
+  u64 *extA = ar.get_n<u64>(nA), *keyA = ar.get_n<u64>(nA);
+  u32 *permA = ar.get_n<u32>(nA);
+  u64 *extB = ar.get_n<u64>(nB), *keyB = ar.get_n<u64>(nB);
+  u32 *permB = ar.get_n<u32>(nB);
+  k_linearize<<<grid_for(nA, 256), 256, 0, st>>>(sa.coords, sa.sn, sa.sm, nA, sa.lin, extA, keyA, permA, ctx->d_err);
+  FCC_LAUNCH_CHECK();
+  k_linearize<<<grid_for(nB, 256), 256, 0, st>>>(sb.coords, sb.sn, sb.sm, nB, sb.lin, extB, keyB, permB, ctx->d_err);
+  FCC_LAUNCH_CHECK();
+  radix_sort_pairs(keyB, permB, nB, bits_for(sb.keyspace - 1), ar, st);
+
+  const bool colb32 = sb.span <= 0xFFFFFFFFull;
+  double *valB = ar.get_n<double>(nB);
+  void *colB = colb32 ? static_cast<void *>(ar.get_n<u32>(nB)) : static_cast<void *>(ar.get_n<u64>(nB));
+  if (colb32)
+    k_gather_b<u32><<<grid_for(nB, 256), 256, 0, st>>>(permB, extB, sb.vals, nB, static_cast<u32 *>(colB), valB);
+  else
+    k_gather_b<u64><<<grid_for(nB, 256), 256, 0, st>>>(permB, extB, sb.vals, nB, static_cast<u64 *>(colB), valB);
+  FCC_LAUNCH_CHECK();
+  u32 *flagB = ar.get_n<u32>(nB), *idxB = ar.get_n<u32>(nB);
+  k_flag_change<<<grid_for(nB, 256), 256, 0, st>>>(keyB, nB, flagB);
+  FCC_LAUNCH_CHECK();
+  scan_exclusive(flagB, idxB, nB, sc32(S_NSEG), ar, st);
+  u64 *ukey = ar.get_n<u64>(nB);
+  u32 *segbeg = ar.get_n<u32>(nB + 1);
+  k_seg_write<<<grid_for(nB, 256), 256, 0, st>>>(keyB, flagB, idxB, nB, ukey, segbeg);
+  FCC_LAUNCH_CHECK();
+
+  // ---- A: sort by row, look up segments, drop unmatched ----
+  radix_sort_pairs(extA, permA, nA, bits_for(sa.span - 1), ar, st);
+  u32 *segTmp = ar.get_n<u32>(nA), *flagA = ar.get_n<u32>(nA), *idxA = ar.get_n<u32>(nA);
+  k_lookup<<<grid_for(nA, 256), 256, 0, st>>>(keyA, permA, nA, ukey, sc32(S_NSEG), segTmp, flagA);
+  FCC_LAUNCH_CHECK();
+  scan_exclusive(flagA, idxA, nA, sc32(S_NA2), ar, st);
+  u64 *rowA = ar.get_n<u64>(nA);
+  u32 *segA = ar.get_n<u32>(nA), *lenA = ar.get_n<u32>(nA);
+  double *valA = ar.get_n<double>(nA);
+  FCC_CUDA(cudaMemsetAsync(lenA, 0, sizeof(u32) * nA, st));
+  k_compact_a<<<grid_for(nA, 256), 256, 0, st>>>(flagA, idxA, nA, permA, extA, segTmp, sa.vals, segbeg, rowA,
+                                                 segA, valA, lenA);
+  FCC_LAUNCH_CHECK();
+  u64 *P = ar.get_n<u64>(nA + 1);
+  scan_exclusive_wide(lenA, P, nA, P + nA, ar, st);
+  FCC_CUDA(cudaMemcpyAsync(d_sc + S_PTOTAL, P + nA, sizeof(u64), cudaMemcpyDeviceToDevice, st));
+  tm.mark(2);
+
+  read_scalars(ctx, d_sc);
+  const u32 nA2 = scalar32(ctx, S_NA2);
+  const u64 ptotal = ctx->h_scalars[S_PTOTAL];
+  if (products) *products = i64(ptotal);
+  if (count_only) {
+    tm.finish();
+    return;
+  }
+  res->products = i64(ptotal);
+  if (nA2 == 0 || ptotal == 0) {
+    tm.finish();
+    *out = res.release();
+    return;
+  }
+
+  // ---- plan ----
+  const u64 LB = sb.span;
+  const size_t smem_cap = ctx->smem_optin - 1024;
+  const u64 max_dense_area = (u64(smem_cap) * 8) / 65;  // 8 bytes + 1 mask bit per position
+  u64 dense_cap = opt.dense_cap > 0 ? std::min<u64>(u64(opt.dense_cap), max_dense_area) : max_dense_area;
+  bool dense = LB <= dense_cap && opt.accumulator != FCC_ACC_HASH;
+  if (opt.accumulator == FCC_ACC_DENSE && !dense)
+    throw Error{FCC_ERR_ARG, "dense accumulator: B external span exceeds the shared-memory tile"};
+  u64 TL = 1;
+  if (opt.rows_per_tile > 0) TL = u64(opt.rows_per_tile);
+  else if (dense) TL = std::max<u64>(1, dense_cap / LB);
+  if (dense && TL * LB > dense_cap)
+    throw Error{FCC_ERR_ARG, "rows_per_tile x B external span exceeds the dense tile capacity"};
+  if (!dense && (unsigned __int128)TL * LB > (unsigned __int128)(~0ull) - 1)
+    throw Error{FCC_ERR_OVERFLOW, "rows_per_tile x B external span exceeds 64 bits"};
+  u32 hslots = 0;
+  if (!dense) {
+    hslots = opt.hash_slots > 0 ? u32(opt.hash_slots) : 8192u;
+    if (hslots & (hslots - 1)) throw Error{FCC_ERR_ARG, "hash_slots must be a power of two"};
+    if (size_t(hslots) * 16 > smem_cap || hslots < 64) throw Error{FCC_ERR_ARG, "hash_slots out of range"};
+  }
+  u64 pmax = opt.products_per_item > 0 ? u64(opt.products_per_item) : (dense ? (u64(1) << 20) : u64(hslots / 2));
+  if (!dense && pmax > hslots / 2) pmax = hslots / 2;
+  const u64 area = TL * LB;
+
+  u32 *tflag = ar.get_n<u32>(nA2), *tidx = ar.get_n<u32>(nA2);
+  k_tile_flags<<<grid_for(nA2, 256), 256, 0, st>>>(rowA, nA2, TL, tflag);
+  FCC_LAUNCH_CHECK();
+  scan_exclusive(tflag, tidx, nA2, sc32(S_NTILES), ar, st);
+  u64 *tile_row0 = ar.get_n<u64>(nA2);
+  u32 *tile_abeg = ar.get_n<u32>(nA2 + 1);
+  k_tile_write<<<grid_for(nA2, 256), 256, 0, st>>>(rowA, tflag, tidx, nA2, TL, tile_row0, tile_abeg);
+  FCC_LAUNCH_CHECK();
+  u32 *t_items = ar.get_n<u32>(nA2), *t_split = ar.get_n<u32>(nA2);
+  u64 *t_cap = ar.get_n<u64>(nA2), *t_hsz = ar.get_n<u64>(nA2);
+  k_tile_items<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), nA2, tile_abeg, P, pmax, area, dense ? 0 : 1,
+                                                   t_items, t_split, t_cap, t_hsz);
+  FCC_LAUNCH_CHECK();
+  u32 *item_off = ar.get_n<u32>(nA2), *split_idx = ar.get_n<u32>(nA2);
+  u64 *t_hoff = ar.get_n<u64>(nA2);
+  scan_exclusive(t_items, item_off, nA2, sc32(S_NITEMS), ar, st);
+  scan_exclusive(t_split, split_idx, nA2, sc32(S_NSPLIT), ar, st);
+  scan_exclusive(t_cap, t_cap, nA2, d_sc + S_CAP, ar, st);
+  scan_exclusive(t_hsz, t_hoff, nA2, d_sc + S_HASH, ar, st);
+  read_scalars(ctx, d_sc);
+  const u32 nitems = scalar32(ctx, S_NITEMS);
+  const u32 nsplit = scalar32(ctx, S_NSPLIT);
+  const u64 cap_total = ctx->h_scalars[S_CAP];
+  const u64 hash_total = ctx->h_scalars[S_HASH];
+
+  Item *items = ar.get_n<Item>(nitems);
+  int *split_of_tile = ar.get_n<int>(nA2);
+  u32 *split_tiles = ar.get_n<u32>(std::max<u32>(nsplit, 1));
+  k_item_write<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), tile_abeg, P, item_off, pmax, items, t_split,
+                                                   split_idx, split_of_tile, split_tiles);
+  FCC_LAUNCH_CHECK();
+  const u64 words = dense ? (area + 31) / 32 : 0;
+  double *gacc = nullptr;
+  u32 *gmask = nullptr;
+  u64 *gkeys = nullptr;
+  double *gvals = nullptr;
+  if (dense && nsplit > 0) {
+    gacc = ar.get_n<double>(size_t(nsplit) * area);
+    gmask = ar.get_n<u32>(size_t(nsplit) * words);
+  }
+  if (!dense && nsplit > 0) {
+    gkeys = ar.get_n<u64>(hash_total);
+    gvals = ar.get_n<double>(hash_total);
+  }
+  tm.mark(3);
+
+  // ---- contract + drain ----
+  Decode dec{};
+  dec.na = sa.lin.n_ext;
+  dec.nb = sb.lin.n_ext;
+  for (int e = 0; e < dec.na; e++) dec.ra[e] = sa.lin.ext_radix[e];
+  for (int e = 0; e < dec.nb; e++) dec.rb[e] = sb.lin.ext_radix[e];
+  dec.narrow = (sa.span <= 0xFFFFFFFFull && sb.span <= 0xFFFFFFFFull) ? 1 : 0;
+
+  // Output capacity: the planner's upper bound, limited to half of the free
+  // device memory; an overflow is detected on the device and retried once
+  // with the exact count (the cursor counts every reservation).
+  size_t free_b = 0, total_b = 0;
+  FCC_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const u64 per_out = 8 + 4 * u64(out_order);
+  const u64 budget = std::max<u64>(u64(free_b / 2) / per_out, 1 << 20);
+  u64 cap = std::max<u64>(std::min(cap_total, budget), 1);
+  if (opt.capacity_hint > 0) cap = std::min<u64>(cap, u64(opt.capacity_hint));
+
+  for (int attempt = 0;; attempt++) {
+    FCC_CUDA(cudaMallocFromPoolAsync(reinterpret_cast<void **>(&res->d_vals), sizeof(double) * cap, ctx->pool, st));
+    if (out_order > 0)
+      FCC_CUDA(cudaMallocFromPoolAsync(reinterpret_cast<void **>(&res->d_coords), sizeof(u32) * cap * out_order,
+                                       ctx->pool, st));
+    res->cap = i64(cap);
+    Out o{res->d_coords, i64(cap), res->d_vals, cap, d_sc + S_CURSOR};
+    FCC_CUDA(cudaMemsetAsync(d_sc + S_CURSOR, 0, sizeof(u64) * 2, st));  // cursor + item counter
+    FCC_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(u32), st));
+    u32 *counter = sc32(S_COUNTER);
+    if (dense) {
+      if (nsplit > 0) {
+        FCC_CUDA(cudaMemsetAsync(gacc, 0, sizeof(double) * nsplit * area, st));
+        FCC_CUDA(cudaMemsetAsync(gmask, 0, sizeof(u32) * nsplit * words, st));
+      }
+      DenseArgs a{items, nitems, counter, tile_row0, tile_abeg, split_of_tile, split_tiles, nsplit,
+                  P, rowA, segA, valA, segbeg, static_cast<const u32 *>(colB), valB,
+                  u32(LB), u32(area), u32(words), gacc, gmask, o, dec, ctx->d_err};
+      const size_t smem = size_t(area) * 8 + size_t(words) * 4;
+      FCC_CUDA(cudaFuncSetAttribute(k_contract_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+      const int grid = grid_tiles(ctx, reinterpret_cast<const void *>(k_contract_dense), smem, nitems);
+      k_contract_dense<<<grid, kTileThreads, smem, st>>>(a);
+      FCC_LAUNCH_CHECK();
+      tm.mark(4);
+      if (nsplit > 0) {
+        k_merge_dense<<<std::min<u32>(nsplit, u32(ctx->num_sms) * 2), kTileThreads, 0, st>>>(a);
+        FCC_LAUNCH_CHECK();
+      }
+    } else {
+      if (nsplit > 0) {
+        FCC_CUDA(cudaMemsetAsync(gkeys, 0xFF, sizeof(u64) * hash_total, st));
+        FCC_CUDA(cudaMemsetAsync(gvals, 0, sizeof(double) * hash_total, st));
+      }
+      const size_t smem = size_t(hslots) * 16;
+      auto launch = [&](auto colptr) {
+        using ColT = std::remove_const_t<std::remove_pointer_t<decltype(colptr)>>;
+        HashArgs<ColT> a{items, nitems, counter, tile_row0, tile_abeg, split_of_tile, split_tiles, nsplit,
+                         P, rowA, segA, valA, segbeg, colptr, valB, LB, u32(TL), hslots, t_hoff, t_hsz,
+                         gkeys, gvals, o, dec, ctx->d_err};
+        FCC_CUDA(cudaFuncSetAttribute(k_contract_hash<ColT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        const int grid = grid_tiles(ctx, reinterpret_cast<const void *>(k_contract_hash<ColT>), smem, nitems);
+        k_contract_hash<ColT><<<grid, kTileThreads, smem, st>>>(a);
+        FCC_LAUNCH_CHECK();
+        tm.mark(4);
+        if (nsplit > 0) {
+          k_merge_hash<ColT><<<std::min<u32>(nsplit, u32(ctx->num_sms) * 2), kTileThreads, 0, st>>>(a);
+          FCC_LAUNCH_CHECK();
+        }
+      };
+      if (colb32) launch(static_cast<const u32 *>(colB));
+      else launch(static_cast<const u64 *>(colB));
+    }
+    tm.mark(5);
+    read_scalars(ctx, d_sc);
+    const u64 produced = ctx->h_scalars[S_CURSOR];
+    const bool overflow = (u32(ctx->h_scalars[S_ERR]) & ERRB_OVERFLOW) != 0 || produced > cap;
+    if (!overflow) {
+      res->nnz = i64(produced);
+      break;
+    }
+    if (attempt >= 1) throw Error{FCC_ERR_CUDA, "output count changed between attempts"};
+    free_result_buffers(res.get(), st);
+    cap = produced;
+    tm.next = 4;  // re-time the contraction
+  }
+  tm.finish();
+  *out = res.release();
+}
+
+}  // namespace fcc

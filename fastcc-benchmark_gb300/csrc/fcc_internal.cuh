@@ -1,0 +1,130 @@
+// Internal declarations shared by the CUDA translation units of
+// libfastcc_gpu.so. Not part of the public ABI (include/fastcc_gpu.h is).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/fastcc_gpu.h"
+
+namespace fcc {
+
+using u32 = uint32_t;
+using u64 = uint64_t;
+using i64 = int64_t;
+
+constexpr u32 kFull = 0xFFFFFFFFu;
+constexpr u64 kEmptyKey = ~0ull;
+
+// Bits of the device error word. The host maps them to fcc_status.
+enum ErrBits : u32 {
+  ERRB_COORD = 1u,     // coordinate outside [0, max_index]
+  ERRB_OVERFLOW = 2u,  // output capacity exceeded (host retries with the exact count)
+  ERRB_HASH = 4u,      // hash probe limit reached
+  ERRB_INTERNAL = 8u,  // an invariant of the plan did not hold
+};
+
+// Thrown inside the library and turned into a status at the C ABI.
+struct Error {
+  int status;
+  std::string msg;
+};
+
+#define FCC_CUDA(call)                                                                  \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      throw ::fcc::Error{e_ == cudaErrorMemoryAllocation ? FCC_ERR_OOM : FCC_ERR_CUDA,  \
+                         std::string(#call) + ": " + cudaGetErrorString(e_)};           \
+  } while (0)
+
+// Every kernel launch is followed by this check; it also counts launches.
+extern std::atomic<long long> g_launches;
+#define FCC_LAUNCH_CHECK()                                         \
+  do {                                                             \
+    ::fcc::g_launches.fetch_add(1, std::memory_order_relaxed);     \
+    FCC_CUDA(cudaGetLastError());                                  \
+  } while (0)
+
+// Grow-only device workspace. Each contraction bump-allocates from one chunk
+// taken from the context's stream-ordered memory pool; a call that outgrows it
+// takes extra chunks, and the next call replaces them by one chunk of the
+// high-water size, so steady-state calls allocate nothing.
+class Arena {
+ public:
+  void init(cudaMemPool_t pool) { pool_ = pool; }
+  void begin(cudaStream_t s);  // start of a call: consolidate to high-water size
+  void *get(size_t bytes);     // 256-byte aligned, valid until the next begin()
+  template <class T> T *get_n(size_t n) { return static_cast<T *>(get(sizeof(T) * (n ? n : 1))); }
+  void release_all(cudaStream_t s);
+  size_t high_water() const { return high_; }
+
+ private:
+  struct Chunk { char *p; size_t size; };
+  cudaMemPool_t pool_ = nullptr;
+  cudaStream_t stream_ = nullptr;
+  std::vector<Chunk> chunks_;
+  size_t used_ = 0, total_used_ = 0, high_ = 0;
+};
+
+}  // namespace fcc
+
+struct fcc_ctx {
+  int device = 0;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaMemPool_t pool = nullptr;
+  fcc::Arena arena;
+  fcc::u32 *d_err = nullptr;       // device error word
+  fcc::u64 *h_scalars = nullptr;   // pinned host scalars for read-backs
+  cudaEvent_t ev[FCC_NUM_PHASES + 1] = {};
+  double phase_ms[FCC_NUM_PHASES] = {};
+  std::string last_error;
+};
+
+struct fcc_result {
+  int32_t order = 0;
+  int64_t nnz = 0;
+  int64_t cap = 0;       // stride between coordinate modes
+  int64_t products = 0;
+  fcc::u32 *d_coords = nullptr;
+  double *d_vals = nullptr;
+  fcc_ctx *ctx = nullptr;
+};
+
+namespace fcc {
+
+// ---- primitives (fcc_prims.cu) -------------------------------------------
+// Exclusive prefix sums; `out` may alias `in`. When total != nullptr the sum of
+// all n inputs is written to *total (device memory).
+void scan_exclusive(const u32 *in, u32 *out, i64 n, u32 *total, Arena &ar, cudaStream_t s);
+void scan_exclusive(const u64 *in, u64 *out, i64 n, u64 *total, Arena &ar, cudaStream_t s);
+// Widening scan: u32 inputs, u64 prefix sums.
+void scan_exclusive_wide(const u32 *in, u64 *out, i64 n, u64 *total, Arena &ar, cudaStream_t s);
+
+// Stable LSD radix sort of (key, value) pairs on the low `nbits` bits of the
+// keys. keys/vals are sorted in place (ping-ponging through scratch buffers
+// taken from the arena).
+void radix_sort_pairs(u64 *keys, u32 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s);
+
+inline int grid_for(i64 n, int threads, int max_blocks = 1 << 20) {
+  i64 b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > max_blocks) b = max_blocks;
+  return int(b);
+}
+
+inline int bits_for(u64 max_value) {  // bits needed to represent max_value
+  int b = 0;
+  while (b < 64 && (max_value >> b) != 0) b++;
+  return b;
+}
+
+}  // namespace fcc

@@ -1,0 +1,286 @@
+"""ctypes binding of libfastcc_gpu.so (include/fastcc_gpu.h) and of the seeded
+generator libfastcc_synth.so (include/fastcc_synth.h).
+
+Loads the in-tree libraries from ``_build/`` and raises if they are missing:
+there is no CPU fallback. ``Tensor`` and ``Context.fastcc_multiply`` mirror the
+reference call ``a.fastcc_multiply<TileAccumulator<double>, double>(b, ctrA,
+ctrB, tile_size)`` (contract.hpp:824-912); the C++ header host/contract.hpp is
+the drop-in for C++ callers.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+GPU_LIB = os.path.join(BUILD, "libfastcc_gpu.so")
+SYNTH_LIB = os.path.join(BUILD, "libfastcc_synth.so")
+
+FCC_HOST, FCC_DEVICE = 0, 1
+ACC_AUTO, ACC_DENSE, ACC_HASH = 0, 1, 2
+RADIX_PER_OPERAND, RADIX_SHARED = 0, 1
+PHASES = ["upload", "index", "plan", "contract", "merge", "total"]
+STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "hash accumulator full",
+          4: "bounded device wait timed out", 5: "CUDA error", 6: "index space exceeds 64 bits",
+          7: "no usable sm_103 device", 8: "output buffer too small"}
+
+
+class FccError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class _CTensor(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int32), ("nnz", ctypes.c_int64),
+                ("max_index", ctypes.c_void_p), ("coords", ctypes.c_void_p),
+                ("stride_nnz", ctypes.c_int64), ("stride_mode", ctypes.c_int64),
+                ("values", ctypes.c_void_p), ("location", ctypes.c_int32)]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("tile_size", ctypes.c_int32), ("accumulator", ctypes.c_int32),
+                ("radix_mode", ctypes.c_int32), ("rows_per_tile", ctypes.c_int32),
+                ("products_per_item", ctypes.c_int64), ("dense_cap", ctypes.c_int32),
+                ("hash_slots", ctypes.c_int32), ("timing", ctypes.c_int32),
+                ("pad0", ctypes.c_int32), ("capacity_hint", ctypes.c_int64),
+                ("reserved", ctypes.c_int32 * 4)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.tile_size = 100
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
+_lib = None
+_synth = None
+
+
+def lib():
+    """The CUDA library; raises when it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(GPU_LIB):
+            raise RuntimeError(f"{GPU_LIB} is missing: run __graft_entry__.build() first")
+        L = ctypes.CDLL(GPU_LIB)
+        vp, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+        L.fcc_ctx_create.argtypes = [i32, ctypes.POINTER(vp)]
+        L.fcc_ctx_destroy.argtypes = [vp]
+        L.fcc_ctx_set_stream.argtypes = [vp, vp]
+        L.fcc_last_error.argtypes = [vp]
+        L.fcc_last_error.restype = ctypes.c_char_p
+        L.fcc_contract.argtypes = [vp, ctypes.POINTER(_CTensor), ctypes.POINTER(_CTensor), vp, vp, i32,
+                                   ctypes.POINTER(Options), ctypes.POINTER(vp)]
+        L.fcc_count_products.argtypes = [vp, ctypes.POINTER(_CTensor), ctypes.POINTER(_CTensor), vp, vp,
+                                         i32, ctypes.POINTER(Options), ctypes.POINTER(i64)]
+        L.fcc_result_info.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i64), ctypes.POINTER(i64)]
+        L.fcc_result_device.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(i64), ctypes.POINTER(vp)]
+        L.fcc_result_copy_to_host.argtypes = [vp, vp, i64, i64, vp]
+        L.fcc_result_free.argtypes = [vp]
+        L.fcc_last_timings.argtypes = [vp, ctypes.POINTER(ctypes.c_double), i32]
+        L.fcc_status_string.restype = ctypes.c_char_p
+        L.fcc_launch_count.restype = ctypes.c_int64
+        _lib = L
+    return _lib
+
+
+def synth_lib():
+    global _synth
+    if _synth is None:
+        if not os.path.exists(SYNTH_LIB):
+            raise RuntimeError(f"{SYNTH_LIB} is missing: run __graft_entry__.build() first")
+        _synth = ctypes.CDLL(SYNTH_LIB)
+        _synth.fcc_synth_coo.restype = ctypes.c_int
+    return _synth
+
+
+# ------------------------------------------------------------- tensors ----
+
+class Tensor:
+    """A COO operand: coords (nnz, order) int32, values (nnz,) float64 and the
+    per-mode max index (the reference's ``shape`` after ``_infer_shape``,
+    contract.hpp:124-144). coords/values may be numpy arrays (host) or CUDA
+    torch tensors (device)."""
+
+    def __init__(self, coords, values, max_index=None):
+        self.coords = coords
+        self.values = values
+        if max_index is None:
+            c = np.asarray(coords) if isinstance(coords, np.ndarray) else coords.cpu().numpy()
+            max_index = c.max(axis=0) if c.shape[0] else np.zeros(c.shape[1], np.int32)
+        self.max_index = np.ascontiguousarray(max_index, dtype=np.int32)
+
+    @property
+    def order(self):
+        return int(self.max_index.shape[0])
+
+    @property
+    def nnz(self):
+        return int(self.values.shape[0])
+
+    def _struct(self):
+        c, v = self.coords, self.values
+        if isinstance(c, np.ndarray):
+            c = np.ascontiguousarray(c, dtype=np.int32)
+            v = np.ascontiguousarray(v, dtype=np.float64)
+            self._keep = (c, v)
+            cp, vp_, loc = c.ctypes.data, v.ctypes.data, FCC_HOST
+            sn, sm = c.strides[0] // 4, (c.strides[1] // 4 if c.ndim == 2 else 1)
+        else:  # torch CUDA tensors
+            import torch
+            assert c.dtype == torch.int32 and v.dtype == torch.float64 and c.is_cuda and v.is_cuda
+            cp, vp_, loc = c.data_ptr(), v.data_ptr(), FCC_DEVICE
+            sn, sm = c.stride(0), c.stride(1)
+            self._keep = (c, v)
+        return _CTensor(self.order, self.nnz, self.max_index.ctypes.data, cp or None, sn, sm,
+                        vp_ or None, loc)
+
+
+class Result:
+    """A device-resident contraction result (order, nnz, SoA coords, values)."""
+
+    def __init__(self, ctx, handle):
+        self._ctx = ctx
+        self._h = ctypes.c_void_p(handle)
+        o, n, p = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int64()
+        lib().fcc_result_info(self._h, ctypes.byref(o), ctypes.byref(n), ctypes.byref(p))
+        self.order, self.nnz, self.products = o.value, n.value, p.value
+
+    def device_pointers(self):
+        c, s, v = ctypes.c_void_p(), ctypes.c_int64(), ctypes.c_void_p()
+        lib().fcc_result_device(self._h, ctypes.byref(c), ctypes.byref(s), ctypes.byref(v))
+        return c.value, s.value, v.value
+
+    def to_numpy(self, coords_out=None, values_out=None):
+        """(coords (nnz, order) int32, values (nnz,) float64) on the host."""
+        coords = coords_out if coords_out is not None else np.empty((self.nnz, self.order), np.int32)
+        vals = values_out if values_out is not None else np.empty(self.nnz, np.float64)
+        if self.nnz:
+            rc = lib().fcc_result_copy_to_host(self._h, coords.ctypes.data if self.order else None,
+                                               coords.strides[0] // 4 if self.order else 1, 1,
+                                               vals.ctypes.data)
+            self._ctx._check(rc)
+        return coords, vals
+
+    def to_numpy_soa(self, coords_out, values_out):
+        """Copies into caller buffers: coords_out (order, >= nnz) int32 (one row
+        per mode), values_out (>= nnz) float64. Pinned buffers copy fastest."""
+        assert coords_out.dtype == np.int32 and values_out.dtype == np.float64
+        assert values_out.shape[0] >= self.nnz
+        if self.order:
+            assert coords_out.shape[0] == self.order and coords_out.shape[1] >= self.nnz
+        if self.nnz:
+            rc = lib().fcc_result_copy_to_host(self._h, coords_out.ctypes.data if self.order else None, 1,
+                                               coords_out.strides[0] // 4 if self.order else 0,
+                                               values_out.ctypes.data)
+            self._ctx._check(rc)
+
+    def free(self):
+        if self._h:
+            lib().fcc_result_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Context:
+    """One device, one stream, one workspace (fcc_ctx)."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        rc = lib().fcc_ctx_create(device, ctypes.byref(h))
+        if rc != 0:
+            raise FccError(rc, lib().fcc_last_error(None).decode())
+        self._h = h
+
+    def _check(self, rc):
+        if rc != 0:
+            raise FccError(rc, lib().fcc_last_error(self._h).decode())
+
+    def set_stream(self, stream_ptr):
+        self._check(lib().fcc_ctx_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def contract(self, a, b, ctr_a, ctr_b, opts=None):
+        ca = np.ascontiguousarray(ctr_a, dtype=np.int32)
+        cb = np.ascontiguousarray(ctr_b, dtype=np.int32)
+        if ca.shape != cb.shape:
+            raise ValueError("contracted mode lists differ in length")
+        ta, tb = a._struct(), b._struct()
+        out = ctypes.c_void_p()
+        o = opts if opts is not None else Options()
+        rc = lib().fcc_contract(self._h, ctypes.byref(ta), ctypes.byref(tb),
+                                ca.ctypes.data if ca.size else None, cb.ctypes.data if cb.size else None,
+                                int(ca.size), ctypes.byref(o), ctypes.byref(out))
+        self._check(rc)
+        return Result(self, out.value)
+
+    def fastcc_multiply(self, a, b, ctr_a, ctr_b, tile_size=100, accumulator=ACC_AUTO):
+        """Mirror of Tensor<DT>::fastcc_multiply<AccType, RES>(other, left_contr,
+        right_contr, tile_size) (contract.hpp:824-827): returns host arrays."""
+        r = self.contract(a, b, ctr_a, ctr_b, Options(tile_size=tile_size, accumulator=accumulator))
+        try:
+            return r.to_numpy()
+        finally:
+            r.free()
+
+    def count_products(self, a, b, ctr_a, ctr_b, opts=None):
+        ca = np.ascontiguousarray(ctr_a, dtype=np.int32)
+        cb = np.ascontiguousarray(ctr_b, dtype=np.int32)
+        ta, tb = a._struct(), b._struct()
+        n = ctypes.c_int64()
+        o = opts if opts is not None else Options()
+        self._check(lib().fcc_count_products(self._h, ctypes.byref(ta), ctypes.byref(tb),
+                                             ca.ctypes.data if ca.size else None,
+                                             cb.ctypes.data if cb.size else None, int(ca.size),
+                                             ctypes.byref(o), ctypes.byref(n)))
+        return n.value
+
+    def timings(self):
+        ms = (ctypes.c_double * 6)()
+        lib().fcc_last_timings(self._h, ms, 6)
+        return dict(zip(PHASES, list(ms)))
+
+    def close(self):
+        if self._h:
+            lib().fcc_ctx_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def launch_count():
+    """Kernels launched by the library in this process so far."""
+    return int(lib().fcc_launch_count())
+
+
+# ----------------------------------------------------------- generator ----
+
+def synth_coo(seed, extents, zipf_s=None, nnz=1000, lognormal=False):
+    """Seeded distinct-coordinate COO tensor (include/fastcc_synth.h).
+    Returns (coords (n, order) int32, values (n,) float64)."""
+    extents = np.ascontiguousarray(extents, dtype=np.int64)
+    order = extents.shape[0]
+    zs = np.zeros(order) if zipf_s is None else np.broadcast_to(np.asarray(zipf_s, np.float64), (order,))
+    zs = np.ascontiguousarray(zs, dtype=np.float64)
+    coords = np.empty((nnz, order), np.int32)
+    vals = np.empty(nnz, np.float64)
+    got = ctypes.c_int64()
+    rc = synth_lib().fcc_synth_coo(ctypes.c_uint64(seed), ctypes.c_int32(order),
+                                   ctypes.c_void_p(extents.ctypes.data), ctypes.c_void_p(zs.ctypes.data),
+                                   ctypes.c_int64(nnz), ctypes.c_int32(1 if lognormal else 0),
+                                   ctypes.c_void_p(coords.ctypes.data), ctypes.c_void_p(vals.ctypes.data),
+                                   ctypes.byref(got))
+    if rc != 0:
+        raise ValueError("fcc_synth_coo rejected the arguments")
+    n = got.value
+    return coords[:n], vals[:n]

@@ -1,0 +1,163 @@
+/*
+ * fastcc_gpu.h - C ABI of the GB300 (sm_103a) sparse x sparse tensor
+ * contraction. Plain pointers and sizes only; no CUDA or C++ types.
+ *
+ * It replaces the CPU path behind the reference's
+ *   template <class AccType, class RES, class RIGHT>
+ *   ListTensor<RES> Tensor<DT>::fastcc_multiply(Tensor<RIGHT> &other,
+ *       CoOrdinate left_contr, CoOrdinate right_contr, int tile_size = 100)
+ * (contract.hpp:824-912 of jianjianh1/fastcc-benchmark). The header-only C++
+ * shim in fastcc-benchmark_gb300/host/contract.hpp keeps that call and its
+ * types and forwards to fcc_contract below.
+ *
+ * Semantics kept from the reference:
+ *  - operand shape = per-mode max index (Tensor::_infer_shape,
+ *    contract.hpp:124-144); radix of a mode = max index + 1;
+ *  - contraction modes are paired by position in ctrA/ctrB; the contraction
+ *    key is linearised in list order with each operand's own radices
+ *    (CoOrdinate::gather_linearize, coordinate.hpp:723-733) unless
+ *    FCC_RADIX_SHARED is requested;
+ *  - output coordinates: A's non-contracted modes in ascending order, then B's
+ *    (CompactCordinate, coordinate.hpp:402-427), decoded with the external
+ *    modes' own extents;
+ *  - one output per structurally reached (A external, B external) pair, exact
+ *    zero sums included (TileAccumulator::drain_into,
+ *    index_tensors.hpp:1039-1060); output order is unspecified, as the
+ *    reference's per-thread list concatenation leaves it (contract.hpp:906-909).
+ * All value arithmetic is IEEE double. Every call returns an fcc_status.
+ */
+#ifndef FASTCC_GPU_H
+#define FASTCC_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FCC_MAX_ORDER 8
+#define FCC_ABI_VERSION 1
+
+typedef enum fcc_status {
+  FCC_OK = 0,
+  FCC_ERR_ARG = 1,       /* invalid argument or coordinate outside [0, max_index] */
+  FCC_ERR_OOM = 2,       /* device or pinned-host allocation failed */
+  FCC_ERR_HASH_FULL = 3, /* a hash accumulator ran out of slots */
+  FCC_ERR_TIMEOUT = 4,   /* a bounded device wait gave up */
+  FCC_ERR_CUDA = 5,      /* CUDA runtime error (see fcc_last_error) */
+  FCC_ERR_OVERFLOW = 6,  /* an index space or count exceeds 64 bits */
+  FCC_ERR_NO_DEVICE = 7, /* no usable sm_103 device */
+  FCC_ERR_CAPACITY = 8   /* caller-provided output buffer too small */
+} fcc_status;
+
+typedef enum fcc_location { FCC_HOST = 0, FCC_DEVICE = 1 } fcc_location;
+
+/* Accumulator policy. The reference selects it by template argument:
+ * TileAccumulator<double> (dense tile, index_tensors.hpp:994-1065) or
+ * TileAccumulatorMap<double> (hash, :843-883). Results are identical. */
+typedef enum fcc_accumulator {
+  FCC_ACC_AUTO = 0,  /* planner picks per contraction */
+  FCC_ACC_DENSE = 1, /* shared-memory dense tile (needs the B external span to fit) */
+  FCC_ACC_HASH = 2   /* shared-memory open-addressing hash, global hash for split tiles */
+} fcc_accumulator;
+
+typedef enum fcc_radix_mode {
+  FCC_RADIX_PER_OPERAND = 0, /* the reference's contraction key (own max index per operand) */
+  FCC_RADIX_SHARED = 1       /* max over both operands per contracted pair */
+} fcc_radix_mode;
+
+/* A COO operand. coords[n*stride_nnz + m*stride_mode] is mode m of nonzero n
+ * (AoS: stride_nnz=order, stride_mode=1; SoA: stride_nnz=1, stride_mode=nnz).
+ * max_index is always a HOST array of `order` entries; coords and values live
+ * where `location` says. Coordinates must lie in [0, max_index[m]]. */
+typedef struct fcc_tensor {
+  int32_t order;
+  int64_t nnz;
+  const int32_t *max_index;
+  const int32_t *coords;
+  int64_t stride_nnz;
+  int64_t stride_mode;
+  const double *values;
+  int32_t location;
+} fcc_tensor;
+
+/* Tuning knobs. Zero-initialise for defaults (fcc_options_default). */
+typedef struct fcc_options {
+  int32_t tile_size;          /* the reference's tile_size; accepted for signature parity, 0 = 100 */
+  int32_t accumulator;        /* fcc_accumulator */
+  int32_t radix_mode;         /* fcc_radix_mode */
+  int32_t rows_per_tile;      /* A external rows per output tile; 0 = planner */
+  int64_t products_per_item;  /* multiply-adds per work item; 0 = planner */
+  int32_t dense_cap;          /* doubles per shared-memory dense tile; 0 = planner */
+  int32_t hash_slots;         /* shared-memory hash slots (power of two); 0 = planner */
+  int32_t timing;             /* 1: record per-phase CUDA-event times (fcc_last_timings) */
+  int32_t pad0;
+  int64_t capacity_hint;      /* first output allocation in entries; 0 = planner bound. A
+                                 smaller hint is not an error: the device counts every output
+                                 and the call retries once with the exact count. */
+  int32_t reserved[4];
+} fcc_options;
+
+typedef struct fcc_ctx fcc_ctx;       /* one device, one stream, one workspace */
+typedef struct fcc_result fcc_result; /* device-resident output of one contraction */
+
+/* Phases reported by fcc_last_timings (milliseconds). */
+enum {
+  FCC_PHASE_UPLOAD = 0,  /* host->device copy of host operands */
+  FCC_PHASE_INDEX = 1,   /* linearise + radix sort + segment build + lookup (index_tensors.hpp:506-547) */
+  FCC_PHASE_PLAN = 2,    /* tiles, work items, capacity */
+  FCC_PHASE_CONTRACT = 3,/* tile contraction + drain (contract.hpp:876-904) */
+  FCC_PHASE_MERGE = 4,   /* split-tile merge drain */
+  FCC_PHASE_TOTAL = 5,
+  FCC_NUM_PHASES = 6
+};
+
+/* Context. device < 0 selects the current device. */
+int fcc_ctx_create(int32_t device, fcc_ctx **out);
+int fcc_ctx_destroy(fcc_ctx *ctx);
+/* Use a caller-owned cudaStream_t (passed as void*); NULL restores the ctx stream. */
+int fcc_ctx_set_stream(fcc_ctx *ctx, void *cuda_stream);
+/* Text of the last error recorded on this context (never NULL). */
+const char *fcc_last_error(const fcc_ctx *ctx);
+const char *fcc_status_string(int32_t status);
+int fcc_options_default(fcc_options *opts);
+
+/*
+ * out = A x B contracted over ctrA[i] <-> ctrB[i], i < k.
+ * Replaces Tensor<DT>::fastcc_multiply (contract.hpp:824-912). Blocks until
+ * the result count is known; the result stays on the device.
+ */
+int fcc_contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                 const int32_t *ctrB, int32_t k, const fcc_options *opts, fcc_result **out);
+
+/* Result access. Replaces ListTensor's compute_nnz_count/run_through_nnz
+ * (index_tensors.hpp:105-114), which are the reference's only accessors. */
+int fcc_result_info(const fcc_result *r, int32_t *order, int64_t *nnz, int64_t *products);
+/* Device pointers: coords SoA as order arrays of nnz uint32 with stride
+ * `*mode_stride` elements between modes; values nnz doubles. */
+int fcc_result_device(const fcc_result *r, const uint32_t **coords, int64_t *mode_stride,
+                      const double **values);
+/* Copies to host buffers; coords gets nnz*order int32 at
+ * coords[n*stride_nnz + m*stride_mode]; either pointer may be NULL. */
+int fcc_result_copy_to_host(const fcc_result *r, int32_t *coords, int64_t stride_nnz,
+                            int64_t stride_mode, double *values);
+int fcc_result_free(fcc_result *r);
+
+/* Per-phase times of the last fcc_contract on ctx with opts.timing=1. */
+int fcc_last_timings(const fcc_ctx *ctx, double *ms, int32_t n);
+
+/* Multiply-add count sum_c nA(c)*nB(c) (SymbolicTensor::count_ops,
+ * index_tensors.hpp:287-303, in 64 bits) computed on the device. */
+int fcc_count_products(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B,
+                       const int32_t *ctrA, const int32_t *ctrB, int32_t k,
+                       const fcc_options *opts, int64_t *products);
+
+int fcc_abi_version(void);
+
+/* Diagnostics: kernels this process has launched through the library so far. */
+int64_t fcc_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
