@@ -152,15 +152,23 @@ __global__ void k_linearize(const int32_t *__restrict__ coords, i64 sn, i64 sm, 
   }
 }
 
+// |v| below this (zeros included) could make a product round to +-0, so the
+// -0.0 "untouched" sentinel of the dense tile cannot be used.
+__device__ __forceinline__ bool tiny_value(double v) { return fabs(v) < 1e-150; }
+
 template <class ColT>
 __global__ void k_gather_b(const u32 *__restrict__ perm, const u64 *__restrict__ ext,
                            const double *__restrict__ vals, i64 n, ColT *__restrict__ col,
-                           double *__restrict__ val) {
+                           double *__restrict__ val, u32 *tiny) {
+  bool t = false;
   for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
     u32 p = perm[i];
     col[i] = ColT(ext[p]);
-    val[i] = vals[p];
+    const double v = vals[p];
+    val[i] = v;
+    t |= tiny_value(v);
   }
+  if (__any_sync(kFull, t) && (threadIdx.x & 31) == 0) atomicOr(tiny, 1u);
 }
 
 __global__ void k_flag_change(const u64 *__restrict__ key, i64 n, u32 *__restrict__ flag) {
@@ -198,19 +206,26 @@ __global__ void k_lookup(const u64 *__restrict__ keyA, const u32 *__restrict__ p
   }
 }
 
+// Keeps the A entries whose key has a B segment, in row order, with the
+// segment's first B entry (sbA) and length.
 __global__ void k_compact_a(const u32 *__restrict__ flag, const u32 *__restrict__ idx, i64 n,
                             const u32 *__restrict__ permA, const u64 *__restrict__ rowSorted,
                             const u32 *__restrict__ segTmp, const double *__restrict__ valsA,
                             const u32 *__restrict__ segbeg, u64 *__restrict__ rowA,
-                            u32 *__restrict__ segA, double *__restrict__ valA, u32 *__restrict__ len) {
+                            u32 *__restrict__ sbA, double *__restrict__ valA, u32 *__restrict__ len,
+                            u32 *tiny) {
+  bool t = false;
   for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
     if (!flag[i]) continue;
     const u32 d = idx[i], s = segTmp[i];
     rowA[d] = rowSorted[i];
-    segA[d] = s;
-    valA[d] = valsA[permA[i]];
+    sbA[d] = segbeg[s];
+    const double v = valsA[permA[i]];
+    valA[d] = v;
+    t |= tiny_value(v);
     len[d] = segbeg[s + 1] - segbeg[s];
   }
+  if (__any_sync(kFull, t) && (threadIdx.x & 31) == 0) atomicOr(tiny, 1u);
 }
 
 // ------------------------------------------------------------ planning ----
@@ -284,10 +299,120 @@ __global__ void k_item_write(const u32 *__restrict__ ntiles_p, const u32 *__rest
   }
 }
 
-// --------------------------------------------------------- dense tiles ----
+// --------------------------------------------------------- tile kernels ----
+//
+// Work: an item is a range [p0, p1) of the global multiply-add index space
+// (A sorted by row; the multiply-adds of A entry e are P[e] .. P[e+1]-1, one
+// per nonzero of its B segment). An item never crosses an output tile. The
+// CTA that takes an item cuts it into chunks; its warps pull chunks from a
+// shared counter. Within a chunk a warp walks the A entries in order:
+//  * a run of >= kLongRun multiply-adds of one entry streams its B segment,
+//    32 lanes x kBatch loads in flight before the accumulator updates;
+//  * shorter entries go one per lane, up to 32 at once, so rows made of many
+//    rare keys (hub rows of Zipf tensors) keep every lane busy.
 
 constexpr int kTileThreads = 512;
-constexpr u32 kUnit = 256;  // multiply-adds per warp work unit
+constexpr int kBatch = 8;
+constexpr u32 kLongRun = 64;
+constexpr u64 kNegZero = 0x8000000000000000ull;
+
+struct ProdSrc {
+  const u64 *P;        // multiply-add prefix per compacted A entry (nA2 + 1)
+  const u64 *rowA;     // A external (row) index
+  const u32 *sbA;      // first B entry of the entry's segment
+  const double *valA;
+  const double *valB;
+};
+
+template <class ColT, class Add>
+__device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__restrict__ colB, u32 alo,
+                                               u32 ahi, u64 q0, u64 q1, u64 row0, u64 LB, Add &add) {
+  const u32 lane = threadIdx.x & 31;
+  u32 lo = alo, hi = ahi;  // last entry with P[e] <= q0
+  while (hi - lo > 1) {
+    const u32 mid = (lo + hi) >> 1;
+    if (__ldg(&s.P[mid]) <= q0) lo = mid; else hi = mid;
+  }
+  u32 e = lo;
+  u64 pos = q0;
+  while (pos < q1) {  // invariant: P[e] <= pos < P[e+1]
+    const u64 pb = __ldg(&s.P[e]), pe = __ldg(&s.P[e + 1]);
+    const u64 stop = min(pe, q1);
+    if (stop - pos >= kLongRun) {
+      const double va = __ldg(&s.valA[e]);
+      const u64 base = (__ldg(&s.rowA[e]) - row0) * LB;
+      const u32 b0 = __ldg(&s.sbA[e]) + u32(pos - pb);
+      const u32 n = u32(stop - pos);
+      for (u32 o = 0; o < n; o += 32 * kBatch) {
+        ColT c[kBatch];
+        double v[kBatch];
+#pragma unroll
+        for (int k = 0; k < kBatch; k++) {
+          const u32 i = o + k * 32 + lane;
+          if (i < n) { c[k] = __ldg(&colB[b0 + i]); v[k] = __ldg(&s.valB[b0 + i]); }
+        }
+#pragma unroll
+        for (int k = 0; k < kBatch; k++) {
+          const u32 i = o + k * 32 + lane;
+          if (i < n) add(base + u64(c[k]), va * v[k]);
+        }
+      }
+      pos = stop;
+      if (stop == pe) ++e;
+    } else {
+      const u32 el = e + lane;
+      u64 sg = 0, tg = 0, pl = 0;
+      if (el < ahi) {
+        pl = __ldg(&s.P[el]);
+        const u64 pr = __ldg(&s.P[el + 1]);
+        sg = max(pl, pos);
+        tg = min(pr, q1);
+        if (sg > tg) sg = tg;
+      }
+      const bool is_short = sg < tg && (tg - sg) < kLongRun;
+      const u32 stop_mask = __ballot_sync(kFull, !is_short);
+      const u32 g = stop_mask ? u32(__ffs(stop_mask) - 1) : 32u;  // >= 1: lane 0 is short
+      if (lane < g) {
+        const double va = __ldg(&s.valA[el]);
+        const u64 base = (__ldg(&s.rowA[el]) - row0) * LB;
+        const u32 b0 = __ldg(&s.sbA[el]) + u32(sg - pl);
+        const u32 n = u32(tg - sg);
+        for (u32 o = 0; o < n; o += kBatch) {
+          ColT c[kBatch];
+          double v[kBatch];
+#pragma unroll
+          for (int k = 0; k < kBatch; k++)
+            if (o + k < n) { c[k] = __ldg(&colB[b0 + o + k]); v[k] = __ldg(&s.valB[b0 + o + k]); }
+#pragma unroll
+          for (int k = 0; k < kBatch; k++)
+            if (o + k < n) add(base + u64(c[k]), va * v[k]);
+        }
+      }
+      pos = __shfl_sync(kFull, tg, g - 1);
+      e += g;
+    }
+  }
+}
+
+// Runs the chunks of one item on the calling CTA (all threads must call).
+template <class ColT, class Add>
+__device__ __forceinline__ void products_item(const ProdSrc &s, const ColT *colB, u32 alo, u32 ahi, u64 p0,
+                                              u64 p1, u64 row0, u64 LB, u32 *s_chunk, Add &add) {
+  const u32 lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const u64 np = p1 - p0;
+  u64 chunk = np / (4 * nwarps);
+  chunk = chunk < 256 ? 256 : (chunk > 4096 ? 4096 : chunk);
+  const u64 nch = (np + chunk - 1) / chunk;
+  for (;;) {
+    u32 c = 0;
+    if (lane == 0) c = atomicAdd(s_chunk, 1u);
+    c = __shfl_sync(kFull, c, 0);
+    if (c >= nch) break;
+    const u64 q0 = p0 + u64(c) * chunk;
+    const u64 q1 = min(q0 + chunk, p1);
+    products_chunk<ColT>(s, colB, alo, ahi, q0, q1, row0, LB, add);
+  }
+}
 
 struct DenseArgs {
   const Item *items;
@@ -298,13 +423,8 @@ struct DenseArgs {
   const int *split_of_tile;
   const u32 *split_tiles;
   u32 nsplit;
-  const u64 *P;
-  const u64 *rowA;
-  const u32 *segA;
-  const double *valA;
-  const u32 *segbeg;
+  ProdSrc src;
   const u32 *colB;
-  const double *valB;
   u32 LB, area, words;
   double *gacc;
   u32 *gmask;
@@ -313,22 +433,42 @@ struct DenseArgs {
   u32 *err;
 };
 
-// Emits every set bit of `mask` (the touched positions of a dense tile) with
-// its accumulated value, coalesced per warp, and clears both.
-__device__ void drain_dense(double *acc, u32 *mask, u32 words, u32 LB, u64 row0, const Out &out,
+// Word `cw + lane` of the touched bitmask of a dense tile. With kSentinel the
+// tile holds -0.0 at untouched positions and the bitmask is built by ballots.
+template <bool kSentinel>
+__device__ __forceinline__ u32 tile_word(const double *acc, const u32 *mask, u32 area, u32 cw, u32 w1) {
+  const u32 lane = threadIdx.x & 31;
+  if (!kSentinel) {
+    const u32 w = cw + lane;
+    return w < w1 ? mask[w] : 0u;
+  }
+  u32 mine = 0;
+  for (u32 i = 0; i < 32 && cw + i < w1; i++) {
+    const u32 pos = (cw + i) * 32 + lane;
+    const bool t = pos < area && u64(__double_as_longlong(acc[pos])) != kNegZero;
+    const u32 b = __ballot_sync(kFull, t);
+    if (lane == i) mine = b;
+  }
+  return mine;
+}
+
+// Emits every touched position of a dense tile with its value, coalesced per
+// warp, and resets it (mask words to 0; values to 0.0, or -0.0 with kSentinel).
+template <bool kSentinel>
+__device__ void drain_dense(double *acc, u32 *mask, u32 area, u32 words, u32 LB, u64 row0, const Out &out,
                             const Decode &dec, u32 *err, u32 *s_wcnt, u64 *s_base) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-  const u32 wpw = (words + nwarps - 1) / nwarps;
+  const u32 wpw = ((words + nwarps - 1) / nwarps + 31) & ~31u;
   const u32 w0 = min(words, u32(warp) * wpw), w1 = min(words, w0 + wpw);
   u32 c = 0;
-  for (u32 w = w0 + lane; w < w1; w += 32) c += __popc(mask[w]);
+  for (u32 cw = w0; cw < w1; cw += 32) c += __popc(tile_word<kSentinel>(acc, mask, area, cw, w1));
   c = __reduce_add_sync(kFull, c);
   if (lane == 0) s_wcnt[warp] = c;
   __syncthreads();
   if (tid == 0) {
     u32 run = 0;
     for (int w = 0; w < nwarps; w++) {
-      u32 x = s_wcnt[w];
+      const u32 x = s_wcnt[w];
       s_wcnt[w] = run;
       run += x;
     }
@@ -337,10 +477,10 @@ __device__ void drain_dense(double *acc, u32 *mask, u32 words, u32 LB, u64 row0,
   __syncthreads();
   const u64 base = *s_base;
   const bool write = base != ~0ull;
+  const double reset = kSentinel ? __longlong_as_double((long long)kNegZero) : 0.0;
   u64 run = write ? base + s_wcnt[warp] : 0;
   for (u32 cw = w0; cw < w1; cw += 32) {
-    const u32 w = cw + lane;
-    const u32 word = w < w1 ? mask[w] : 0u;
+    const u32 word = tile_word<kSentinel>(acc, mask, area, cw, w1);
     const u32 incl = warp_incl_u32(__popc(word));
     const u32 tot = __shfl_sync(kFull, incl, 31);
     for (u32 kk = 0; kk < tot; kk += 32) {
@@ -348,7 +488,7 @@ __device__ void drain_dense(double *acc, u32 *mask, u32 words, u32 LB, u64 row0,
       u32 lo = 0;
 #pragma unroll
       for (u32 step = 16; step >= 1; step >>= 1) {
-        u32 v = __shfl_sync(kFull, incl, lo + step - 1);
+        const u32 v = __shfl_sync(kFull, incl, lo + step - 1);
         if (v <= k) lo += step;
       }
       const u32 wsrc = __shfl_sync(kFull, word, lo);
@@ -358,84 +498,79 @@ __device__ void drain_dense(double *acc, u32 *mask, u32 words, u32 LB, u64 row0,
         const u32 bit = __fns(wsrc, 0, int(nth) + 1);
         const u32 pos = (cw + lo) * 32 + bit;
         const double v = acc[pos];
-        acc[pos] = 0.0;
+        acc[pos] = reset;
         if (write) emit(out, dec, run + k, row0 + pos / LB, pos % LB, v);
       }
     }
-    if (w < w1) mask[w] = 0u;
+    if (!kSentinel && cw + lane < w1) mask[cw + lane] = 0u;
     run += tot;
   }
 }
 
-__device__ void flush_dense(double *acc, u32 *mask, u32 words, double *gacc, u32 *gmask) {
-  for (u32 w = threadIdx.x; w < words; w += blockDim.x) {
-    u32 word = mask[w];
-    if (!word) continue;
-    atomicOr(&gmask[w], word);
-    mask[w] = 0u;
-    while (word) {
-      const u32 pos = w * 32 + u32(__ffs(word) - 1);
-      word &= word - 1;
+// Adds a partial tile into its global split-tile buffer and resets it.
+template <bool kSentinel>
+__device__ void flush_dense(double *acc, u32 *mask, u32 area, u32 words, double *gacc, u32 *gmask) {
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const double reset = kSentinel ? __longlong_as_double((long long)kNegZero) : 0.0;
+  for (u32 w = warp; w < words; w += nwarps) {
+    const u32 pos = w * 32 + lane;
+    bool t;
+    if (kSentinel) t = pos < area && u64(__double_as_longlong(acc[pos])) != kNegZero;
+    else t = (mask[w] >> lane) & 1u;
+    const u32 b = __ballot_sync(kFull, t);
+    if (t) {
       atomicAdd(&gacc[pos], acc[pos]);
-      acc[pos] = 0.0;
+      acc[pos] = reset;
     }
+    if (lane == 0 && b) atomicOr(&gmask[w], b);
+    if (!kSentinel && lane == 0) mask[w] = 0u;
   }
 }
 
+template <bool kSentinel>
+struct DenseAdd {
+  double *acc;
+  u32 *mask;
+  __device__ __forceinline__ void operator()(u64 pos, double v) const {
+    atomicAdd(&acc[pos], v);
+    if (!kSentinel) atomicOr(&mask[pos >> 5], 1u << (pos & 31));
+  }
+};
+
+template <bool kSentinel>
 __global__ void __launch_bounds__(kTileThreads, 1) k_contract_dense(DenseArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   double *acc = reinterpret_cast<double *>(smem);
   u32 *mask = reinterpret_cast<u32 *>(acc + a.area);
-  __shared__ u32 s_item;
+  __shared__ u32 s_item, s_chunk;
   __shared__ u32 s_wcnt[32];
   __shared__ u64 s_base;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-  for (u32 i = tid; i < a.area; i += blockDim.x) acc[i] = 0.0;
-  for (u32 i = tid; i < a.words; i += blockDim.x) mask[i] = 0u;
-  __syncthreads();
+  const int tid = threadIdx.x;
+  const double init = kSentinel ? __longlong_as_double((long long)kNegZero) : 0.0;
+  for (u32 i = tid; i < a.area; i += blockDim.x) acc[i] = init;
+  if (!kSentinel)
+    for (u32 i = tid; i < a.words; i += blockDim.x) mask[i] = 0u;
+  DenseAdd<kSentinel> add{acc, mask};
   for (;;) {
-    if (tid == 0) s_item = atomicAdd(a.counter, 1u);
+    if (tid == 0) {
+      s_item = atomicAdd(a.counter, 1u);
+      s_chunk = 0;
+    }
     __syncthreads();
     const u32 it = s_item;
     if (it >= a.nitems) break;
     const Item item = a.items[it];
     const u32 t = item.tile;
-    const u32 alo = a.tile_abeg[t], ahi = a.tile_abeg[t + 1];
     const u64 row0 = a.tile_row0[t];
-    const u64 nunits = (item.p1 - item.p0 + kUnit - 1) / kUnit;
-    for (u64 u = warp; u < nunits; u += nwarps) {
-      const u64 q0 = item.p0 + u * kUnit;
-      const u64 q1 = min(q0 + kUnit, item.p1);
-      u32 lo = alo, hi = ahi;  // P[lo] <= q0 < P[hi]
-      while (hi - lo > 1) {
-        const u32 mid = (lo + hi) >> 1;
-        if (a.P[mid] <= q0) lo = mid; else hi = mid;
-      }
-      u32 ai = lo;
-      u64 pa = a.P[ai];
-      while (pa < q1) {
-        const u64 pe = a.P[ai + 1];
-        const u64 s0 = max(q0, pa), s1 = min(q1, pe);
-        const double va = a.valA[ai];
-        const u32 base = u32(a.rowA[ai] - row0) * a.LB;
-        const u32 sb = a.segbeg[a.segA[ai]] + u32(s0 - pa);
-        const u32 cnt = u32(s1 - s0);
-        for (u32 o = lane; o < cnt; o += 32) {
-          const u32 b = sb + o;
-          const u32 pos = base + a.colB[b];
-          atomicAdd(&acc[pos], va * a.valB[b]);
-          atomicOr(&mask[pos >> 5], 1u << (pos & 31));
-        }
-        ++ai;
-        pa = pe;
-      }
-    }
+    products_item<u32>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, row0, a.LB,
+                       &s_chunk, add);
     __syncthreads();
     const int sidx = a.split_of_tile[t];
     if (sidx < 0)
-      drain_dense(acc, mask, a.words, a.LB, row0, a.out, a.dec, a.err, s_wcnt, &s_base);
+      drain_dense<kSentinel>(acc, mask, a.area, a.words, a.LB, row0, a.out, a.dec, a.err, s_wcnt, &s_base);
     else
-      flush_dense(acc, mask, a.words, a.gacc + u64(sidx) * a.area, a.gmask + u64(sidx) * a.words);
+      flush_dense<kSentinel>(acc, mask, a.area, a.words, a.gacc + u64(sidx) * a.area,
+                             a.gmask + u64(sidx) * a.words);
     __syncthreads();
   }
 }
@@ -445,8 +580,8 @@ __global__ void __launch_bounds__(kTileThreads) k_merge_dense(DenseArgs a) {
   __shared__ u64 s_base;
   for (u32 s = blockIdx.x; s < a.nsplit; s += gridDim.x) {
     const u64 row0 = a.tile_row0[a.split_tiles[s]];
-    drain_dense(a.gacc + u64(s) * a.area, a.gmask + u64(s) * a.words, a.words, a.LB, row0, a.out,
-                a.dec, a.err, s_wcnt, &s_base);
+    drain_dense<false>(a.gacc + u64(s) * a.area, a.gmask + u64(s) * a.words, a.area, a.words, a.LB, row0,
+                       a.out, a.dec, a.err, s_wcnt, &s_base);
     __syncthreads();
   }
 }
@@ -463,16 +598,11 @@ struct HashArgs {
   const int *split_of_tile;
   const u32 *split_tiles;
   u32 nsplit;
-  const u64 *P;
-  const u64 *rowA;
-  const u32 *segA;
-  const double *valA;
-  const u32 *segbeg;
+  ProdSrc src;
   const ColT *colB;
-  const double *valB;
   u64 LB;
   u32 TL;
-  u32 slots;  // shared-memory slots (power of two)
+  u32 slots;        // shared-memory slots (power of two)
   const u64 *hoff;  // per tile: first slot of its global region (split tiles)
   const u64 *hsz;   // per tile: global region size, a power of two (split tiles)
   u64 *gkeys;
@@ -497,7 +627,7 @@ __device__ void drain_hash(u64 *keys, double *vals, u64 nslots, u64 LB, u32 TL, 
   if (tid == 0) {
     u32 run = 0;
     for (int w = 0; w < nwarps; w++) {
-      u32 x = s_wcnt[w];
+      const u32 x = s_wcnt[w];
       s_wcnt[w] = run;
       run += x;
     }
@@ -527,7 +657,7 @@ __device__ void drain_hash(u64 *keys, double *vals, u64 nslots, u64 LB, u32 TL, 
 __device__ __forceinline__ void global_hash_add(u64 *gk, double *gv, u64 hs, u64 key, double v, u32 *err) {
   u64 h = u64(hash_slot(key)) & (hs - 1);
   for (u64 probe = 0; probe < hs; probe++) {
-    u64 cur = atomicCAS(reinterpret_cast<unsigned long long *>(&gk[h]), kEmptyKey, key);
+    const u64 cur = atomicCAS(reinterpret_cast<unsigned long long *>(&gk[h]), kEmptyKey, key);
     if (cur == kEmptyKey || cur == key) {
       atomicAdd(&gv[h], v);
       return;
@@ -537,70 +667,53 @@ __device__ __forceinline__ void global_hash_add(u64 *gk, double *gv, u64 hs, u64
   atomicOr(err, ERRB_HASH);
 }
 
+struct HashAdd {
+  u64 *hk;
+  double *hv;
+  u32 hmask;
+  u32 *err;
+  __device__ __forceinline__ void operator()(u64 key, double v) const {
+    u32 h = hash_slot(key) & hmask;
+    for (u32 probe = 0; probe <= hmask; ++probe) {
+      const u64 cur = *reinterpret_cast<volatile u64 *>(&hk[h]);
+      if (cur == key) { atomicAdd(&hv[h], v); return; }
+      if (cur == kEmptyKey) {
+        const u64 old = atomicCAS(reinterpret_cast<unsigned long long *>(&hk[h]), kEmptyKey, key);
+        if (old == kEmptyKey || old == key) { atomicAdd(&hv[h], v); return; }
+      }
+      h = (h + 1) & hmask;
+    }
+    atomicOr(err, ERRB_HASH);
+  }
+};
+
 template <class ColT>
 __global__ void __launch_bounds__(kTileThreads, 1) k_contract_hash(HashArgs<ColT> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   u64 *hk = reinterpret_cast<u64 *>(smem);
   double *hv = reinterpret_cast<double *>(hk + a.slots);
-  __shared__ u32 s_item;
+  __shared__ u32 s_item, s_chunk;
   __shared__ u32 s_wcnt[32];
   __shared__ u64 s_base;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const int tid = threadIdx.x;
   for (u32 i = tid; i < a.slots; i += blockDim.x) { hk[i] = kEmptyKey; hv[i] = 0.0; }
-  __syncthreads();
   for (;;) {
-    if (tid == 0) s_item = atomicAdd(a.counter, 1u);
+    if (tid == 0) {
+      s_item = atomicAdd(a.counter, 1u);
+      s_chunk = 0;
+    }
     __syncthreads();
     const u32 it = s_item;
     if (it >= a.nitems) break;
     const Item item = a.items[it];
     const u32 t = item.tile;
-    const u32 alo = a.tile_abeg[t], ahi = a.tile_abeg[t + 1];
     const u64 row0 = a.tile_row0[t];
     const u64 np = item.p1 - item.p0;
     u32 hsl = 64;
     while (u64(hsl) < 2 * np && hsl < a.slots) hsl <<= 1;
-    const u32 hmask = hsl - 1;
-    const u64 nunits = (np + kUnit - 1) / kUnit;
-    for (u64 u = warp; u < nunits; u += nwarps) {
-      const u64 q0 = item.p0 + u * kUnit;
-      const u64 q1 = min(q0 + kUnit, item.p1);
-      u32 lo = alo, hi = ahi;
-      while (hi - lo > 1) {
-        const u32 mid = (lo + hi) >> 1;
-        if (a.P[mid] <= q0) lo = mid; else hi = mid;
-      }
-      u32 ai = lo;
-      u64 pa = a.P[ai];
-      while (pa < q1) {
-        const u64 pe = a.P[ai + 1];
-        const u64 s0 = max(q0, pa), s1 = min(q1, pe);
-        const double va = a.valA[ai];
-        const u64 kbase = (a.rowA[ai] - row0) * a.LB;
-        const u32 sb = a.segbeg[a.segA[ai]] + u32(s0 - pa);
-        const u32 cnt = u32(s1 - s0);
-        for (u32 o = lane; o < cnt; o += 32) {
-          const u32 b = sb + o;
-          const u64 key = kbase + u64(a.colB[b]);
-          const double p = va * a.valB[b];
-          u32 h = hash_slot(key) & hmask;
-          u32 probe = 0;
-          for (;; ++probe) {
-            if (probe > hmask) { atomicOr(a.err, ERRB_HASH); break; }
-            const u64 cur = *reinterpret_cast<volatile u64 *>(&hk[h]);
-            if (cur == key) break;
-            if (cur == kEmptyKey) {
-              const u64 old = atomicCAS(reinterpret_cast<unsigned long long *>(&hk[h]), kEmptyKey, key);
-              if (old == kEmptyKey || old == key) break;
-            }
-            h = (h + 1) & hmask;
-          }
-          if (probe <= hmask) atomicAdd(&hv[h], p);
-        }
-        ++ai;
-        pa = pe;
-      }
-    }
+    HashAdd add{hk, hv, hsl - 1, a.err};
+    products_item<ColT>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, row0, a.LB,
+                        &s_chunk, add);
     __syncthreads();
     const int sidx = a.split_of_tile[t];
     if (sidx < 0) {
@@ -727,7 +840,7 @@ const double *upload_values(fcc_ctx *ctx, const fcc_tensor *t) {
 
 // Device scalar block: slot numbers in a u64 array.
 enum Scalar { S_NSEG = 0, S_NA2, S_NTILES, S_NITEMS, S_NSPLIT, S_CAP, S_HASH, S_CURSOR, S_COUNTER,
-              S_PTOTAL, S_ERR, S_COUNT };
+              S_PTOTAL, S_ERR, S_TINY, S_COUNT };
 
 // Copies the scalar block and the error word to pinned host memory, waits,
 // and raises the error bits that are not recoverable.
@@ -861,9 +974,11 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   double *valB = ar.get_n<double>(nB);
   void *colB = colb32 ? static_cast<void *>(ar.get_n<u32>(nB)) : static_cast<void *>(ar.get_n<u64>(nB));
   if (colb32)
-    k_gather_b<u32><<<grid_for(nB, 256), 256, 0, st>>>(permB, extB, sb.vals, nB, static_cast<u32 *>(colB), valB);
+    k_gather_b<u32><<<grid_for(nB, 256), 256, 0, st>>>(permB, extB, sb.vals, nB, static_cast<u32 *>(colB), valB,
+                                                       sc32(S_TINY));
   else
-    k_gather_b<u64><<<grid_for(nB, 256), 256, 0, st>>>(permB, extB, sb.vals, nB, static_cast<u64 *>(colB), valB);
+    k_gather_b<u64><<<grid_for(nB, 256), 256, 0, st>>>(permB, extB, sb.vals, nB, static_cast<u64 *>(colB), valB,
+                                                       sc32(S_TINY));
   FCC_LAUNCH_CHECK();
   u32 *flagB = ar.get_n<u32>(nB), *idxB = ar.get_n<u32>(nB);
   k_flag_change<<<grid_for(nB, 256), 256, 0, st>>>(keyB, nB, flagB);
@@ -881,11 +996,11 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   FCC_LAUNCH_CHECK();
   scan_exclusive(flagA, idxA, nA, sc32(S_NA2), ar, st);
   u64 *rowA = ar.get_n<u64>(nA);
-  u32 *segA = ar.get_n<u32>(nA), *lenA = ar.get_n<u32>(nA);
+  u32 *sbA = ar.get_n<u32>(nA), *lenA = ar.get_n<u32>(nA);
   double *valA = ar.get_n<double>(nA);
   FCC_CUDA(cudaMemsetAsync(lenA, 0, sizeof(u32) * nA, st));
   k_compact_a<<<grid_for(nA, 256), 256, 0, st>>>(flagA, idxA, nA, permA, extA, segTmp, sa.vals, segbeg, rowA,
-                                                 segA, valA, lenA);
+                                                 sbA, valA, lenA, sc32(S_TINY));
   FCC_LAUNCH_CHECK();
   u64 *P = ar.get_n<u64>(nA + 1);
   scan_exclusive_wide(lenA, P, nA, P + nA, ar, st);
@@ -979,6 +1094,15 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   tm.mark(3);
 
   // ---- contract + drain ----
+  // Dense tiles that the multiply-adds fill well keep -0.0 at untouched
+  // positions instead of a touched bitmask (one shared atomic per multiply-add
+  // instead of two); it needs inputs without zero or tiny values, which could
+  // make a product round to -0.0.
+  const bool tiny = (ctx->h_scalars[S_TINY] & 1) != 0;
+  const u32 ntiles = scalar32(ctx, S_NTILES);
+  bool sentinel = dense && !tiny && opt.dense_mode != FCC_DENSE_BITMASK &&
+                  (opt.dense_mode == FCC_DENSE_SENTINEL || ptotal >= u64(ntiles) * area / 4);
+  const ProdSrc src{P, rowA, sbA, valA, valB};
   Decode dec{};
   dec.na = sa.lin.n_ext;
   dec.nb = sb.lin.n_ext;
@@ -1012,12 +1136,15 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
         FCC_CUDA(cudaMemsetAsync(gmask, 0, sizeof(u32) * nsplit * words, st));
       }
       DenseArgs a{items, nitems, counter, tile_row0, tile_abeg, split_of_tile, split_tiles, nsplit,
-                  P, rowA, segA, valA, segbeg, static_cast<const u32 *>(colB), valB,
-                  u32(LB), u32(area), u32(words), gacc, gmask, o, dec, ctx->d_err};
-      const size_t smem = size_t(area) * 8 + size_t(words) * 4;
-      FCC_CUDA(cudaFuncSetAttribute(k_contract_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-      const int grid = grid_tiles(ctx, reinterpret_cast<const void *>(k_contract_dense), smem, nitems);
-      k_contract_dense<<<grid, kTileThreads, smem, st>>>(a);
+                  src, static_cast<const u32 *>(colB), u32(LB), u32(area), u32(words), gacc, gmask, o, dec,
+                  ctx->d_err};
+      const size_t smem = size_t(area) * 8 + (sentinel ? 0 : size_t(words) * 4);
+      const void *kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true>)
+                                  : reinterpret_cast<const void *>(k_contract_dense<false>);
+      FCC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+      const int grid = grid_tiles(ctx, kern, smem, nitems);
+      if (sentinel) k_contract_dense<true><<<grid, kTileThreads, smem, st>>>(a);
+      else k_contract_dense<false><<<grid, kTileThreads, smem, st>>>(a);
       FCC_LAUNCH_CHECK();
       tm.mark(4);
       if (nsplit > 0) {
@@ -1033,8 +1160,7 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       auto launch = [&](auto colptr) {
         using ColT = std::remove_const_t<std::remove_pointer_t<decltype(colptr)>>;
         HashArgs<ColT> a{items, nitems, counter, tile_row0, tile_abeg, split_of_tile, split_tiles, nsplit,
-                         P, rowA, segA, valA, segbeg, colptr, valB, LB, u32(TL), hslots, t_hoff, t_hsz,
-                         gkeys, gvals, o, dec, ctx->d_err};
+                         src, colptr, LB, u32(TL), hslots, t_hoff, t_hsz, gkeys, gvals, o, dec, ctx->d_err};
         FCC_CUDA(cudaFuncSetAttribute(k_contract_hash<ColT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
         const int grid = grid_tiles(ctx, reinterpret_cast<const void *>(k_contract_hash<ColT>), smem, nitems);
         k_contract_hash<ColT><<<grid, kTileThreads, smem, st>>>(a);

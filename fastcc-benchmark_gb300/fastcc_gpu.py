@@ -20,6 +20,7 @@ SYNTH_LIB = os.path.join(BUILD, "libfastcc_synth.so")
 FCC_HOST, FCC_DEVICE = 0, 1
 ACC_AUTO, ACC_DENSE, ACC_HASH = 0, 1, 2
 RADIX_PER_OPERAND, RADIX_SHARED = 0, 1
+DENSE_AUTO, DENSE_BITMASK, DENSE_SENTINEL = 0, 1, 2
 PHASES = ["upload", "index", "plan", "contract", "merge", "total"]
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "hash accumulator full",
           4: "bounded device wait timed out", 5: "CUDA error", 6: "index space exceeds 64 bits",
@@ -45,7 +46,7 @@ class Options(ctypes.Structure):
                 ("products_per_item", ctypes.c_int64), ("dense_cap", ctypes.c_int32),
                 ("hash_slots", ctypes.c_int32), ("timing", ctypes.c_int32),
                 ("pad0", ctypes.c_int32), ("capacity_hint", ctypes.c_int64),
-                ("reserved", ctypes.c_int32 * 4)]
+                ("dense_mode", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
     def __init__(self, **kw):
         super().__init__()

@@ -95,8 +95,18 @@ typedef struct fcc_options {
   int64_t capacity_hint;      /* first output allocation in entries; 0 = planner bound. A
                                  smaller hint is not an error: the device counts every output
                                  and the call retries once with the exact count. */
-  int32_t reserved[4];
+  int32_t dense_mode;         /* fcc_dense_mode: how a dense tile marks touched positions */
+  int32_t reserved[3];
 } fcc_options;
+
+/* Touched-position tracking of the dense accumulator. Both emit every touched
+ * position, exact zero sums included. The sentinel form is used only when no
+ * input value is zero or below 1e-150 in magnitude. */
+typedef enum fcc_dense_mode {
+  FCC_DENSE_AUTO = 0,     /* sentinel when the tiles are well filled */
+  FCC_DENSE_BITMASK = 1,  /* a touched bit per position */
+  FCC_DENSE_SENTINEL = 2  /* untouched positions hold -0.0 */
+} fcc_dense_mode;
 
 typedef struct fcc_ctx fcc_ctx;       /* one device, one stream, one workspace */
 typedef struct fcc_result fcc_result; /* device-resident output of one contraction */

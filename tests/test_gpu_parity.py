@@ -36,6 +36,9 @@ VARIANTS = [
     {"dense_cap": 2048, "products_per_item": 300},
     {"capacity_hint": 3},                                   # overflow -> exact-count retry
     {"hash_slots": 64},
+    {"dense_mode": F.DENSE_SENTINEL},
+    {"dense_mode": F.DENSE_SENTINEL, "products_per_item": 9},
+    {"dense_mode": F.DENSE_BITMASK, "products_per_item": 11},
 ]
 
 
@@ -174,8 +177,27 @@ def test_exact_zero_sums_are_emitted(ctx):
     a = F.Tensor(np.array([[0, 0], [0, 1]], np.int32), np.array([1.0, 1.0]), np.array([0, 1], np.int32))
     b = F.Tensor(np.array([[0, 0], [0, 1]], np.int32), np.array([2.0, -2.0]), np.array([0, 1], np.int32))
     for acc in (F.ACC_DENSE, F.ACC_HASH):
-        c, v = ctx.fastcc_multiply(a, b, [1], [1], accumulator=acc)
-        assert c.tolist() == [[0, 0]] and v.tolist() == [0.0]
+        for mode in (F.DENSE_AUTO, F.DENSE_BITMASK, F.DENSE_SENTINEL):
+            r = ctx.contract(a, b, [1], [1], F.Options(accumulator=acc, dense_mode=mode))
+            c, v = r.to_numpy()
+            r.free()
+            assert c.tolist() == [[0, 0]] and v.tolist() == [0.0]
+
+
+def test_zero_valued_inputs_keep_touched_positions(ctx):
+    # zero inputs make products of -0.0 and +0.0; every touched position is
+    # still emitted (the -0.0 sentinel is not used for such inputs)
+    rng = np.random.Generator(np.random.PCG64(31))
+    g = load_golden("readme_small_t16")
+    av = g["a_vals"].copy()
+    bv = g["b_vals"].copy()
+    av[rng.choice(av.size, av.size // 3, replace=False)] = 0.0
+    bv[rng.choice(bv.size, bv.size // 3, replace=False)] = -0.0
+    args = (g["a_coords"], av, g["a_max"], g["b_coords"], bv, g["b_max"], g["ctr_a"], g["ctr_b"])
+    o = run_oracle(*args)
+    for mode in (F.DENSE_AUTO, F.DENSE_SENTINEL, F.DENSE_BITMASK):
+        c, v, _ = run_gpu(ctx, *args, dense_mode=mode)
+        check_parity(c, v, o["coords"], o["values"], o["abs_sum"])
 
 
 def test_full_contraction_is_a_scalar(ctx):
