@@ -311,8 +311,8 @@ __global__ void k_item_write(const u32 *__restrict__ ntiles_p, const u32 *__rest
 //  * shorter entries go one per lane, up to 32 at once, so rows made of many
 //    rare keys (hub rows of Zipf tensors) keep every lane busy.
 
-constexpr int kTileThreads = 512;
-constexpr int kBatch = 8;
+constexpr int kTileThreads = 1024;
+constexpr int kBatch = 4;
 constexpr u32 kLongRun = 64;
 constexpr u64 kNegZero = 0x8000000000000000ull;
 
@@ -323,6 +323,27 @@ struct ProdSrc {
   const double *valA;
   const double *valB;
 };
+
+// Lanes that run different A entries can update the same output position at
+// once (Zipf hub columns sit in most segments). Colliding lanes are summed
+// with shuffles first and one atomic is issued per distinct position.
+template <class Add>
+__device__ __forceinline__ void add_aggregated(Add &add, u64 key, double v) {
+  const u32 lane = threadIdx.x & 31;
+  const u32 am = __activemask();
+  const u32 peers = __match_any_sync(am, key);
+  if (peers == (1u << lane)) {
+    add(key, v);
+    return;
+  }
+  const int leader = __ffs(peers) - 1;
+  double s = v;
+  for (u32 rest = peers & (peers - 1); rest; rest &= rest - 1) {
+    const double x = __shfl_sync(peers, v, __ffs(rest) - 1);
+    if (int(lane) == leader) s += x;
+  }
+  if (int(lane) == leader) add(key, s);
+}
 
 template <class ColT, class Add>
 __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__restrict__ colB, u32 alo,
@@ -385,7 +406,7 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
             if (o + k < n) { c[k] = __ldg(&colB[b0 + o + k]); v[k] = __ldg(&s.valB[b0 + o + k]); }
 #pragma unroll
           for (int k = 0; k < kBatch; k++)
-            if (o + k < n) add(base + u64(c[k]), va * v[k]);
+            if (o + k < n) add_aggregated(add, base + u64(c[k]), va * v[k]);
         }
       }
       pos = __shfl_sync(kFull, tg, g - 1);
