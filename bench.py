@@ -204,6 +204,36 @@ def run_profile_case(name):
             r.free()
 
 
+def run_sweep(name, variants, reps=3):
+    """Times option sets on one workload (device-resident, median of reps),
+    one JSON line per option set."""
+    import torch
+
+    import build_lib
+    build_lib.build_all()
+    import fastcc_gpu as F
+    import workloads
+    w = {"zipf3": workloads.zipf3, "twomode": workloads.twomode, "readme": workloads.readme}[name]()
+    a, b = w["a"], w["b"]
+    A = F.Tensor(torch.from_numpy(a.coords).cuda(), torch.from_numpy(a.values).cuda(), a.max_index)
+    B = A if b is a else F.Tensor(torch.from_numpy(b.coords).cuda(), torch.from_numpy(b.values).cuda(),
+                                  b.max_index)
+    torch.cuda.synchronize()
+    with F.Context(0) as ctx:
+        for v in variants:
+            opts = F.Options(timing=1, **v)
+            tot, con = [], []
+            for rep in range(reps + 1):
+                r = ctx.contract(A, B, w["ctr_a"], w["ctr_b"], opts)
+                t = ctx.timings()
+                r.free()
+                if rep:
+                    tot.append(t["total"])
+                    con.append(t["contract"])
+            print(json.dumps({"workload": name, "options": v, "total_ms": statistics.median(tot),
+                              "contract_ms": statistics.median(con)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -214,7 +244,13 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--profile", choices=["zipf3-small", "twomode-small", "readme"],
                     help="one warm-up and one timed contraction of a small case, for ncu captures")
+    ap.add_argument("--sweep", choices=["zipf3", "twomode", "readme"],
+                    help="time the option sets given by --variants (JSON list) on a workload")
+    ap.add_argument("--variants", default="[{}]")
     args = ap.parse_args()
+    if args.sweep:
+        run_sweep(args.sweep, json.loads(args.variants))
+        return
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_setup()
     if args.impl == "reference":

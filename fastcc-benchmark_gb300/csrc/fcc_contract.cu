@@ -326,26 +326,24 @@ struct ProdSrc {
 
 // Lanes that run different A entries can update the same output position at
 // once (Zipf hub columns sit in most segments). Colliding lanes are summed
-// with shuffles first and one atomic is issued per distinct position.
-template <class Add>
-__device__ __forceinline__ void add_aggregated(Add &add, u64 key, double v) {
+// with shuffles first; only the lowest lane of each group keeps an update.
+// Returns true for the lanes whose (key, *v) must still be applied.
+template <class KeyT>
+__device__ __forceinline__ bool aggregate_lanes(KeyT key, double *v) {
   const u32 lane = threadIdx.x & 31;
-  const u32 am = __activemask();
-  const u32 peers = __match_any_sync(am, key);
-  if (peers == (1u << lane)) {
-    add(key, v);
-    return;
-  }
+  const u32 peers = __match_any_sync(__activemask(), key);
+  if (peers == (1u << lane)) return true;
   const int leader = __ffs(peers) - 1;
-  double s = v;
+  double s = *v;
   for (u32 rest = peers & (peers - 1); rest; rest &= rest - 1) {
-    const double x = __shfl_sync(peers, v, __ffs(rest) - 1);
+    const double x = __shfl_sync(peers, *v, __ffs(rest) - 1);
     if (int(lane) == leader) s += x;
   }
-  if (int(lane) == leader) add(key, s);
+  *v = s;
+  return int(lane) == leader;
 }
 
-template <class ColT, class Add>
+template <class ColT, class KeyT, class Add>
 __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__restrict__ colB, u32 alo,
                                                u32 ahi, u64 q0, u64 q1, u64 row0, u64 LB, Add &add) {
   const u32 lane = threadIdx.x & 31;
@@ -361,7 +359,7 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
     const u64 stop = min(pe, q1);
     if (stop - pos >= kLongRun) {
       const double va = __ldg(&s.valA[e]);
-      const u64 base = (__ldg(&s.rowA[e]) - row0) * LB;
+      const KeyT base = KeyT((__ldg(&s.rowA[e]) - row0) * LB);
       const u32 b0 = __ldg(&s.sbA[e]) + u32(pos - pb);
       const u32 n = u32(stop - pos);
       for (u32 o = 0; o < n; o += 32 * kBatch) {
@@ -372,11 +370,17 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
           const u32 i = o + k * 32 + lane;
           if (i < n) { c[k] = __ldg(&colB[b0 + i]); v[k] = __ldg(&s.valB[b0 + i]); }
         }
+        KeyT key[kBatch];
+        double val[kBatch];
+        u32 valid = 0;
 #pragma unroll
         for (int k = 0; k < kBatch; k++) {
           const u32 i = o + k * 32 + lane;
-          if (i < n) add(base + u64(c[k]), va * v[k]);
+          key[k] = base + KeyT(c[k]);
+          val[k] = va * v[k];
+          if (i < n) valid |= 1u << k;
         }
+        add.batch(key, val, valid);
       }
       pos = stop;
       if (stop == pe) ++e;
@@ -395,7 +399,7 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
       const u32 g = stop_mask ? u32(__ffs(stop_mask) - 1) : 32u;  // >= 1: lane 0 is short
       if (lane < g) {
         const double va = __ldg(&s.valA[el]);
-        const u64 base = (__ldg(&s.rowA[el]) - row0) * LB;
+        const KeyT base = KeyT((__ldg(&s.rowA[el]) - row0) * LB);
         const u32 b0 = __ldg(&s.sbA[el]) + u32(sg - pl);
         const u32 n = u32(tg - sg);
         for (u32 o = 0; o < n; o += kBatch) {
@@ -404,9 +408,16 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
 #pragma unroll
           for (int k = 0; k < kBatch; k++)
             if (o + k < n) { c[k] = __ldg(&colB[b0 + o + k]); v[k] = __ldg(&s.valB[b0 + o + k]); }
+          KeyT key[kBatch];
+          double val[kBatch];
+          u32 valid = 0;
 #pragma unroll
-          for (int k = 0; k < kBatch; k++)
-            if (o + k < n) add_aggregated(add, base + u64(c[k]), va * v[k]);
+          for (int k = 0; k < kBatch; k++) {
+            key[k] = base + KeyT(c[k]);
+            val[k] = va * v[k];
+            if (o + k < n && aggregate_lanes(key[k], &val[k])) valid |= 1u << k;
+          }
+          add.batch(key, val, valid);
         }
       }
       pos = __shfl_sync(kFull, tg, g - 1);
@@ -416,7 +427,7 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
 }
 
 // Runs the chunks of one item on the calling CTA (all threads must call).
-template <class ColT, class Add>
+template <class ColT, class KeyT, class Add>
 __device__ __forceinline__ void products_item(const ProdSrc &s, const ColT *colB, u32 alo, u32 ahi, u64 p0,
                                               u64 p1, u64 row0, u64 LB, u32 *s_chunk, Add &add) {
   const u32 lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
@@ -431,7 +442,7 @@ __device__ __forceinline__ void products_item(const ProdSrc &s, const ColT *colB
     if (c >= nch) break;
     const u64 q0 = p0 + u64(c) * chunk;
     const u64 q1 = min(q0 + chunk, p1);
-    products_chunk<ColT>(s, colB, alo, ahi, q0, q1, row0, LB, add);
+    products_chunk<ColT, KeyT>(s, colB, alo, ahi, q0, q1, row0, LB, add);
   }
 }
 
@@ -548,18 +559,48 @@ __device__ void flush_dense(double *acc, u32 *mask, u32 area, u32 words, double 
   }
 }
 
+// Shared-memory FP64 accumulation. The loads and compare-and-swaps of a batch
+// are issued back to back, so a thread has kBatch updates in flight; a CAS
+// that lost a race is retried on its own.
 template <bool kSentinel>
 struct DenseAdd {
   double *acc;
   u32 *mask;
-  __device__ __forceinline__ void operator()(u64 pos, double v) const {
-    atomicAdd(&acc[pos], v);
-    if (!kSentinel) atomicOr(&mask[pos >> 5], 1u << (pos & 31));
+  __device__ __forceinline__ void batch(const u32 (&key)[kBatch], const double (&val)[kBatch], u32 valid) const {
+    unsigned long long old[kBatch];
+#pragma unroll
+    for (int k = 0; k < kBatch; k++)
+      if ((valid >> k) & 1u) old[k] = *reinterpret_cast<volatile unsigned long long *>(&acc[key[k]]);
+    u32 fail = 0;
+#pragma unroll
+    for (int k = 0; k < kBatch; k++)
+      if ((valid >> k) & 1u) {
+        const unsigned long long got =
+            atomicCAS(reinterpret_cast<unsigned long long *>(&acc[key[k]]), old[k],
+                      (unsigned long long)__double_as_longlong(__longlong_as_double((long long)old[k]) + val[k]));
+        if (got != old[k]) fail |= 1u << k;
+      }
+#pragma unroll
+    for (int k = 0; k < kBatch; k++) {
+      if ((fail >> k) & 1u) {
+        unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(&acc[key[k]]), assumed;
+        do {
+          assumed = cur;
+          cur = atomicCAS(reinterpret_cast<unsigned long long *>(&acc[key[k]]), assumed,
+                          (unsigned long long)__double_as_longlong(__longlong_as_double((long long)assumed) + val[k]));
+        } while (cur != assumed);
+      }
+    }
+    if (!kSentinel) {
+#pragma unroll
+      for (int k = 0; k < kBatch; k++)
+        if ((valid >> k) & 1u) atomicOr(&mask[key[k] >> 5], 1u << (key[k] & 31));
+    }
   }
 };
 
-template <bool kSentinel>
-__global__ void __launch_bounds__(kTileThreads, 1) k_contract_dense(DenseArgs a) {
+template <bool kSentinel, int kThreads>
+__global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   double *acc = reinterpret_cast<double *>(smem);
   u32 *mask = reinterpret_cast<u32 *>(acc + a.area);
@@ -583,8 +624,8 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_contract_dense(DenseArgs a)
     const Item item = a.items[it];
     const u32 t = item.tile;
     const u64 row0 = a.tile_row0[t];
-    products_item<u32>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, row0, a.LB,
-                       &s_chunk, add);
+    products_item<u32, u32>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, row0, a.LB,
+                            &s_chunk, add);
     __syncthreads();
     const int sidx = a.split_of_tile[t];
     if (sidx < 0)
@@ -706,10 +747,15 @@ struct HashAdd {
     }
     atomicOr(err, ERRB_HASH);
   }
+  __device__ __forceinline__ void batch(const u64 (&key)[kBatch], const double (&val)[kBatch], u32 valid) const {
+#pragma unroll
+    for (int k = 0; k < kBatch; k++)
+      if ((valid >> k) & 1u) (*this)(key[k], val[k]);
+  }
 };
 
-template <class ColT>
-__global__ void __launch_bounds__(kTileThreads, 1) k_contract_hash(HashArgs<ColT> a) {
+template <class ColT, int kThreads>
+__global__ void __launch_bounds__(kThreads, 1) k_contract_hash(HashArgs<ColT> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   u64 *hk = reinterpret_cast<u64 *>(smem);
   double *hv = reinterpret_cast<double *>(hk + a.slots);
@@ -733,8 +779,8 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_contract_hash(HashArgs<ColT
     u32 hsl = 64;
     while (u64(hsl) < 2 * np && hsl < a.slots) hsl <<= 1;
     HashAdd add{hk, hv, hsl - 1, a.err};
-    products_item<ColT>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, row0, a.LB,
-                        &s_chunk, add);
+    products_item<ColT, u64>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, row0, a.LB,
+                             &s_chunk, add);
     __syncthreads();
     const int sidx = a.split_of_tile[t];
     if (sidx < 0) {
@@ -877,9 +923,9 @@ void read_scalars(fcc_ctx *ctx, u64 *d_sc) {
 
 u32 scalar32(fcc_ctx *ctx, int s) { return u32(ctx->h_scalars[s] & 0xFFFFFFFFu); }
 
-int grid_tiles(fcc_ctx *ctx, const void *kernel, size_t smem, u32 nitems) {
+int grid_tiles(fcc_ctx *ctx, const void *kernel, int threads, size_t smem, u32 nitems) {
   int per_sm = 0;
-  FCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTileThreads, smem));
+  FCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
   if (per_sm < 1) throw Error{FCC_ERR_CUDA, "tile kernel does not fit on an SM"};
   i64 g = i64(per_sm) * ctx->num_sms;
   if (g > i64(nitems)) g = nitems;
@@ -1124,6 +1170,8 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   bool sentinel = dense && !tiny && opt.dense_mode != FCC_DENSE_BITMASK &&
                   (opt.dense_mode == FCC_DENSE_SENTINEL || ptotal >= u64(ntiles) * area / 4);
   const ProdSrc src{P, rowA, sbA, valA, valB};
+  const int threads = opt.tile_threads > 0 ? opt.tile_threads : kTileThreads;
+  if (threads != 512 && threads != 1024) throw Error{FCC_ERR_ARG, "tile_threads must be 512 or 1024"};
   Decode dec{};
   dec.na = sa.lin.n_ext;
   dec.nb = sb.lin.n_ext;
@@ -1160,12 +1208,20 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
                   src, static_cast<const u32 *>(colB), u32(LB), u32(area), u32(words), gacc, gmask, o, dec,
                   ctx->d_err};
       const size_t smem = size_t(area) * 8 + (sentinel ? 0 : size_t(words) * 4);
-      const void *kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true>)
-                                  : reinterpret_cast<const void *>(k_contract_dense<false>);
+      const void *kern;
+      if (threads == 512) kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true, 512>)
+                                          : reinterpret_cast<const void *>(k_contract_dense<false, 512>);
+      else kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true, 1024>)
+                           : reinterpret_cast<const void *>(k_contract_dense<false, 1024>);
       FCC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-      const int grid = grid_tiles(ctx, kern, smem, nitems);
-      if (sentinel) k_contract_dense<true><<<grid, kTileThreads, smem, st>>>(a);
-      else k_contract_dense<false><<<grid, kTileThreads, smem, st>>>(a);
+      const int grid = grid_tiles(ctx, kern, threads, smem, nitems);
+      if (threads == 512) {
+        if (sentinel) k_contract_dense<true, 512><<<grid, 512, smem, st>>>(a);
+        else k_contract_dense<false, 512><<<grid, 512, smem, st>>>(a);
+      } else {
+        if (sentinel) k_contract_dense<true, 1024><<<grid, 1024, smem, st>>>(a);
+        else k_contract_dense<false, 1024><<<grid, 1024, smem, st>>>(a);
+      }
       FCC_LAUNCH_CHECK();
       tm.mark(4);
       if (nsplit > 0) {
@@ -1182,9 +1238,12 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
         using ColT = std::remove_const_t<std::remove_pointer_t<decltype(colptr)>>;
         HashArgs<ColT> a{items, nitems, counter, tile_row0, tile_abeg, split_of_tile, split_tiles, nsplit,
                          src, colptr, LB, u32(TL), hslots, t_hoff, t_hsz, gkeys, gvals, o, dec, ctx->d_err};
-        FCC_CUDA(cudaFuncSetAttribute(k_contract_hash<ColT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        const int grid = grid_tiles(ctx, reinterpret_cast<const void *>(k_contract_hash<ColT>), smem, nitems);
-        k_contract_hash<ColT><<<grid, kTileThreads, smem, st>>>(a);
+        const void *kern = threads == 512 ? reinterpret_cast<const void *>(k_contract_hash<ColT, 512>)
+                                          : reinterpret_cast<const void *>(k_contract_hash<ColT, 1024>);
+        FCC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        const int grid = grid_tiles(ctx, kern, threads, smem, nitems);
+        if (threads == 512) k_contract_hash<ColT, 512><<<grid, 512, smem, st>>>(a);
+        else k_contract_hash<ColT, 1024><<<grid, 1024, smem, st>>>(a);
         FCC_LAUNCH_CHECK();
         tm.mark(4);
         if (nsplit > 0) {

@@ -46,7 +46,8 @@ class Options(ctypes.Structure):
                 ("products_per_item", ctypes.c_int64), ("dense_cap", ctypes.c_int32),
                 ("hash_slots", ctypes.c_int32), ("timing", ctypes.c_int32),
                 ("pad0", ctypes.c_int32), ("capacity_hint", ctypes.c_int64),
-                ("dense_mode", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("dense_mode", ctypes.c_int32), ("tile_threads", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
 
     def __init__(self, **kw):
         super().__init__()

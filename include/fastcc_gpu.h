@@ -96,7 +96,8 @@ typedef struct fcc_options {
                                  smaller hint is not an error: the device counts every output
                                  and the call retries once with the exact count. */
   int32_t dense_mode;         /* fcc_dense_mode: how a dense tile marks touched positions */
-  int32_t reserved[3];
+  int32_t tile_threads;       /* threads per tile CTA: 512 or 1024; 0 = default */
+  int32_t reserved[2];
 } fcc_options;
 
 /* Touched-position tracking of the dense accumulator. Both emit every touched
