@@ -328,18 +328,22 @@ struct ProdSrc {
 // once (Zipf hub columns sit in most segments). Colliding lanes are summed
 // with shuffles first; only the lowest lane of each group keeps an update.
 // Returns true for the lanes whose (key, *v) must still be applied.
+// An update is fma(m, x, acc): normally m = va, x = vb. A group leader
+// carries m = 1 and x = the group's sum of products.
 template <class KeyT>
-__device__ __forceinline__ bool aggregate_lanes(KeyT key, double *v) {
+__device__ __forceinline__ bool aggregate_lanes(KeyT key, double *m, double *x) {
   const u32 lane = threadIdx.x & 31;
   const u32 peers = __match_any_sync(__activemask(), key);
   if (peers == (1u << lane)) return true;
   const int leader = __ffs(peers) - 1;
-  double s = *v;
+  const double p = *m * *x;
+  double s = p;
   for (u32 rest = peers & (peers - 1); rest; rest &= rest - 1) {
-    const double x = __shfl_sync(peers, *v, __ffs(rest) - 1);
-    if (int(lane) == leader) s += x;
+    const double y = __shfl_sync(peers, p, __ffs(rest) - 1);
+    if (int(lane) == leader) s += y;
   }
-  *v = s;
+  *m = 1.0;
+  *x = s;
   return int(lane) == leader;
 }
 
@@ -371,16 +375,16 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
           if (i < n) { c[k] = __ldg(&colB[b0 + i]); v[k] = __ldg(&s.valB[b0 + i]); }
         }
         KeyT key[kBatch];
-        double val[kBatch];
+        double m[kBatch];
         u32 valid = 0;
 #pragma unroll
         for (int k = 0; k < kBatch; k++) {
           const u32 i = o + k * 32 + lane;
           key[k] = base + KeyT(c[k]);
-          val[k] = va * v[k];
+          m[k] = va;
           if (i < n) valid |= 1u << k;
         }
-        add.batch(key, val, valid);
+        add.batch(key, m, v, valid);
       }
       pos = stop;
       if (stop == pe) ++e;
@@ -409,15 +413,15 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
           for (int k = 0; k < kBatch; k++)
             if (o + k < n) { c[k] = __ldg(&colB[b0 + o + k]); v[k] = __ldg(&s.valB[b0 + o + k]); }
           KeyT key[kBatch];
-          double val[kBatch];
+          double m[kBatch];
           u32 valid = 0;
 #pragma unroll
           for (int k = 0; k < kBatch; k++) {
             key[k] = base + KeyT(c[k]);
-            val[k] = va * v[k];
-            if (o + k < n && aggregate_lanes(key[k], &val[k])) valid |= 1u << k;
+            m[k] = va;
+            if (o + k < n && aggregate_lanes(key[k], &m[k], &v[k])) valid |= 1u << k;
           }
-          add.batch(key, val, valid);
+          add.batch(key, m, v, valid);
         }
       }
       pos = __shfl_sync(kFull, tg, g - 1);
@@ -566,7 +570,8 @@ template <bool kSentinel>
 struct DenseAdd {
   double *acc;
   u32 *mask;
-  __device__ __forceinline__ void batch(const u32 (&key)[kBatch], const double (&val)[kBatch], u32 valid) const {
+  __device__ __forceinline__ void batch(const u32 (&key)[kBatch], const double (&m)[kBatch],
+                                        const double (&x)[kBatch], u32 valid) const {
     unsigned long long old[kBatch];
 #pragma unroll
     for (int k = 0; k < kBatch; k++)
@@ -575,9 +580,9 @@ struct DenseAdd {
 #pragma unroll
     for (int k = 0; k < kBatch; k++)
       if ((valid >> k) & 1u) {
-        const unsigned long long got =
-            atomicCAS(reinterpret_cast<unsigned long long *>(&acc[key[k]]), old[k],
-                      (unsigned long long)__double_as_longlong(__longlong_as_double((long long)old[k]) + val[k]));
+        const unsigned long long got = atomicCAS(
+            reinterpret_cast<unsigned long long *>(&acc[key[k]]), old[k],
+            (unsigned long long)__double_as_longlong(fma(m[k], x[k], __longlong_as_double((long long)old[k]))));
         if (got != old[k]) fail |= 1u << k;
       }
 #pragma unroll
@@ -586,8 +591,9 @@ struct DenseAdd {
         unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(&acc[key[k]]), assumed;
         do {
           assumed = cur;
-          cur = atomicCAS(reinterpret_cast<unsigned long long *>(&acc[key[k]]), assumed,
-                          (unsigned long long)__double_as_longlong(__longlong_as_double((long long)assumed) + val[k]));
+          cur = atomicCAS(
+              reinterpret_cast<unsigned long long *>(&acc[key[k]]), assumed,
+              (unsigned long long)__double_as_longlong(fma(m[k], x[k], __longlong_as_double((long long)assumed))));
         } while (cur != assumed);
       }
     }
@@ -734,23 +740,34 @@ struct HashAdd {
   double *hv;
   u32 hmask;
   u32 *err;
-  __device__ __forceinline__ void operator()(u64 key, double v) const {
+  // hv[slot] = fma(m, x, hv[slot]) with a CAS loop (one FP64 instruction per
+  // multiply-add: FP64 issue rate bounds these kernels on this GPU).
+  __device__ __forceinline__ void fma_slot(u32 h, double m, double x) const {
+    unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(&hv[h]), assumed;
+    do {
+      assumed = cur;
+      cur = atomicCAS(reinterpret_cast<unsigned long long *>(&hv[h]), assumed,
+                      (unsigned long long)__double_as_longlong(fma(m, x, __longlong_as_double((long long)assumed))));
+    } while (cur != assumed);
+  }
+  __device__ __forceinline__ void operator()(u64 key, double m, double x) const {
     u32 h = hash_slot(key) & hmask;
     for (u32 probe = 0; probe <= hmask; ++probe) {
       const u64 cur = *reinterpret_cast<volatile u64 *>(&hk[h]);
-      if (cur == key) { atomicAdd(&hv[h], v); return; }
+      if (cur == key) { fma_slot(h, m, x); return; }
       if (cur == kEmptyKey) {
         const u64 old = atomicCAS(reinterpret_cast<unsigned long long *>(&hk[h]), kEmptyKey, key);
-        if (old == kEmptyKey || old == key) { atomicAdd(&hv[h], v); return; }
+        if (old == kEmptyKey || old == key) { fma_slot(h, m, x); return; }
       }
       h = (h + 1) & hmask;
     }
     atomicOr(err, ERRB_HASH);
   }
-  __device__ __forceinline__ void batch(const u64 (&key)[kBatch], const double (&val)[kBatch], u32 valid) const {
+  __device__ __forceinline__ void batch(const u64 (&key)[kBatch], const double (&m)[kBatch],
+                                        const double (&x)[kBatch], u32 valid) const {
 #pragma unroll
     for (int k = 0; k < kBatch; k++)
-      if ((valid >> k) & 1u) (*this)(key[k], val[k]);
+      if ((valid >> k) & 1u) (*this)(key[k], m[k], x[k]);
   }
 };
 
