@@ -328,8 +328,8 @@ struct ProdSrc {
 // once (Zipf hub columns sit in most segments). Colliding lanes are summed
 // with shuffles first; only the lowest lane of each group keeps an update.
 // Returns true for the lanes whose (key, *v) must still be applied.
-// An update is fma(m, x, acc): normally m = va, x = vb. A group leader
-// carries m = 1 and x = the group's sum of products.
+// An update adds m * x: normally m = va, x = vb. A group leader carries
+// m = 1 and x = the group's sum of products.
 template <class KeyT>
 __device__ __forceinline__ bool aggregate_lanes(KeyT key, double *m, double *x) {
   const u32 lane = threadIdx.x & 31;
@@ -563,45 +563,23 @@ __device__ void flush_dense(double *acc, u32 *mask, u32 area, u32 words, double 
   }
 }
 
-// Shared-memory FP64 accumulation. The loads and compare-and-swaps of a batch
-// are issued back to back, so a thread has kBatch updates in flight; a CAS
-// that lost a race is retried on its own.
+// Shared-memory FP64 accumulation: one DMUL and one shared-memory atomic add
+// per multiply-add. The shared-memory unit performs the FP64 add itself
+// (measured on GB300: 1.4 such updates per clock per SM, against 1.0 for a
+// compare-and-swap loop and about 1.3 FP64-pipe instructions per clock), and
+// the update returns nothing, so a warp never waits on it.
 template <bool kSentinel>
 struct DenseAdd {
   double *acc;
   u32 *mask;
   __device__ __forceinline__ void batch(const u32 (&key)[kBatch], const double (&m)[kBatch],
                                         const double (&x)[kBatch], u32 valid) const {
-    unsigned long long old[kBatch];
-#pragma unroll
-    for (int k = 0; k < kBatch; k++)
-      if ((valid >> k) & 1u) old[k] = *reinterpret_cast<volatile unsigned long long *>(&acc[key[k]]);
-    u32 fail = 0;
 #pragma unroll
     for (int k = 0; k < kBatch; k++)
       if ((valid >> k) & 1u) {
-        const unsigned long long got = atomicCAS(
-            reinterpret_cast<unsigned long long *>(&acc[key[k]]), old[k],
-            (unsigned long long)__double_as_longlong(fma(m[k], x[k], __longlong_as_double((long long)old[k]))));
-        if (got != old[k]) fail |= 1u << k;
+        atomicAdd(&acc[key[k]], m[k] * x[k]);
+        if (!kSentinel) atomicOr(&mask[key[k] >> 5], 1u << (key[k] & 31));
       }
-#pragma unroll
-    for (int k = 0; k < kBatch; k++) {
-      if ((fail >> k) & 1u) {
-        unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(&acc[key[k]]), assumed;
-        do {
-          assumed = cur;
-          cur = atomicCAS(
-              reinterpret_cast<unsigned long long *>(&acc[key[k]]), assumed,
-              (unsigned long long)__double_as_longlong(fma(m[k], x[k], __longlong_as_double((long long)assumed))));
-        } while (cur != assumed);
-      }
-    }
-    if (!kSentinel) {
-#pragma unroll
-      for (int k = 0; k < kBatch; k++)
-        if ((valid >> k) & 1u) atomicOr(&mask[key[k] >> 5], 1u << (key[k] & 31));
-    }
   }
 };
 
@@ -740,24 +718,14 @@ struct HashAdd {
   double *hv;
   u32 hmask;
   u32 *err;
-  // hv[slot] = fma(m, x, hv[slot]) with a CAS loop (one FP64 instruction per
-  // multiply-add: FP64 issue rate bounds these kernels on this GPU).
-  __device__ __forceinline__ void fma_slot(u32 h, double m, double x) const {
-    unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(&hv[h]), assumed;
-    do {
-      assumed = cur;
-      cur = atomicCAS(reinterpret_cast<unsigned long long *>(&hv[h]), assumed,
-                      (unsigned long long)__double_as_longlong(fma(m, x, __longlong_as_double((long long)assumed))));
-    } while (cur != assumed);
-  }
   __device__ __forceinline__ void operator()(u64 key, double m, double x) const {
     u32 h = hash_slot(key) & hmask;
     for (u32 probe = 0; probe <= hmask; ++probe) {
       const u64 cur = *reinterpret_cast<volatile u64 *>(&hk[h]);
-      if (cur == key) { fma_slot(h, m, x); return; }
+      if (cur == key) { atomicAdd(&hv[h], m * x); return; }
       if (cur == kEmptyKey) {
         const u64 old = atomicCAS(reinterpret_cast<unsigned long long *>(&hk[h]), kEmptyKey, key);
-        if (old == kEmptyKey || old == key) { fma_slot(h, m, x); return; }
+        if (old == kEmptyKey || old == key) { atomicAdd(&hv[h], m * x); return; }
       }
       h = (h + 1) & hmask;
     }
