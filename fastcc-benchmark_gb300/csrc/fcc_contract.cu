@@ -47,6 +47,7 @@ struct Decode {
   int na, nb;
   int narrow;  // every radix and both spans < 2^32
   u64 ra[FCC_MAX_ORDER], rb[FCC_MAX_ORDER];
+  const u32 *inv_col;  // renumbered B column -> B external index (NULL: identity)
 };
 
 struct Out {
@@ -81,6 +82,7 @@ __device__ __forceinline__ u32 hash_slot(u64 key) {
 __device__ __forceinline__ void emit(const Out &o, const Decode &d, u64 idx, u64 row, u64 col,
                                      double v) {
   u32 *c = o.coords;
+  if (d.inv_col) col = d.inv_col[col];
   if (d.narrow) {
     u32 r = u32(row);
     for (int e = d.na - 1; e > 0; --e) {
@@ -299,6 +301,48 @@ __global__ void k_item_write(const u32 *__restrict__ ntiles_p, const u32 *__rest
   }
 }
 
+// ------------------------------------------------- hot-column remap ----
+//
+// B external indices are renumbered by descending frequency so that "one of
+// the `hot` most frequent columns" is the test q < hot in the tile kernels;
+// inv_col maps back when outputs are written.
+
+template <class ColT>
+__global__ void k_col_hist(const ColT *__restrict__ col, i64 n, u32 *__restrict__ count) {
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
+    const u32 c = u32(col[i]);
+    const u32 peers = __match_any_sync(__activemask(), c);
+    if ((threadIdx.x & 31) == u32(__ffs(peers) - 1)) atomicAdd(&count[c], u32(__popc(peers)));
+  }
+}
+
+__global__ void k_col_sortkeys(const u32 *__restrict__ count, u64 LB, int bits, u64 *__restrict__ key,
+                               u32 *__restrict__ idx) {
+  for (u64 c = u64(blockIdx.x) * blockDim.x + threadIdx.x; c < LB; c += u64(gridDim.x) * blockDim.x) {
+    key[c] = (u64(~count[c]) << bits) | c;  // ascending = most frequent first
+    idx[c] = u32(c);
+  }
+}
+
+__global__ void k_col_tables(const u64 *__restrict__ key, u64 LB, int bits, u32 hot, u32 *__restrict__ colmap,
+                             u32 *__restrict__ inv, unsigned long long *hot_count) {
+  u64 part = 0;
+  for (u64 r = u64(blockIdx.x) * blockDim.x + threadIdx.x; r < LB; r += u64(gridDim.x) * blockDim.x) {
+    const u32 c = u32(key[r] & ((u64(1) << bits) - 1));
+    colmap[c] = u32(r);
+    inv[r] = c;
+    if (r < hot) part += u64(~u32(key[r] >> bits));
+  }
+  part = __reduce_add_sync(kFull, u32(part));  // hot counts fit 32 bits per warp (nnz < 2^31)
+  if ((threadIdx.x & 31) == 0 && part) atomicAdd(hot_count, (unsigned long long)part);
+}
+
+template <class ColT>
+__global__ void k_apply_colmap(ColT *__restrict__ col, i64 n, const u32 *__restrict__ colmap) {
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x)
+    col[i] = ColT(colmap[u32(col[i])]);
+}
+
 // --------------------------------------------------------- tile kernels ----
 //
 // Work: an item is a range [p0, p1) of the global multiply-add index space
@@ -462,6 +506,7 @@ struct DenseArgs {
   ProdSrc src;
   const u32 *colB;
   u32 LB, area, words;
+  u32 hot;  // renumbered columns [0, hot) are accumulated per warp (row tiles only)
   double *gacc;
   u32 *gmask;
   Out out;
@@ -568,26 +613,68 @@ __device__ void flush_dense(double *acc, u32 *mask, u32 area, u32 words, double 
 // (measured on GB300: 1.4 such updates per clock per SM, against 1.0 for a
 // compare-and-swap loop and about 1.3 FP64-pipe instructions per clock), and
 // the update returns nothing, so a warp never waits on it.
+//
+// Zipf-like operands send most multiply-adds of a row to a few columns (for
+// Zipf(1.2) over 20,000 columns, ~70% land in the 64 most frequent). Updates
+// to one address from many warps serialise in the shared-memory atomic unit,
+// so the most frequent columns (renumbered to [0, hot) on the host) get a
+// private copy per warp, summed into the tile before the drain.
 template <bool kSentinel>
 struct DenseAdd {
   double *acc;
   u32 *mask;
+  double *priv;  // this warp's copy of the hot columns
+  u32 *pmask;    // its touched bits (bitmask mode)
+  u32 hot;
   __device__ __forceinline__ void batch(const u32 (&key)[kBatch], const double (&m)[kBatch],
                                         const double (&x)[kBatch], u32 valid) const {
 #pragma unroll
     for (int k = 0; k < kBatch; k++)
       if ((valid >> k) & 1u) {
-        atomicAdd(&acc[key[k]], m[k] * x[k]);
-        if (!kSentinel) atomicOr(&mask[key[k] >> 5], 1u << (key[k] & 31));
+        const u32 q = key[k];
+        if (q < hot) {
+          atomicAdd(&priv[q], m[k] * x[k]);
+          if (!kSentinel) atomicOr(&pmask[q >> 5], 1u << (q & 31));
+        } else {
+          atomicAdd(&acc[q], m[k] * x[k]);
+          if (!kSentinel) atomicOr(&mask[q >> 5], 1u << (q & 31));
+        }
       }
   }
 };
 
+// Sums the per-warp hot-column copies into tile positions [0, hot) and resets
+// them. Call between barriers.
+template <bool kSentinel>
+__device__ __forceinline__ void merge_hot_dense(double *acc, u32 *mask, double *priv, u32 *pmask, u32 hot) {
+  const u32 nwarps = blockDim.x >> 5, pw = hot / 32;
+  const double init = kSentinel ? __longlong_as_double((long long)kNegZero) : 0.0;
+  for (u32 i = threadIdx.x; i < hot; i += blockDim.x) {
+    double s = init;
+    u32 touched = 0;
+    for (u32 w = 0; w < nwarps; w++) {
+      s += priv[w * hot + i];
+      priv[w * hot + i] = init;
+      if (!kSentinel) touched |= (pmask[w * pw + i / 32] >> (i & 31)) & 1u;
+    }
+    acc[i] = s;
+    if (!kSentinel && touched) atomicOr(&mask[i >> 5], 1u << (i & 31));
+  }
+  __syncthreads();
+  if (!kSentinel)
+    for (u32 i = threadIdx.x; i < nwarps * pw; i += blockDim.x) pmask[i] = 0u;
+}
+
 template <bool kSentinel, int kThreads>
 __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
+  // layout: acc[area] | mask[words] (bitmask mode) | priv[nwarps*hot] | pmask[nwarps*hot/32]
   double *acc = reinterpret_cast<double *>(smem);
   u32 *mask = reinterpret_cast<u32 *>(acc + a.area);
+  const u32 nwarps = blockDim.x >> 5, warp = threadIdx.x >> 5;
+  const size_t off = (size_t(a.area) * 8 + (kSentinel ? 0 : size_t(a.words) * 4) + 15) & ~size_t(15);
+  double *priv = reinterpret_cast<double *>(smem + off);
+  u32 *pmask = reinterpret_cast<u32 *>(priv + size_t(nwarps) * a.hot);
   __shared__ u32 s_item, s_chunk;
   __shared__ u32 s_wcnt[32];
   __shared__ u64 s_base;
@@ -596,7 +683,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
   for (u32 i = tid; i < a.area; i += blockDim.x) acc[i] = init;
   if (!kSentinel)
     for (u32 i = tid; i < a.words; i += blockDim.x) mask[i] = 0u;
-  DenseAdd<kSentinel> add{acc, mask};
+  for (u32 i = tid; i < nwarps * a.hot; i += blockDim.x) priv[i] = init;
+  if (!kSentinel)
+    for (u32 i = tid; i < nwarps * (a.hot / 32); i += blockDim.x) pmask[i] = 0u;
+  DenseAdd<kSentinel> add{acc, mask, priv + size_t(warp) * a.hot, pmask + size_t(warp) * (a.hot / 32), a.hot};
   for (;;) {
     if (tid == 0) {
       s_item = atomicAdd(a.counter, 1u);
@@ -611,6 +701,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
     products_item<u32, u32>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, row0, a.LB,
                             &s_chunk, add);
     __syncthreads();
+    if (a.hot) {
+      merge_hot_dense<kSentinel>(acc, mask, priv, pmask, a.hot);
+      __syncthreads();
+    }
     const int sidx = a.split_of_tile[t];
     if (sidx < 0)
       drain_dense<kSentinel>(acc, mask, a.area, a.words, a.LB, row0, a.out, a.dec, a.err, s_wcnt, &s_base);
@@ -649,6 +743,7 @@ struct HashArgs {
   u64 LB;
   u32 TL;
   u32 slots;        // shared-memory slots (power of two)
+  u32 hot;          // renumbered columns [0, hot) accumulated per warp (TL == 1 only)
   const u64 *hoff;  // per tile: first slot of its global region (split tiles)
   const u64 *hsz;   // per tile: global region size, a power of two (split tiles)
   u64 *gkeys;
@@ -718,14 +813,25 @@ struct HashAdd {
   double *hv;
   u32 hmask;
   u32 *err;
+  double *priv;  // this warp's copy of the hot columns (keys [0, hot) when TL == 1)
+  u32 *pmask;
+  u32 hot;
   __device__ __forceinline__ void operator()(u64 key, double m, double x) const {
+    if (key < hot) {
+      atomicAdd(&priv[key], m * x);
+      atomicOr(&pmask[key >> 5], 1u << (key & 31));
+      return;
+    }
+    insert(key, m * x);
+  }
+  __device__ __forceinline__ void insert(u64 key, double p) const {
     u32 h = hash_slot(key) & hmask;
     for (u32 probe = 0; probe <= hmask; ++probe) {
       const u64 cur = *reinterpret_cast<volatile u64 *>(&hk[h]);
-      if (cur == key) { atomicAdd(&hv[h], m * x); return; }
+      if (cur == key) { atomicAdd(&hv[h], p); return; }
       if (cur == kEmptyKey) {
         const u64 old = atomicCAS(reinterpret_cast<unsigned long long *>(&hk[h]), kEmptyKey, key);
-        if (old == kEmptyKey || old == key) { atomicAdd(&hv[h], m * x); return; }
+        if (old == kEmptyKey || old == key) { atomicAdd(&hv[h], p); return; }
       }
       h = (h + 1) & hmask;
     }
@@ -742,13 +848,19 @@ struct HashAdd {
 template <class ColT, int kThreads>
 __global__ void __launch_bounds__(kThreads, 1) k_contract_hash(HashArgs<ColT> a) {
   extern __shared__ __align__(16) unsigned char smem[];
+  // layout: hk[slots] | hv[slots] | priv[nwarps*hot] | pmask[nwarps*hot/32]
   u64 *hk = reinterpret_cast<u64 *>(smem);
   double *hv = reinterpret_cast<double *>(hk + a.slots);
+  const u32 nwarps = blockDim.x >> 5, warp = threadIdx.x >> 5, pw = a.hot / 32;
+  double *priv = hv + a.slots;
+  u32 *pmask = reinterpret_cast<u32 *>(priv + size_t(nwarps) * a.hot);
   __shared__ u32 s_item, s_chunk;
   __shared__ u32 s_wcnt[32];
   __shared__ u64 s_base;
   const int tid = threadIdx.x;
   for (u32 i = tid; i < a.slots; i += blockDim.x) { hk[i] = kEmptyKey; hv[i] = 0.0; }
+  for (u32 i = tid; i < nwarps * a.hot; i += blockDim.x) priv[i] = 0.0;
+  for (u32 i = tid; i < nwarps * pw; i += blockDim.x) pmask[i] = 0u;
   for (;;) {
     if (tid == 0) {
       s_item = atomicAdd(a.counter, 1u);
@@ -763,10 +875,25 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_hash(HashArgs<ColT> a)
     const u64 np = item.p1 - item.p0;
     u32 hsl = 64;
     while (u64(hsl) < 2 * np && hsl < a.slots) hsl <<= 1;
-    HashAdd add{hk, hv, hsl - 1, a.err};
+    HashAdd add{hk, hv, hsl - 1, a.err, priv + size_t(warp) * a.hot, pmask + size_t(warp) * pw, a.hot};
     products_item<ColT, u64>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, row0, a.LB,
                              &s_chunk, add);
     __syncthreads();
+    if (a.hot) {  // per-warp hot columns -> the table (their keys were counted in np)
+      for (u32 i = tid; i < a.hot; i += blockDim.x) {
+        double sum = 0.0;
+        u32 touched = 0;
+        for (u32 w = 0; w < nwarps; w++) {
+          sum += priv[w * a.hot + i];
+          priv[w * a.hot + i] = 0.0;
+          touched |= (pmask[w * pw + i / 32] >> (i & 31)) & 1u;
+        }
+        if (touched) add.insert(i, sum);
+      }
+      __syncthreads();
+      for (u32 i = tid; i < nwarps * pw; i += blockDim.x) pmask[i] = 0u;
+      __syncthreads();
+    }
     const int sidx = a.split_of_tile[t];
     if (sidx < 0) {
       drain_hash(hk, hv, hsl, a.LB, a.TL, row0, a.out, a.dec, a.err, s_wcnt, &s_base);
@@ -892,7 +1019,7 @@ const double *upload_values(fcc_ctx *ctx, const fcc_tensor *t) {
 
 // Device scalar block: slot numbers in a u64 array.
 enum Scalar { S_NSEG = 0, S_NA2, S_NTILES, S_NITEMS, S_NSPLIT, S_CAP, S_HASH, S_CURSOR, S_COUNTER,
-              S_PTOTAL, S_ERR, S_TINY, S_COUNT };
+              S_PTOTAL, S_ERR, S_TINY, S_HOT, S_COUNT };
 
 // Copies the scalar block and the error word to pinned host memory, waits,
 // and raises the error bits that are not recoverable.
@@ -1098,6 +1225,33 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   u64 pmax = opt.products_per_item > 0 ? u64(opt.products_per_item) : (dense ? (u64(1) << 20) : u64(hslots / 2));
   if (!dense && pmax > hslots / 2) pmax = hslots / 2;
   const u64 area = TL * LB;
+  const int threads = opt.tile_threads > 0 ? opt.tile_threads : kTileThreads;
+  if (threads != 512 && threads != 1024) throw Error{FCC_ERR_ARG, "tile_threads must be 512 or 1024"};
+  if (opt.hot_columns < -1 || (opt.hot_columns > 0 && opt.hot_columns % 32))
+    throw Error{FCC_ERR_ARG, "hot_columns must be -1, 0 or a positive multiple of 32"};
+
+  // Hot columns (row tiles only): frequency of each B column, most frequent first.
+  const u32 hot_want = opt.hot_columns > 0 ? u32(opt.hot_columns) : 128u;
+  const bool hot_try = TL == 1 && opt.hot_columns >= 0 && LB <= (u64(1) << 26) && LB >= 2 * u64(hot_want);
+  u32 *colmap = nullptr, *inv_col = nullptr;
+  if (hot_try) {
+    const int lbits = bits_for(LB - 1);
+    u32 *count = ar.get_n<u32>(LB);
+    u64 *ckey = ar.get_n<u64>(LB);
+    u32 *cidx = ar.get_n<u32>(LB);
+    colmap = ar.get_n<u32>(LB);
+    inv_col = ar.get_n<u32>(LB);
+    FCC_CUDA(cudaMemsetAsync(count, 0, sizeof(u32) * LB, st));
+    if (colb32) k_col_hist<u32><<<grid_for(nB, 256), 256, 0, st>>>(static_cast<const u32 *>(colB), nB, count);
+    else k_col_hist<u64><<<grid_for(nB, 256), 256, 0, st>>>(static_cast<const u64 *>(colB), nB, count);
+    FCC_LAUNCH_CHECK();
+    k_col_sortkeys<<<grid_for(i64(LB), 256), 256, 0, st>>>(count, LB, lbits, ckey, cidx);
+    FCC_LAUNCH_CHECK();
+    radix_sort_pairs(ckey, cidx, i64(LB), 32 + lbits, ar, st);
+    k_col_tables<<<grid_for(i64(LB), 256), 256, 0, st>>>(ckey, LB, lbits, hot_want, colmap, inv_col,
+                                                        reinterpret_cast<unsigned long long *>(d_sc + S_HOT));
+    FCC_LAUNCH_CHECK();
+  }
 
   u32 *tflag = ar.get_n<u32>(nA2), *tidx = ar.get_n<u32>(nA2);
   k_tile_flags<<<grid_for(nA2, 256), 256, 0, st>>>(rowA, nA2, TL, tflag);
@@ -1154,10 +1308,27 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   const u32 ntiles = scalar32(ctx, S_NTILES);
   bool sentinel = dense && !tiny && opt.dense_mode != FCC_DENSE_BITMASK &&
                   (opt.dense_mode == FCC_DENSE_SENTINEL || ptotal >= u64(ntiles) * area / 4);
+  // Per-warp hot columns when they draw a large share of B (auto: >= 10% of
+  // the entries in the 128 most frequent columns and >= 4x their uniform
+  // share) and the private copies fit next to the tile.
+  u32 hot = 0;
+  const u32 nwarps = u32(threads / 32);
+  if (hot_try) {
+    const double share = double(ctx->h_scalars[S_HOT]) / double(nB);
+    const bool want = opt.hot_columns > 0 || (share >= 0.10 && share >= 4.0 * double(hot_want) / double(LB));
+    const size_t base_smem = dense ? ((size_t(area) * 8 + (sentinel ? 0 : size_t(words) * 4) + 15) & ~size_t(15))
+                                   : size_t(hslots) * 16;
+    const size_t priv = size_t(nwarps) * hot_want * 8 + size_t(nwarps) * (hot_want / 32) * 4;
+    if (want && base_smem + priv <= smem_cap) {
+      hot = hot_want;
+      if (colb32) k_apply_colmap<u32><<<grid_for(nB, 256), 256, 0, st>>>(static_cast<u32 *>(colB), nB, colmap);
+      else k_apply_colmap<u64><<<grid_for(nB, 256), 256, 0, st>>>(static_cast<u64 *>(colB), nB, colmap);
+      FCC_LAUNCH_CHECK();
+    }
+  }
   const ProdSrc src{P, rowA, sbA, valA, valB};
-  const int threads = opt.tile_threads > 0 ? opt.tile_threads : kTileThreads;
-  if (threads != 512 && threads != 1024) throw Error{FCC_ERR_ARG, "tile_threads must be 512 or 1024"};
   Decode dec{};
+  dec.inv_col = hot ? inv_col : nullptr;
   dec.na = sa.lin.n_ext;
   dec.nb = sb.lin.n_ext;
   for (int e = 0; e < dec.na; e++) dec.ra[e] = sa.lin.ext_radix[e];
@@ -1190,9 +1361,10 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
         FCC_CUDA(cudaMemsetAsync(gmask, 0, sizeof(u32) * nsplit * words, st));
       }
       DenseArgs a{items, nitems, counter, tile_row0, tile_abeg, split_of_tile, split_tiles, nsplit,
-                  src, static_cast<const u32 *>(colB), u32(LB), u32(area), u32(words), gacc, gmask, o, dec,
+                  src, static_cast<const u32 *>(colB), u32(LB), u32(area), u32(words), hot, gacc, gmask, o, dec,
                   ctx->d_err};
-      const size_t smem = size_t(area) * 8 + (sentinel ? 0 : size_t(words) * 4);
+      const size_t smem = ((size_t(area) * 8 + (sentinel ? 0 : size_t(words) * 4) + 15) & ~size_t(15)) +
+                          size_t(nwarps) * hot * 8 + size_t(nwarps) * (hot / 32) * 4;
       const void *kern;
       if (threads == 512) kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true, 512>)
                                           : reinterpret_cast<const void *>(k_contract_dense<false, 512>);
@@ -1218,11 +1390,11 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
         FCC_CUDA(cudaMemsetAsync(gkeys, 0xFF, sizeof(u64) * hash_total, st));
         FCC_CUDA(cudaMemsetAsync(gvals, 0, sizeof(double) * hash_total, st));
       }
-      const size_t smem = size_t(hslots) * 16;
+      const size_t smem = size_t(hslots) * 16 + size_t(nwarps) * hot * 8 + size_t(nwarps) * (hot / 32) * 4;
       auto launch = [&](auto colptr) {
         using ColT = std::remove_const_t<std::remove_pointer_t<decltype(colptr)>>;
         HashArgs<ColT> a{items, nitems, counter, tile_row0, tile_abeg, split_of_tile, split_tiles, nsplit,
-                         src, colptr, LB, u32(TL), hslots, t_hoff, t_hsz, gkeys, gvals, o, dec, ctx->d_err};
+                         src, colptr, LB, u32(TL), hslots, hot, t_hoff, t_hsz, gkeys, gvals, o, dec, ctx->d_err};
         const void *kern = threads == 512 ? reinterpret_cast<const void *>(k_contract_hash<ColT, 512>)
                                           : reinterpret_cast<const void *>(k_contract_hash<ColT, 1024>);
         FCC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));

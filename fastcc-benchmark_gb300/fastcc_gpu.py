@@ -47,7 +47,7 @@ class Options(ctypes.Structure):
                 ("hash_slots", ctypes.c_int32), ("timing", ctypes.c_int32),
                 ("pad0", ctypes.c_int32), ("capacity_hint", ctypes.c_int64),
                 ("dense_mode", ctypes.c_int32), ("tile_threads", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 2)]
+                ("hot_columns", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
 
     def __init__(self, **kw):
         super().__init__()

@@ -39,6 +39,11 @@ VARIANTS = [
     {"dense_mode": F.DENSE_SENTINEL},
     {"dense_mode": F.DENSE_SENTINEL, "products_per_item": 9},
     {"dense_mode": F.DENSE_BITMASK, "products_per_item": 11},
+    {"hot_columns": 32, "rows_per_tile": 1},
+    {"hot_columns": 32, "rows_per_tile": 1, "dense_mode": F.DENSE_BITMASK, "products_per_item": 13},
+    {"hot_columns": 64, "accumulator": F.ACC_HASH},
+    {"hot_columns": 32, "accumulator": F.ACC_HASH, "products_per_item": 6, "tile_threads": 512},
+    {"tile_threads": 512, "hot_columns": -1},
 ]
 
 
