@@ -183,7 +183,8 @@ def run_profile_case(name):
     import fastcc_gpu as F
     import workloads
     if name == "zipf3-small":
-        w = workloads.zipf3(seed=1, nnz=2_500_000, dims=(10_000, 10_000, 250_000))
+        # same extents as the benchmark workload (same tile shape), a quarter of the nonzeros
+        w = workloads.zipf3(seed=1, nnz=2_500_000)
     elif name == "twomode-small":
         w = workloads.twomode(seed=1, nnz=1_250_000, dims=(2_500, 2_500, 1_000, 50))
     else:
