@@ -391,20 +391,41 @@ __device__ __forceinline__ bool aggregate_lanes(KeyT key, double *m, double *x) 
   return int(lane) == leader;
 }
 
+constexpr u64 kNoSkip = ~0ull;
+constexpr u32 kNoEntry = 0xFFFFFFFFu;
+
+// Multiply-adds of A entry e that fall inside [p0, p1).
+__device__ __forceinline__ u64 coverage(const u64 *__restrict__ P, u32 e, u64 p0, u64 p1) {
+  const u64 lo = max(__ldg(&P[e]), p0), hi = min(__ldg(&P[e + 1]), p1);
+  return hi > lo ? hi - lo : 0;
+}
+
+// One warp runs the multiply-adds [q0, q1) of an item [p0, p1). Entries that
+// cover >= skip multiply-adds of the item were run by the whole CTA and are
+// skipped. e0: the entry holding q0, or kNoEntry to search for it.
 template <class ColT, class KeyT, class Add>
 __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__restrict__ colB, u32 alo,
-                                               u32 ahi, u64 q0, u64 q1, u64 row0, u64 LB, Add &add) {
+                                               u32 ahi, u32 e0, u64 q0, u64 q1, u64 p0, u64 p1, u64 skip,
+                                               u64 row0, u64 LB, Add &add) {
   const u32 lane = threadIdx.x & 31;
-  u32 lo = alo, hi = ahi;  // last entry with P[e] <= q0
-  while (hi - lo > 1) {
-    const u32 mid = (lo + hi) >> 1;
-    if (__ldg(&s.P[mid]) <= q0) lo = mid; else hi = mid;
+  u32 e = e0;
+  if (e == kNoEntry) {
+    u32 lo = alo, hi = ahi;  // last entry with P[e] <= q0
+    while (hi - lo > 1) {
+      const u32 mid = (lo + hi) >> 1;
+      if (__ldg(&s.P[mid]) <= q0) lo = mid; else hi = mid;
+    }
+    e = lo;
   }
-  u32 e = lo;
   u64 pos = q0;
   while (pos < q1) {  // invariant: P[e] <= pos < P[e+1]
     const u64 pb = __ldg(&s.P[e]), pe = __ldg(&s.P[e + 1]);
     const u64 stop = min(pe, q1);
+    if (skip != kNoSkip && coverage(s.P, e, p0, p1) >= skip) {
+      pos = stop;
+      ++e;
+      continue;
+    }
     if (stop - pos >= kLongRun) {
       const double va = __ldg(&s.valA[e]);
       const KeyT base = KeyT((__ldg(&s.rowA[e]) - row0) * LB);
@@ -435,14 +456,16 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
     } else {
       const u32 el = e + lane;
       u64 sg = 0, tg = 0, pl = 0;
+      bool run_by_cta = false;
       if (el < ahi) {
         pl = __ldg(&s.P[el]);
         const u64 pr = __ldg(&s.P[el + 1]);
         sg = max(pl, pos);
         tg = min(pr, q1);
         if (sg > tg) sg = tg;
+        run_by_cta = skip != kNoSkip && coverage(s.P, el, p0, p1) >= skip;
       }
-      const bool is_short = sg < tg && (tg - sg) < kLongRun;
+      const bool is_short = sg < tg && (tg - sg) < kLongRun && !run_by_cta;
       const u32 stop_mask = __ballot_sync(kFull, !is_short);
       const u32 g = stop_mask ? u32(__ffs(stop_mask) - 1) : 32u;  // >= 1: lane 0 is short
       if (lane < g) {
@@ -474,7 +497,8 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
   }
 }
 
-// Runs the chunks of one item on the calling CTA (all threads must call).
+// Runs the chunks of one item on the calling CTA (all threads must call);
+// chunk starts are searched for.
 template <class ColT, class KeyT, class Add>
 __device__ __forceinline__ void products_item(const ProdSrc &s, const ColT *colB, u32 alo, u32 ahi, u64 p0,
                                               u64 p1, u64 row0, u64 LB, u32 *s_chunk, Add &add) {
@@ -490,7 +514,117 @@ __device__ __forceinline__ void products_item(const ProdSrc &s, const ColT *colB
     if (c >= nch) break;
     const u64 q0 = p0 + u64(c) * chunk;
     const u64 q1 = min(q0 + chunk, p1);
-    products_chunk<ColT, KeyT>(s, colB, alo, ahi, q0, q1, row0, LB, add);
+    products_chunk<ColT, KeyT>(s, colB, alo, ahi, kNoEntry, q0, q1, p0, p1, kNoSkip, row0, LB, add);
+  }
+}
+
+// ---- dense items in two phases ----
+//
+// Phase 1: an A entry with >= kCtaRun multiply-adds in the item is run by the
+// whole CTA. Its B segment holds distinct columns, so every tile position gets
+// at most one update from it and a plain FMA read-modify-write is exact;
+// barriers separate consecutive entries. On Zipf operands these entries hold
+// most multiply-adds (85% on the 10M-nonzero benchmark tensor).
+// Phase 2: the other entries, by warps pulling chunks, with compare-and-swap
+// FMAs. The item plan (built by one pass over the item's entries) lists the
+// phase-1 entries and the first entry of every chunk, so chunks start without
+// a search.
+
+constexpr u32 kCtaRun = 1024;
+constexpr int kCtaPer = 8;
+constexpr u32 kListMax = 1024;   // items hold at most kListMax * kCtaRun multiply-adds
+constexpr u32 kChunkMax = 2048;
+
+struct ItemPlan {
+  u32 ea, eb, nlong, nchunk, next;
+  u64 chunk;
+  u32 list[kListMax];
+  u32 start[kChunkMax];
+};
+
+__device__ void build_item_plan(const u64 *__restrict__ P, u32 alo, u32 ahi, u64 p0, u64 p1, ItemPlan &pl) {
+  const u32 tid = threadIdx.x, nwarps = blockDim.x >> 5;
+  if (tid == 0) {
+    u32 lo = alo, hi = ahi;  // last entry with P[e] <= p0
+    while (hi - lo > 1) {
+      const u32 mid = (lo + hi) >> 1;
+      if (__ldg(&P[mid]) <= p0) lo = mid; else hi = mid;
+    }
+    pl.ea = lo;
+    u32 l2 = lo, h2 = ahi;  // first entry with P[e] >= p1 (P[ahi] >= p1)
+    while (l2 < h2) {
+      const u32 mid = (l2 + h2) >> 1;
+      if (__ldg(&P[mid]) < p1) l2 = mid + 1; else h2 = mid;
+    }
+    pl.eb = l2;
+    const u64 np = p1 - p0;
+    u64 chunk = np / (4 * nwarps);
+    chunk = chunk < 256 ? 256 : (chunk > 4096 ? 4096 : chunk);
+    if ((np + chunk - 1) / chunk > kChunkMax) chunk = (np + kChunkMax - 1) / kChunkMax;
+    pl.chunk = chunk;
+    pl.nchunk = u32((np + chunk - 1) / chunk);
+    pl.nlong = 0;
+    pl.next = 0;
+  }
+  __syncthreads();
+  const u64 chunk = pl.chunk;
+  for (u32 e = pl.ea + tid; e < pl.eb; e += blockDim.x) {
+    const u64 lo = max(__ldg(&P[e]), p0), hi = min(__ldg(&P[e + 1]), p1);
+    if (hi <= lo) continue;
+    if (hi - lo >= kCtaRun) {
+      const u32 i = atomicAdd(&pl.nlong, 1u);
+      if (i < kListMax) pl.list[i] = e;
+    }
+    for (u64 c = (lo - p0 + chunk - 1) / chunk; c < (hi - p0 + chunk - 1) / chunk; c++) pl.start[c] = e;
+  }
+  __syncthreads();
+}
+
+template <bool kSentinel, class Add>
+__device__ void dense_item(const ProdSrc &s, const u32 *__restrict__ colB, u32 alo, u32 ahi, u64 p0, u64 p1,
+                           u64 row0, u32 LB, double *acc, u32 *mask, ItemPlan &pl, Add &add) {
+  build_item_plan(s.P, alo, ahi, p0, p1, pl);
+  const u32 tid = threadIdx.x, lane = tid & 31;
+  const u32 nlong = min(pl.nlong, kListMax);
+  for (u32 li = 0; li < nlong; li++) {
+    const u32 e = pl.list[li];
+    const u64 pb = __ldg(&s.P[e]);
+    const u64 lo = max(pb, p0), hi = min(__ldg(&s.P[e + 1]), p1);
+    const double va = __ldg(&s.valA[e]);
+    const u32 base = u32(__ldg(&s.rowA[e]) - row0) * LB;
+    const u32 b0 = __ldg(&s.sbA[e]) + u32(lo - pb);
+    const u32 n = u32(hi - lo);
+    for (u32 o = 0; o < n; o += blockDim.x * kCtaPer) {
+      u32 c[kCtaPer];
+      double v[kCtaPer];
+#pragma unroll
+      for (int k = 0; k < kCtaPer; k++) {
+        const u32 i = o + k * blockDim.x + tid;
+        if (i < n) { c[k] = __ldg(&colB[b0 + i]); v[k] = __ldg(&s.valB[b0 + i]); }
+      }
+#pragma unroll
+      for (int k = 0; k < kCtaPer; k++) {
+        const u32 i = o + k * blockDim.x + tid;
+        if (i < n) {
+          const u32 q = base + c[k];
+          acc[q] = fma(va, v[k], acc[q]);
+          if (!kSentinel) atomicOr(&mask[q >> 5], 1u << (q & 31));
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // phase 2
+  const u64 chunk = pl.chunk;
+  const u32 nch = pl.nchunk;
+  for (;;) {
+    u32 c = 0;
+    if (lane == 0) c = atomicAdd(&pl.next, 1u);
+    c = __shfl_sync(kFull, c, 0);
+    if (c >= nch) break;
+    const u64 q0 = p0 + u64(c) * chunk;
+    const u64 q1 = min(q0 + chunk, p1);
+    products_chunk<u32, u32>(s, colB, alo, ahi, pl.start[c], q0, q1, p0, p1, u64(kCtaRun), row0, LB, add);
   }
 }
 
@@ -514,77 +648,84 @@ struct DenseArgs {
   u32 *err;
 };
 
-// Word `cw + lane` of the touched bitmask of a dense tile. With kSentinel the
-// tile holds -0.0 at untouched positions and the bitmask is built by ballots.
+// The touched mask of positions [32w, 32w+32) of a dense tile, in every lane.
+// With kSentinel the tile holds -0.0 at untouched positions and the mask is a
+// ballot.
 template <bool kSentinel>
-__device__ __forceinline__ u32 tile_word(const double *acc, const u32 *mask, u32 area, u32 cw, u32 w1) {
-  const u32 lane = threadIdx.x & 31;
-  if (!kSentinel) {
-    const u32 w = cw + lane;
-    return w < w1 ? mask[w] : 0u;
-  }
-  u32 mine = 0;
-  for (u32 i = 0; i < 32 && cw + i < w1; i++) {
-    const u32 pos = (cw + i) * 32 + lane;
-    const bool t = pos < area && u64(__double_as_longlong(acc[pos])) != kNegZero;
-    const u32 b = __ballot_sync(kFull, t);
-    if (lane == i) mine = b;
-  }
-  return mine;
+__device__ __forceinline__ u32 group_mask(const double *acc, const u32 *mask, u32 area, u32 w) {
+  if (!kSentinel) return mask[w];
+  const u32 pos = w * 32 + (threadIdx.x & 31);
+  const bool t = pos < area && u64(__double_as_longlong(acc[pos])) != kNegZero;
+  return __ballot_sync(kFull, t);
 }
 
-// Emits every touched position of a dense tile with its value, coalesced per
-// warp, and resets it (mask words to 0; values to 0.0, or -0.0 with kSentinel).
+// Exclusive prefix sum of v over the block; *total gets the sum. s_warp holds
+// 32 entries. Ends with a barrier.
+__device__ __forceinline__ u32 block_excl_u32(u32 v, u32 *s_warp, u32 *total) {
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const u32 incl = warp_incl_u32(v);
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    u32 x = lane < nwarps ? s_warp[lane] : 0u;
+    x = warp_incl_u32(x);
+    if (lane < nwarps) s_warp[lane] = x;
+  }
+  __syncthreads();
+  const u32 before = warp ? s_warp[warp - 1] : 0u;
+  *total = s_warp[nwarps - 1];
+  __syncthreads();
+  return before + incl - v;
+}
+
+// Emits every touched position of a dense tile with its value and resets it
+// (mask words to 0; values to 0.0, or -0.0 with kSentinel). Pass 1 counts the
+// touched positions of each 32-position group, one prefix sum over the groups
+// reserves the output range, pass 2 writes each group's outputs contiguously.
+// s_cnt holds `words` (<= 4 * blockDim.x) entries.
 template <bool kSentinel>
 __device__ void drain_dense(double *acc, u32 *mask, u32 area, u32 words, u32 LB, u64 row0, const Out &out,
-                            const Decode &dec, u32 *err, u32 *s_wcnt, u64 *s_base) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-  const u32 wpw = ((words + nwarps - 1) / nwarps + 31) & ~31u;
-  const u32 w0 = min(words, u32(warp) * wpw), w1 = min(words, w0 + wpw);
-  u32 c = 0;
-  for (u32 cw = w0; cw < w1; cw += 32) c += __popc(tile_word<kSentinel>(acc, mask, area, cw, w1));
-  c = __reduce_add_sync(kFull, c);
-  if (lane == 0) s_wcnt[warp] = c;
-  __syncthreads();
-  if (tid == 0) {
-    u32 run = 0;
-    for (int w = 0; w < nwarps; w++) {
-      const u32 x = s_wcnt[w];
-      s_wcnt[w] = run;
-      run += x;
-    }
-    *s_base = reserve(out, run, err);
+                            const Decode &dec, u32 *err, u32 *s_cnt, u32 *s_warp, u64 *s_base) {
+  const u32 tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  for (u32 w = warp; w < words; w += nwarps) {
+    const u32 b = group_mask<kSentinel>(acc, mask, area, w);
+    if (lane == 0) s_cnt[w] = __popc(b);
   }
+  __syncthreads();
+  const u32 ipt = (words + blockDim.x - 1) / blockDim.x;  // groups per thread (<= 4)
+  u32 loc[4], sum = 0;
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const u32 w = tid * ipt + j;
+    loc[j] = (u32(j) < ipt && w < words) ? s_cnt[w] : 0u;
+    sum += loc[j];
+  }
+  u32 total;
+  u32 run = block_excl_u32(sum, s_warp, &total);
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const u32 w = tid * ipt + j;
+    if (u32(j) < ipt && w < words) s_cnt[w] = run;
+    run += loc[j];
+  }
+  if (tid == 0) *s_base = reserve(out, total, err);
   __syncthreads();
   const u64 base = *s_base;
   const bool write = base != ~0ull;
   const double reset = kSentinel ? __longlong_as_double((long long)kNegZero) : 0.0;
-  u64 run = write ? base + s_wcnt[warp] : 0;
-  for (u32 cw = w0; cw < w1; cw += 32) {
-    const u32 word = tile_word<kSentinel>(acc, mask, area, cw, w1);
-    const u32 incl = warp_incl_u32(__popc(word));
-    const u32 tot = __shfl_sync(kFull, incl, 31);
-    for (u32 kk = 0; kk < tot; kk += 32) {
-      const u32 k = kk + lane;
-      u32 lo = 0;
-#pragma unroll
-      for (u32 step = 16; step >= 1; step >>= 1) {
-        const u32 v = __shfl_sync(kFull, incl, lo + step - 1);
-        if (v <= k) lo += step;
-      }
-      const u32 wsrc = __shfl_sync(kFull, word, lo);
-      const u32 isrc = __shfl_sync(kFull, incl, lo);
-      if (k < tot) {
-        const u32 nth = k - (isrc - __popc(wsrc));
-        const u32 bit = __fns(wsrc, 0, int(nth) + 1);
-        const u32 pos = (cw + lo) * 32 + bit;
-        const double v = acc[pos];
-        acc[pos] = reset;
-        if (write) emit(out, dec, run + k, row0 + pos / LB, pos % LB, v);
-      }
+  const u32 lt = (1u << lane) - 1u;
+  for (u32 w = warp; w < words; w += nwarps) {
+    const u32 b = group_mask<kSentinel>(acc, mask, area, w);
+    if ((b >> lane) & 1u) {
+      const u32 pos = w * 32 + lane;
+      const double v = acc[pos];
+      acc[pos] = reset;
+      if (write) emit(out, dec, base + s_cnt[w] + __popc(b & lt), row0 + pos / LB, pos % LB, v);
     }
-    if (!kSentinel && cw + lane < w1) mask[cw + lane] = 0u;
-    run += tot;
+    if (!kSentinel) {
+      __syncwarp();
+      if (lane == 0) mask[w] = 0u;
+    }
   }
 }
 
@@ -668,7 +809,7 @@ __device__ __forceinline__ void merge_hot_dense(double *acc, u32 *mask, double *
       priv[w * hot + i] = init;
       if (!kSentinel) touched |= (pmask[w * pw + i / 32] >> (i & 31)) & 1u;
     }
-    acc[i] = s;
+    acc[i] += s;  // -0.0 + -0.0 stays the untouched sentinel
     if (!kSentinel && touched) atomicOr(&mask[i >> 5], 1u << (i & 31));
   }
   __syncthreads();
@@ -686,9 +827,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
   const size_t off = (size_t(a.area) * 8 + (kSentinel ? 0 : size_t(a.words) * 4) + 15) & ~size_t(15);
   double *priv = reinterpret_cast<double *>(smem + off);
   u32 *pmask = reinterpret_cast<u32 *>(priv + size_t(nwarps) * a.hot);
-  __shared__ u32 s_item, s_chunk;
-  __shared__ u32 s_wcnt[32];
+  __shared__ u32 s_item;
+  __shared__ u32 s_warp[32];
+  __shared__ u32 s_cnt[1024];
   __shared__ u64 s_base;
+  __shared__ ItemPlan plan;
   const int tid = threadIdx.x;
   const double init = kSentinel ? __longlong_as_double((long long)kNegZero) : 0.0;
   for (u32 i = tid; i < a.area; i += blockDim.x) acc[i] = init;
@@ -699,18 +842,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
     for (u32 i = tid; i < nwarps * (a.hot / 32); i += blockDim.x) pmask[i] = 0u;
   DenseAdd<kSentinel> add{acc, mask, priv + size_t(warp) * a.hot, pmask + size_t(warp) * (a.hot / 32), a.hot};
   for (;;) {
-    if (tid == 0) {
-      s_item = atomicAdd(a.counter, 1u);
-      s_chunk = 0;
-    }
+    if (tid == 0) s_item = atomicAdd(a.counter, 1u);
     __syncthreads();
     const u32 it = s_item;
     if (it >= a.nitems) break;
     const Item item = a.items[it];
     const u32 t = item.tile;
     const u64 row0 = a.tile_row0[t];
-    products_item<u32, u32>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, row0, a.LB,
-                            &s_chunk, add);
+    dense_item<kSentinel>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, row0, a.LB, acc,
+                          mask, plan, add);
     __syncthreads();
     if (a.hot) {
       merge_hot_dense<kSentinel>(acc, mask, priv, pmask, a.hot);
@@ -718,7 +858,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
     }
     const int sidx = a.split_of_tile[t];
     if (sidx < 0)
-      drain_dense<kSentinel>(acc, mask, a.area, a.words, a.LB, row0, a.out, a.dec, a.err, s_wcnt, &s_base);
+      drain_dense<kSentinel>(acc, mask, a.area, a.words, a.LB, row0, a.out, a.dec, a.err, s_cnt, s_warp,
+                             &s_base);
     else
       flush_dense<kSentinel>(acc, mask, a.area, a.words, a.gacc + u64(sidx) * a.area,
                              a.gmask + u64(sidx) * a.words);
@@ -727,12 +868,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
 }
 
 __global__ void __launch_bounds__(kTileThreads) k_merge_dense(DenseArgs a) {
-  __shared__ u32 s_wcnt[32];
+  __shared__ u32 s_warp[32];
+  __shared__ u32 s_cnt[1024];
   __shared__ u64 s_base;
   for (u32 s = blockIdx.x; s < a.nsplit; s += gridDim.x) {
     const u64 row0 = a.tile_row0[a.split_tiles[s]];
     drain_dense<false>(a.gacc + u64(s) * a.area, a.gmask + u64(s) * a.words, a.area, a.words, a.LB, row0,
-                       a.out, a.dec, a.err, s_wcnt, &s_base);
+                       a.out, a.dec, a.err, s_cnt, s_warp, &s_base);
     __syncthreads();
   }
 }
@@ -1215,7 +1357,9 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   // ---- plan ----
   const u64 LB = sb.span;
   const size_t smem_cap = ctx->smem_optin - 1024;
-  const u64 max_dense_area = (u64(smem_cap) * 8) / 65;  // 8 bytes + 1 mask bit per position
+  // the dense kernel's static shared memory (item plan, drain counts) comes first
+  const size_t dense_dyn_cap = smem_cap - (sizeof(ItemPlan) + 4096 + 512);
+  const u64 max_dense_area = std::min<u64>((u64(dense_dyn_cap) * 8) / 65, 32 * 1024);  // 8 B + 1 mask bit
   u64 dense_cap = opt.dense_cap > 0 ? std::min<u64>(u64(opt.dense_cap), max_dense_area) : max_dense_area;
   bool dense = LB <= dense_cap && opt.accumulator != FCC_ACC_HASH;
   if (opt.accumulator == FCC_ACC_DENSE && !dense)
@@ -1235,6 +1379,7 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   }
   u64 pmax = opt.products_per_item > 0 ? u64(opt.products_per_item) : (dense ? (u64(1) << 20) : u64(hslots / 2));
   if (!dense && pmax > hslots / 2) pmax = hslots / 2;
+  if (dense && pmax > u64(kListMax) * kCtaRun) pmax = u64(kListMax) * kCtaRun;
   const u64 area = TL * LB;
   const int threads = opt.tile_threads > 0 ? opt.tile_threads : kTileThreads;
   if (threads != 512 && threads != 1024) throw Error{FCC_ERR_ARG, "tile_threads must be 512 or 1024"};
@@ -1330,7 +1475,7 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     const size_t base_smem = dense ? ((size_t(area) * 8 + (sentinel ? 0 : size_t(words) * 4) + 15) & ~size_t(15))
                                    : size_t(hslots) * 16;
     const size_t priv = size_t(nwarps) * hot_want * 8 + size_t(nwarps) * (hot_want / 32) * 4;
-    if (want && base_smem + priv <= smem_cap) {
+    if (want && base_smem + priv <= (dense ? dense_dyn_cap : smem_cap)) {
       hot = hot_want;
       if (colb32) k_apply_colmap<u32><<<grid_for(nB, 256), 256, 0, st>>>(static_cast<u32 *>(colB), nB, colmap);
       else k_apply_colmap<u64><<<grid_for(nB, 256), 256, 0, st>>>(static_cast<u64 *>(colB), nB, colmap);
