@@ -79,6 +79,8 @@ __device__ __forceinline__ u32 hash_slot(u64 key) {
   return u32((key * 0x9E3779B97F4A7C15ull) >> 32) ^ u32(key >> 29);
 }
 
+// Output stores are evict-first (st.global.cs): the output streams through
+// L2 once and should not push out the B segments the tile kernels re-read.
 __device__ __forceinline__ void emit(const Out &o, const Decode &d, u64 idx, u64 row, u64 col,
                                      double v) {
   u32 *c = o.coords;
@@ -87,34 +89,34 @@ __device__ __forceinline__ void emit(const Out &o, const Decode &d, u64 idx, u64
     u32 r = u32(row);
     for (int e = d.na - 1; e > 0; --e) {
       u32 rad = u32(d.ra[e]), q = r / rad;
-      c[e * o.stride + idx] = r - q * rad;
+      __stcs(&c[e * o.stride + idx], r - q * rad);
       r = q;
     }
-    if (d.na > 0) c[idx] = r;
+    if (d.na > 0) __stcs(&c[idx], r);
     u32 s = u32(col);
     for (int e = d.nb - 1; e > 0; --e) {
       u32 rad = u32(d.rb[e]), q = s / rad;
-      c[(d.na + e) * o.stride + idx] = s - q * rad;
+      __stcs(&c[(d.na + e) * o.stride + idx], s - q * rad);
       s = q;
     }
-    if (d.nb > 0) c[d.na * o.stride + idx] = s;
+    if (d.nb > 0) __stcs(&c[d.na * o.stride + idx], s);
   } else {
     u64 r = row;
     for (int e = d.na - 1; e > 0; --e) {
       u64 q = r / d.ra[e];
-      c[e * o.stride + idx] = u32(r - q * d.ra[e]);
+      __stcs(&c[e * o.stride + idx], u32(r - q * d.ra[e]));
       r = q;
     }
-    if (d.na > 0) c[idx] = u32(r);
+    if (d.na > 0) __stcs(&c[idx], u32(r));
     u64 s = col;
     for (int e = d.nb - 1; e > 0; --e) {
       u64 q = s / d.rb[e];
-      c[(d.na + e) * o.stride + idx] = u32(s - q * d.rb[e]);
+      __stcs(&c[(d.na + e) * o.stride + idx], u32(s - q * d.rb[e]));
       s = q;
     }
-    if (d.nb > 0) c[d.na * o.stride + idx] = u32(s);
+    if (d.nb > 0) __stcs(&c[d.na * o.stride + idx], u32(s));
   }
-  o.vals[idx] = v;
+  __stcs(&o.vals[idx], v);
 }
 
 // Reserves `total` outputs with one atomic; ~0 marks "over capacity".
@@ -400,9 +402,12 @@ __device__ __forceinline__ u64 coverage(const u64 *__restrict__ P, u32 e, u64 p0
   return hi > lo ? hi - lo : 0;
 }
 
-// One warp runs the multiply-adds [q0, q1) of an item [p0, p1). Entries that
-// cover >= skip multiply-adds of the item were run by the whole CTA and are
-// skipped. e0: the entry holding q0, or kNoEntry to search for it.
+// One warp runs the multiply-adds [q0, q1) of an item [p0, p1), in windows of
+// 32 consecutive A entries (entry e + lane in each lane). Entries with >= skip
+// multiply-adds in the item were run by the whole CTA and are left out; the
+// others overlapping [q0, q1) are either streamed by the whole warp, one after
+// another (>= kLongRun multiply-adds in the chunk), or run one per lane.
+// e0: the entry holding q0, or kNoEntry to search for it.
 template <class ColT, class KeyT, class Add>
 __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__restrict__ colB, u32 alo,
                                                u32 ahi, u32 e0, u64 q0, u64 q1, u64 p0, u64 p1, u64 skip,
@@ -417,27 +422,43 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
     }
     e = lo;
   }
-  u64 pos = q0;
-  while (pos < q1) {  // invariant: P[e] <= pos < P[e+1]
-    const u64 pb = __ldg(&s.P[e]), pe = __ldg(&s.P[e + 1]);
-    const u64 stop = min(pe, q1);
-    if (skip != kNoSkip && coverage(s.P, e, p0, p1) >= skip) {
-      pos = stop;
-      ++e;
-      continue;
+  for (;; e += 32) {
+    const u32 el = e + lane;
+    u64 sg = 0, tg = 0, pl = 0;
+    if (el < ahi) {
+      pl = __ldg(&s.P[el]);
+      const u64 pr = __ldg(&s.P[el + 1]);
+      sg = max(pl, q0);
+      tg = min(pr, q1);
+      if (sg > tg) sg = tg;
+      if (skip != kNoSkip && min(pr, p1) - max(pl, p0) >= skip) tg = sg;  // run by the CTA
     }
-    if (stop - pos >= kLongRun) {
-      const double va = __ldg(&s.valA[e]);
-      const KeyT base = KeyT((__ldg(&s.rowA[e]) - row0) * LB);
-      const u32 b0 = __ldg(&s.sbA[e]) + u32(pos - pb);
-      const u32 n = u32(stop - pos);
-      for (u32 o = 0; o < n; o += 32 * kBatch) {
+    const bool any_left = __any_sync(kFull, el < ahi && pl < q1);
+    const u64 n = tg - sg;
+    u32 stream = __ballot_sync(kFull, n >= kLongRun);
+    const bool mine = n > 0 && n < kLongRun;
+    double va = 0.0;
+    KeyT base = 0;
+    u32 b0 = 0;
+    if (n > 0) {
+      va = __ldg(&s.valA[el]);
+      base = KeyT((__ldg(&s.rowA[el]) - row0) * LB);
+      b0 = __ldg(&s.sbA[el]) + u32(sg - pl);
+    }
+    while (stream) {  // warp-wide runs
+      const int j = __ffs(stream) - 1;
+      stream &= stream - 1;
+      const double wva = __shfl_sync(kFull, va, j);
+      const KeyT wbase = __shfl_sync(kFull, base, j);
+      const u32 wb0 = __shfl_sync(kFull, b0, j);
+      const u32 wn = u32(__shfl_sync(kFull, n, j));
+      for (u32 o = 0; o < wn; o += 32 * kBatch) {
         ColT c[kBatch];
         double v[kBatch];
 #pragma unroll
         for (int k = 0; k < kBatch; k++) {
           const u32 i = o + k * 32 + lane;
-          if (i < n) { c[k] = __ldg(&colB[b0 + i]); v[k] = __ldg(&s.valB[b0 + i]); }
+          if (i < wn) { c[k] = __ldg(&colB[wb0 + i]); v[k] = __ldg(&s.valB[wb0 + i]); }
         }
         KeyT key[kBatch];
         double m[kBatch];
@@ -445,55 +466,37 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
 #pragma unroll
         for (int k = 0; k < kBatch; k++) {
           const u32 i = o + k * 32 + lane;
-          key[k] = base + KeyT(c[k]);
-          m[k] = va;
-          if (i < n) valid |= 1u << k;
+          key[k] = wbase + KeyT(c[k]);
+          m[k] = wva;
+          if (i < wn) valid |= 1u << k;
         }
         add.batch(key, m, v, valid);
       }
-      pos = stop;
-      if (stop == pe) ++e;
-    } else {
-      const u32 el = e + lane;
-      u64 sg = 0, tg = 0, pl = 0;
-      bool run_by_cta = false;
-      if (el < ahi) {
-        pl = __ldg(&s.P[el]);
-        const u64 pr = __ldg(&s.P[el + 1]);
-        sg = max(pl, pos);
-        tg = min(pr, q1);
-        if (sg > tg) sg = tg;
-        run_by_cta = skip != kNoSkip && coverage(s.P, el, p0, p1) >= skip;
-      }
-      const bool is_short = sg < tg && (tg - sg) < kLongRun && !run_by_cta;
-      const u32 stop_mask = __ballot_sync(kFull, !is_short);
-      const u32 g = stop_mask ? u32(__ffs(stop_mask) - 1) : 32u;  // >= 1: lane 0 is short
-      if (lane < g) {
-        const double va = __ldg(&s.valA[el]);
-        const KeyT base = KeyT((__ldg(&s.rowA[el]) - row0) * LB);
-        const u32 b0 = __ldg(&s.sbA[el]) + u32(sg - pl);
-        const u32 n = u32(tg - sg);
-        for (u32 o = 0; o < n; o += kBatch) {
-          ColT c[kBatch];
-          double v[kBatch];
-#pragma unroll
-          for (int k = 0; k < kBatch; k++)
-            if (o + k < n) { c[k] = __ldg(&colB[b0 + o + k]); v[k] = __ldg(&s.valB[b0 + o + k]); }
-          KeyT key[kBatch];
-          double m[kBatch];
-          u32 valid = 0;
-#pragma unroll
-          for (int k = 0; k < kBatch; k++) {
-            key[k] = base + KeyT(c[k]);
-            m[k] = va;
-            if (o + k < n && aggregate_lanes(key[k], &m[k], &v[k])) valid |= 1u << k;
-          }
-          add.batch(key, m, v, valid);
-        }
-      }
-      pos = __shfl_sync(kFull, tg, g - 1);
-      e += g;
     }
+    if (mine) {  // one entry per lane
+      const u32 cnt = u32(n);
+      for (u32 o = 0; o < cnt; o += kBatch) {
+        ColT c[kBatch];
+        double v[kBatch];
+#pragma unroll
+        for (int k = 0; k < kBatch; k++)
+          if (o + k < cnt) { c[k] = __ldg(&colB[b0 + o + k]); v[k] = __ldg(&s.valB[b0 + o + k]); }
+        KeyT key[kBatch];
+        double m[kBatch];
+        u32 valid = 0;
+#pragma unroll
+        for (int k = 0; k < kBatch; k++) {
+          key[k] = base + KeyT(c[k]);
+          m[k] = va;
+          if (o + k < cnt && aggregate_lanes(key[k], &m[k], &v[k])) valid |= 1u << k;
+        }
+        add.batch(key, m, v, valid);
+      }
+    }
+    if (!any_left) break;
+    // the window's last entry reaches past q1: done
+    const u64 last_end = __shfl_sync(kFull, (el < ahi) ? __ldg(&s.P[el + 1]) : ~0ull, 31);
+    if (last_end >= q1) break;
   }
 }
 
