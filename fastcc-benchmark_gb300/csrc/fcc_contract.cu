@@ -357,7 +357,7 @@ __global__ void k_apply_colmap(ColT *__restrict__ col, i64 n, const u32 *__restr
 //  * shorter entries go one per lane, up to 32 at once, so rows made of many
 //    rare keys (hub rows of Zipf tensors) keep every lane busy.
 
-constexpr int kTileThreads = 1024;
+constexpr int kTileThreads = 512;  // default; 1024 is the other instantiation (tile_threads)
 constexpr int kBatch = 4;
 constexpr u32 kLongRun = 64;
 constexpr u64 kNegZero = 0x8000000000000000ull;
@@ -1391,7 +1391,7 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
 
   // Hot columns (row tiles only): frequency of each B column, most frequent first.
   const u32 hot_want = opt.hot_columns > 0 ? u32(opt.hot_columns) : 128u;
-  const bool hot_try = TL == 1 && opt.hot_columns >= 0 && LB <= (u64(1) << 26) && LB >= 2 * u64(hot_want);
+  const bool hot_try = TL == 1 && opt.hot_columns > 0 && LB <= (u64(1) << 26) && LB >= 2 * u64(hot_want);
   u32 *colmap = nullptr, *inv_col = nullptr;
   if (hot_try) {
     const int lbits = bits_for(LB - 1);
@@ -1467,14 +1467,14 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   const u32 ntiles = scalar32(ctx, S_NTILES);
   bool sentinel = dense && !tiny && opt.dense_mode != FCC_DENSE_BITMASK &&
                   (opt.dense_mode == FCC_DENSE_SENTINEL || ptotal >= u64(ntiles) * area / 4);
-  // Per-warp hot columns when they draw a large share of B (auto: >= 10% of
-  // the entries in the 128 most frequent columns and >= 4x their uniform
-  // share) and the private copies fit next to the tile.
+  // Per-warp hot columns on request (hot_columns > 0) when the private copies
+  // fit next to the tile. Not automatic: measured on the 10M-nonzero Zipf(1.2)
+  // benchmark tensor they cost more than the contention they remove, because
+  // its heavy segments spread over all columns.
   u32 hot = 0;
   const u32 nwarps = u32(threads / 32);
   if (hot_try) {
-    const double share = double(ctx->h_scalars[S_HOT]) / double(nB);
-    const bool want = opt.hot_columns > 0 || (share >= 0.10 && share >= 4.0 * double(hot_want) / double(LB));
+    const bool want = opt.hot_columns > 0;
     const size_t base_smem = dense ? ((size_t(area) * 8 + (sentinel ? 0 : size_t(words) * 4) + 15) & ~size_t(15))
                                    : size_t(hslots) * 16;
     const size_t priv = size_t(nwarps) * hot_want * 8 + size_t(nwarps) * (hot_want / 32) * 4;

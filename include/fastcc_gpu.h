@@ -96,10 +96,9 @@ typedef struct fcc_options {
                                  smaller hint is not an error: the device counts every output
                                  and the call retries once with the exact count. */
   int32_t dense_mode;         /* fcc_dense_mode: how a dense tile marks touched positions */
-  int32_t tile_threads;       /* threads per tile CTA: 512 or 1024; 0 = default */
+  int32_t tile_threads;       /* threads per tile CTA: 512 (default) or 1024 */
   int32_t hot_columns;        /* per-warp copies of the most frequent B columns in row tiles:
-                                 -1 off, 0 auto (128 when they draw a large share), or a count
-                                 (multiple of 32) */
+                                 0 or -1 off (default), or a count (multiple of 32) */
   int32_t reserved[1];
 } fcc_options;
 
