@@ -4,20 +4,34 @@
 
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <vector>
 
 #include "fcc_internal.cuh"
 
 namespace fcc {
-void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
-              const int32_t *ctrB, int k, const fcc_options &opt, fcc_result **out, i64 *products,
+void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+              const int32_t *ctrB, int k, const fcc_options &opt, fcc_result *res, i64 *products,
               bool count_only);
 }
 
 namespace {
 
 thread_local std::string g_last_error;  // errors without a context
+
+fcc::Runtime runtime_of(fcc_ctx *ctx) {
+  fcc::Runtime rt(ctx->arena);
+  rt.stream = ctx->stream;
+  rt.d_err = ctx->d_err;
+  rt.h_scalars = ctx->h_scalars;
+  rt.num_sms = ctx->num_sms;
+  rt.smem_optin = ctx->smem_optin;
+  rt.ev = ctx->ev;
+  rt.phase_ms = ctx->phase_ms;
+  rt.pool = ctx->pool;
+  return rt;
+}
 
 template <class F>
 int guarded(fcc_ctx *ctx, F &&f) {
@@ -38,6 +52,10 @@ int guarded(fcc_ctx *ctx, F &&f) {
 }
 
 }  // namespace
+
+namespace fcc {
+void set_thread_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace fcc
 
 extern "C" {
 
@@ -148,7 +166,13 @@ int fcc_contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const i
   *out = nullptr;
   fcc_options o;
   if (opts) o = *opts; else fcc_options_default(&o);
-  return guarded(ctx, [&] { fcc::contract(ctx, A, B, ctrA, ctrB, k, o, out, nullptr, false); });
+  return guarded(ctx, [&] {
+    fcc::Runtime rt = runtime_of(ctx);
+    std::unique_ptr<fcc_result> r(new fcc_result());
+    r->ctx = ctx;
+    fcc::contract(&rt, A, B, ctrA, ctrB, k, o, r.get(), nullptr, false);
+    *out = r.release();
+  });
 }
 
 int fcc_count_products(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
@@ -156,7 +180,10 @@ int fcc_count_products(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, c
   if (!ctx || !products) return FCC_ERR_ARG;
   fcc_options o;
   if (opts) o = *opts; else fcc_options_default(&o);
-  return guarded(ctx, [&] { fcc::contract(ctx, A, B, ctrA, ctrB, k, o, nullptr, products, true); });
+  return guarded(ctx, [&] {
+    fcc::Runtime rt = runtime_of(ctx);
+    fcc::contract(&rt, A, B, ctrA, ctrB, k, o, nullptr, products, true);
+  });
 }
 
 int fcc_result_info(const fcc_result *r, int32_t *order, int64_t *nnz, int64_t *products) {
@@ -210,7 +237,7 @@ int fcc_result_copy_to_host(const fcc_result *r, int32_t *coords, int64_t stride
 
 int fcc_result_free(fcc_result *r) {
   if (!r) return FCC_ERR_ARG;
-  if (r->ctx) {
+  if (r->ctx && r->owned) {
     cudaSetDevice(r->ctx->device);
     if (r->d_vals) cudaFreeAsync(r->d_vals, r->ctx->stream);
     if (r->d_coords) cudaFreeAsync(r->d_coords, r->ctx->stream);

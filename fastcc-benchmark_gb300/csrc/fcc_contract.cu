@@ -1156,7 +1156,7 @@ void build_side(const fcc_tensor *t, const int32_t *ctr, const int32_t *other_ma
   }
 }
 
-const int32_t *upload_coords(fcc_ctx *ctx, const fcc_tensor *t) {
+const int32_t *upload_coords(Runtime *ctx, const fcc_tensor *t) {
   if (t->nnz == 0 || t->order == 0 || t->location == FCC_DEVICE) return t->coords;
   const i64 extent = (t->nnz - 1) * t->stride_nnz + i64(t->order - 1) * t->stride_mode + 1;
   int32_t *d = ctx->arena.get_n<int32_t>(size_t(extent));
@@ -1165,7 +1165,7 @@ const int32_t *upload_coords(fcc_ctx *ctx, const fcc_tensor *t) {
   return d;
 }
 
-const double *upload_values(fcc_ctx *ctx, const fcc_tensor *t) {
+const double *upload_values(Runtime *ctx, const fcc_tensor *t) {
   if (t->nnz == 0 || t->location == FCC_DEVICE) return t->values;
   double *d = ctx->arena.get_n<double>(size_t(t->nnz));
   FCC_CUDA(cudaMemcpyAsync(d, t->values, sizeof(double) * size_t(t->nnz), cudaMemcpyHostToDevice,
@@ -1179,7 +1179,7 @@ enum Scalar { S_NSEG = 0, S_NA2, S_NTILES, S_NITEMS, S_NSPLIT, S_CAP, S_HASH, S_
 
 // Copies the scalar block and the error word to pinned host memory, waits,
 // and raises the error bits that are not recoverable.
-void read_scalars(fcc_ctx *ctx, u64 *d_sc) {
+void read_scalars(Runtime *ctx, u64 *d_sc) {
   FCC_CUDA(cudaMemcpyAsync(d_sc + S_ERR, ctx->d_err, sizeof(u32), cudaMemcpyDeviceToDevice, ctx->stream));
   FCC_CUDA(cudaMemcpyAsync(ctx->h_scalars, d_sc, sizeof(u64) * S_COUNT, cudaMemcpyDeviceToHost, ctx->stream));
   FCC_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1189,9 +1189,9 @@ void read_scalars(fcc_ctx *ctx, u64 *d_sc) {
   if (err & ERRB_INTERNAL) throw Error{FCC_ERR_CUDA, "internal plan invariant violated"};
 }
 
-u32 scalar32(fcc_ctx *ctx, int s) { return u32(ctx->h_scalars[s] & 0xFFFFFFFFu); }
+u32 scalar32(Runtime *ctx, int s) { return u32(ctx->h_scalars[s] & 0xFFFFFFFFu); }
 
-int grid_tiles(fcc_ctx *ctx, const void *kernel, int threads, size_t smem, u32 nitems) {
+int grid_tiles(Runtime *ctx, const void *kernel, int threads, size_t smem, u32 nitems) {
   int per_sm = 0;
   FCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
   if (per_sm < 1) throw Error{FCC_ERR_CUDA, "tile kernel does not fit on an SM"};
@@ -1201,14 +1201,16 @@ int grid_tiles(fcc_ctx *ctx, const void *kernel, int threads, size_t smem, u32 n
 }
 
 void free_result_buffers(fcc_result *r, cudaStream_t s) {
-  if (r->d_vals) cudaFreeAsync(r->d_vals, s);
-  if (r->d_coords) cudaFreeAsync(r->d_coords, s);
+  if (r->owned) {
+    if (r->d_vals) cudaFreeAsync(r->d_vals, s);
+    if (r->d_coords) cudaFreeAsync(r->d_coords, s);
+  }
   r->d_vals = nullptr;
   r->d_coords = nullptr;
 }
 
 struct Timing {
-  fcc_ctx *ctx;
+  Runtime *ctx;
   bool on;
   int next = 0;
   void mark(int slot) {  // records every slot up to `slot`
@@ -1231,9 +1233,11 @@ struct Timing {
 }  // namespace
 
 // The whole contraction. count_only stops after the segment lookup and
-// returns the multiply-add count in *products.
-void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
-              const int32_t *ctrB, int k, const fcc_options &opt, fcc_result **out, i64 *products,
+// returns the multiply-add count in *products. res (NULL when count_only)
+// receives the output; its buffers come from ctx->pool, or are the caller's
+// buffers of ctx when ctx->pool is NULL.
+void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+              const int32_t *ctrB, int k, const fcc_options &opt, fcc_result *res, i64 *products,
               bool count_only) {
   check_tensor(A, "A");
   check_tensor(B, "B");
@@ -1252,27 +1256,27 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   build_side(B, ctrB, A->max_index, ctrA, k, opt.radix_mode, sb);
   const int out_order = sa.lin.n_ext + sb.lin.n_ext;
   cudaStream_t st = ctx->stream;
-  Timing tm{ctx, opt.timing != 0};
-  for (int i = 0; i < FCC_NUM_PHASES; i++) ctx->phase_ms[i] = 0;
+  Timing tm{ctx, opt.timing != 0 && ctx->ev != nullptr};
+  if (ctx->phase_ms)
+    for (int i = 0; i < FCC_NUM_PHASES; i++) ctx->phase_ms[i] = 0;
 
-  std::unique_ptr<fcc_result> res;
   if (!count_only) {
-    res.reset(new fcc_result());
     res->order = out_order;
-    res->ctx = ctx;
+    res->owned = ctx->pool != nullptr;
   }
   struct Cleanup {
-    std::unique_ptr<fcc_result> &r;
+    fcc_result *r;
     cudaStream_t s;
-    ~Cleanup() { if (r) free_result_buffers(r.get(), s); }
-  } cleanup{res, st};
+    bool done = false;
+    ~Cleanup() { if (r && !done) free_result_buffers(r, s); }
+  } cleanup{count_only ? nullptr : res, st};
 
   ctx->arena.begin(st);
   tm.mark(0);
   if (A->nnz == 0 || B->nnz == 0) {
     if (products) *products = 0;
     tm.finish();
-    if (out) *out = res.release();
+    cleanup.done = true;
     return;
   }
 
@@ -1353,7 +1357,7 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   res->products = i64(ptotal);
   if (nA2 == 0 || ptotal == 0) {
     tm.finish();
-    *out = res.release();
+    cleanup.done = true;
     return;
   }
 
@@ -1504,13 +1508,21 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   u64 cap = std::max<u64>(std::min(cap_total, budget), 1);
   if (opt.capacity_hint > 0) cap = std::min<u64>(cap, u64(opt.capacity_hint));
 
+  if (!ctx->pool) cap = ctx->out_cap;  // caller buffers: their capacity, no retry
   for (int attempt = 0;; attempt++) {
-    FCC_CUDA(cudaMallocFromPoolAsync(reinterpret_cast<void **>(&res->d_vals), sizeof(double) * cap, ctx->pool, st));
-    if (out_order > 0)
-      FCC_CUDA(cudaMallocFromPoolAsync(reinterpret_cast<void **>(&res->d_coords), sizeof(u32) * cap * out_order,
-                                       ctx->pool, st));
-    res->cap = i64(cap);
-    Out o{res->d_coords, i64(cap), res->d_vals, cap, d_sc + S_CURSOR};
+    i64 stride = i64(cap);
+    if (ctx->pool) {
+      FCC_CUDA(cudaMallocFromPoolAsync(reinterpret_cast<void **>(&res->d_vals), sizeof(double) * cap, ctx->pool, st));
+      if (out_order > 0)
+        FCC_CUDA(cudaMallocFromPoolAsync(reinterpret_cast<void **>(&res->d_coords),
+                                         sizeof(u32) * cap * out_order, ctx->pool, st));
+    } else {
+      res->d_vals = ctx->out_vals;
+      res->d_coords = ctx->out_coords;
+      stride = ctx->out_stride;
+    }
+    res->cap = stride;
+    Out o{res->d_coords, stride, res->d_vals, cap, d_sc + S_CURSOR};
     FCC_CUDA(cudaMemsetAsync(d_sc + S_CURSOR, 0, sizeof(u64) * 2, st));  // cursor + item counter
     FCC_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(u32), st));
     u32 *counter = sc32(S_COUNTER);
@@ -1578,13 +1590,18 @@ void contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       res->nnz = i64(produced);
       break;
     }
+    if (!ctx->pool) {
+      res->nnz = i64(produced);  // tells the caller the capacity it needs
+      throw Error{FCC_ERR_CAPACITY, "the output needs " + std::to_string(produced) + " entries, the buffers hold " +
+                                        std::to_string(cap)};
+    }
     if (attempt >= 1) throw Error{FCC_ERR_CUDA, "output count changed between attempts"};
-    free_result_buffers(res.get(), st);
+    free_result_buffers(res, st);
     cap = produced;
     tm.next = 4;  // re-time the contraction
   }
   tm.finish();
-  *out = res.release();
+  cleanup.done = true;
 }
 
 }  // namespace fcc

@@ -55,9 +55,17 @@ extern std::atomic<long long> g_launches;
 // taken from the context's stream-ordered memory pool; a call that outgrows it
 // takes extra chunks, and the next call replaces them by one chunk of the
 // high-water size, so steady-state calls allocate nothing.
+//
+// A fixed arena (init_fixed) instead bump-allocates from a caller-given
+// buffer, never allocates, and reports FCC_ERR_CAPACITY when it runs out.
 class Arena {
  public:
   void init(cudaMemPool_t pool) { pool_ = pool; }
+  void init_fixed(void *base, size_t size) {
+    fixed_ = true;
+    fbase_ = static_cast<char *>(base);
+    fsize_ = size;
+  }
   void begin(cudaStream_t s);  // start of a call: consolidate to high-water size
   void *get(size_t bytes);     // 256-byte aligned, valid until the next begin()
   template <class T> T *get_n(size_t n) { return static_cast<T *>(get(sizeof(T) * (n ? n : 1))); }
@@ -70,7 +78,31 @@ class Arena {
   cudaStream_t stream_ = nullptr;
   std::vector<Chunk> chunks_;
   size_t used_ = 0, total_used_ = 0, high_ = 0;
+  bool fixed_ = false;
+  char *fbase_ = nullptr;  // fixed mode: the caller's buffer
+  size_t fsize_ = 0;
 };
+
+// What one contraction runs against: a context's stream, workspace and
+// scratch words, or the fixed scratch of an allocation-free call.
+struct Runtime {
+  explicit Runtime(Arena &a) : arena(a) {}
+  Arena &arena;
+  cudaStream_t stream = nullptr;
+  u32 *d_err = nullptr;            // device error word
+  u64 *h_scalars = nullptr;        // host buffer of >= 32 entries
+  int num_sms = 0;
+  size_t smem_optin = 0;
+  cudaEvent_t *ev = nullptr;       // FCC_NUM_PHASES + 1 events; NULL: no timing
+  double *phase_ms = nullptr;      // FCC_NUM_PHASES entries or NULL
+  cudaMemPool_t pool = nullptr;    // result buffers; NULL: the caller's buffers below
+  u32 *out_coords = nullptr;       // caller output: coords SoA with out_stride between modes
+  i64 out_stride = 0;
+  double *out_vals = nullptr;
+  u64 out_cap = 0;
+};
+
+void set_thread_error(const std::string &msg);
 
 }  // namespace fcc
 
@@ -97,6 +129,7 @@ struct fcc_result {
   fcc::u32 *d_coords = nullptr;
   double *d_vals = nullptr;
   fcc_ctx *ctx = nullptr;
+  bool owned = true;     // false: the buffers belong to the caller
 };
 
 namespace fcc {

@@ -14,6 +14,10 @@ std::atomic<long long> g_launches{0};
 
 void Arena::begin(cudaStream_t s) {
   stream_ = s;
+  if (fixed_) {
+    used_ = total_used_ = 0;
+    return;
+  }
   bool consolidate = chunks_.size() > 1 || (chunks_.size() == 1 && chunks_[0].size < high_);
   if (consolidate) {
     for (auto &c : chunks_) FCC_CUDA(cudaFreeAsync(c.p, s));
@@ -31,6 +35,16 @@ void Arena::begin(cudaStream_t s) {
 
 void *Arena::get(size_t bytes) {
   bytes = (bytes + 255) & ~size_t(255);
+  if (fixed_) {
+    if (used_ + bytes > fsize_)
+      throw Error{FCC_ERR_CAPACITY, "the fixed scratch (" + std::to_string(fsize_) +
+                                        " bytes) is too small for this contraction"};
+    char *p = fbase_ + used_;
+    used_ += bytes;
+    total_used_ = used_;
+    if (used_ > high_) high_ = used_;
+    return p;
+  }
   if (chunks_.empty() || used_ + bytes > chunks_.back().size) {
     size_t sz = size_t(64) << 20;
     if (!chunks_.empty() && chunks_.back().size > sz) sz = chunks_.back().size;
@@ -48,6 +62,7 @@ void *Arena::get(size_t bytes) {
 }
 
 void Arena::release_all(cudaStream_t s) {
+  if (fixed_) return;
   for (auto &c : chunks_) cudaFreeAsync(c.p, s);
   chunks_.clear();
   used_ = total_used_ = 0;

@@ -167,6 +167,44 @@ int fcc_count_products(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B,
 
 int fcc_abi_version(void);
 
+/*
+ * fcc_contract_noalloc - the contraction for callers that cannot allocate
+ * device memory. It has no counterpart in the reference (whose CPU code
+ * allocates freely).
+ *
+ * Some hosts forbid device allocation after start-up: services that reserve
+ * all device memory for their own pool, real-time loops where cudaMalloc's
+ * device-wide synchronisation and unbounded latency are not acceptable, or
+ * plugins that must leave their host process's device heap alone. They cannot
+ * create an fcc_ctx (which allocates a workspace, events and result buffers).
+ * This entry point takes the inputs and the OUTPUT buffers from the caller
+ * and runs the same kernels, with every temporary taken from one static
+ * device array of FCC_NOALLOC_SCRATCH_BYTES (32 MiB) defined in the library.
+ * Every GPU that loads the library holds that array until the process exits.
+ * It calls no cudaMalloc, cudaFree or other allocating routine.
+ *
+ * Limits: nnz(A) + nnz(B) <= FCC_NOALLOC_MAX_NNZ, and the contraction's
+ * temporaries must fit the array; otherwise FCC_ERR_CAPACITY with a message
+ * (fcc_last_error(NULL)). Outputs go to out_coords (mode m at
+ * out_coords[m * out_mode_stride + i], uint32) and out_values, device
+ * buffers of out_capacity entries; when the output is larger, the call
+ * returns FCC_ERR_CAPACITY and *out_nnz holds the count needed.
+ *
+ * Set-up: the first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture. Work runs on cuda_stream (a cudaStream_t, NULL
+ * for the default stream) and the call returns when the result is ready.
+ * All calls share the one array and it keeps the last call's contents: calls
+ * that overlap on the GPU (other host threads, other streams) race with each
+ * other and must be serialised by the caller. opts->timing is ignored.
+ */
+#define FCC_NOALLOC_SCRATCH_BYTES (32u << 20)
+#define FCC_NOALLOC_MAX_NNZ 131072
+int fcc_contract_noalloc(const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                         const int32_t *ctrB, int32_t k, const fcc_options *opts, void *cuda_stream,
+                         uint32_t *out_coords, int64_t out_mode_stride, double *out_values,
+                         int64_t out_capacity, int64_t *out_nnz, int64_t *out_products);
+
 /* Diagnostics: kernels this process has launched through the library so far. */
 int64_t fcc_launch_count(void);
 

@@ -1,0 +1,98 @@
+"""fcc_contract_noalloc against fcc_contract, through the C ABI.
+
+fcc_contract_noalloc serves callers that cannot allocate device memory: hosts
+that reserve the whole device heap for their own pool, real-time loops that
+must not stall on cudaMalloc's device-wide synchronisation, plugins that must
+leave their host's device heap alone. It takes the caller's input and output
+buffers and keeps every temporary in one static device array inside the
+library. Here it runs twice in a row on the same inputs; each result must
+match fcc_contract's on the same inputs: the same output coordinate set and
+values within 1e-12 * S (S = the oracle's sum of |a*b| per output), the
+tolerance of the other parity tests. The capacity errors are checked too.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import fastcc_gpu as F
+import oracle
+import workloads
+from helpers import check_parity, sort_rows
+
+pytestmark = pytest.mark.gpu
+
+MAX_NNZ = 131072
+
+
+def _entry():
+    fn = F.lib().fcc_contract_noalloc
+    vp, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+    fn.argtypes = [ctypes.POINTER(F._CTensor), ctypes.POINTER(F._CTensor), vp, vp, i32,
+                   ctypes.POINTER(F.Options), vp, vp, i64, vp, i64, ctypes.POINTER(i64),
+                   ctypes.POINTER(i64)]
+    fn.restype = ctypes.c_int
+    return fn
+
+
+def _call(ta, tb, ca, cb, out_c, out_v, cap):
+    n, p = ctypes.c_int64(), ctypes.c_int64()
+    sa, sb = ta._struct(), tb._struct()
+    rc = _entry()(ctypes.byref(sa), ctypes.byref(sb), ca.ctypes.data, cb.ctypes.data, len(ca), None,
+                  None, out_c.data_ptr(), out_c.stride(0), out_v.data_ptr(), cap, ctypes.byref(n),
+                  ctypes.byref(p))
+    return rc, n.value, p.value
+
+
+def test_noalloc_matches_fcc_contract_twice():
+    import torch
+    w = workloads.readme(seed=21, scale=0.4)
+    a, b = w["a"], w["b"]
+    assert a.nnz + b.nnz <= MAX_NNZ
+    ca = np.asarray(w["ctr_a"], np.int32)
+    cb = np.asarray(w["ctr_b"], np.int32)
+    # the existing entry point (host operands) and the oracle's |a*b| sums
+    with F.Context(0) as ctx:
+        r = ctx.contract(a, b, ca, cb)
+        ref_c, ref_v = r.to_numpy()
+        order, n_ref, prod_ref = r.order, r.nnz, r.products
+        r.free()
+    o = oracle.fastcc_multiply(a.coords, a.values, a.max_index, b.coords, b.values, b.max_index,
+                               ca, cb, want_abs=True)
+    check_parity(ref_c, ref_v, o["coords"], o["values"], o["abs_sum"])
+    ref_c, ref_v = sort_rows(ref_c, ref_v)
+    oc, oabs = sort_rows(o["coords"], o["abs_sum"])
+    assert np.array_equal(ref_c, oc)
+
+    # device operands and caller-owned output buffers
+    ta = F.Tensor(torch.from_numpy(a.coords).cuda(), torch.from_numpy(a.values).cuda(), a.max_index)
+    tb = F.Tensor(torch.from_numpy(b.coords).cuda(), torch.from_numpy(b.values).cuda(), b.max_index)
+    cap = n_ref + 1000
+    out_c = torch.empty((order, cap), dtype=torch.int32, device="cuda")
+    out_v = torch.empty(cap, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    for call in range(2):
+        out_v.fill_(float("nan"))
+        out_c.fill_(-1)
+        torch.cuda.synchronize()
+        rc, n, p = _call(ta, tb, ca, cb, out_c, out_v, cap)
+        assert rc == 0, (call, rc, F.lib().fcc_last_error(None))
+        assert n == n_ref and p == prod_ref
+        got_c = out_c[:, :n].t().cpu().numpy()
+        got_v = out_v[:n].cpu().numpy()
+        check_parity(got_c, got_v, ref_c, ref_v, oabs)
+
+
+def test_noalloc_reports_capacity():
+    import torch
+    w = workloads.readme(seed=22, scale=0.1)
+    a, b = w["a"], w["b"]
+    ca = np.asarray(w["ctr_a"], np.int32)
+    cb = np.asarray(w["ctr_b"], np.int32)
+    out_c = torch.empty((3, 16), dtype=torch.int32, device="cuda")
+    out_v = torch.empty(16, dtype=torch.float64, device="cuda")
+    rc, n, _ = _call(a, b, ca, cb, out_c, out_v, 16)
+    assert rc == 8 and n > 16  # FCC_ERR_CAPACITY, with the count needed
+    big = workloads.readme(seed=23, scale=0.7)  # 210,000 nonzeros in all
+    rc, _, _ = _call(big["a"], big["b"], ca, cb, out_c, out_v, 16)
+    assert rc == 8
