@@ -1,0 +1,266 @@
+// contract.hpp - header-only drop-in for the reference's contract.hpp
+// (jianjianh1/fastcc-benchmark) whose one contraction,
+//   a.fastcc_multiply<TileAccumulator<double>, double>(b, {1, 3}, {1, 2})
+// (contract.hpp:824-912, README.md:9-13), runs on a GB300 through the C ABI
+// of libfastcc_gpu.so (include/fastcc_gpu.h).
+//
+// Kept from the reference: the names Tensor<DT>, NNZ<DT>, CoOrdinate,
+// ListTensor<DT>, TileAccumulator<DT>, TileAccumulatorMap<DT>; the
+// fastcc_multiply signature and its template arguments; the caller's duty to
+// run _infer_dimensionality() / _infer_shape() first (benchmark.cpp:47-48);
+// ListTensor::compute_nnz_count() and run_through_nnz().
+// Different: ListTensor owns its entries and exposes them (size, coords,
+// value); output coordinates are decoded correctly; errors throw fcc::Error.
+// Compute is FP64 whatever DT and RES are (values are converted).
+#ifndef FASTCC_GB300_CONTRACT_HPP
+#define FASTCC_GB300_CONTRACT_HPP
+
+#include <cstdint>
+#include <initializer_list>
+#include <memory>
+#include <mutex>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "fastcc_gpu.h"
+
+namespace fcc {
+
+// A failed call: status is an fcc_status (include/fastcc_gpu.h).
+class Error : public std::runtime_error {
+ public:
+  Error(int status, const std::string &msg) : std::runtime_error(msg), status(status) {}
+  int status;
+};
+
+// One context per process (device 0 unless fcc::set_device is called
+// before the first contraction), created on first use.
+inline std::mutex &context_mutex() {
+  static std::mutex m;
+  return m;
+}
+inline int &default_device() {
+  static int d = 0;
+  return d;
+}
+inline void set_device(int device) { default_device() = device; }
+inline fcc_ctx *default_context() {
+  struct Holder {
+    fcc_ctx *ctx = nullptr;
+    ~Holder() {
+      if (ctx) fcc_ctx_destroy(ctx);
+    }
+  };
+  static Holder h;
+  if (!h.ctx) {
+    int st = fcc_ctx_create(default_device(), &h.ctx);
+    if (st != FCC_OK) throw Error(st, std::string("fcc_ctx_create: ") + fcc_last_error(nullptr));
+  }
+  return h.ctx;
+}
+
+}  // namespace fcc
+
+// Policy tags: the reference's accumulators (index_tensors.hpp:843-883,
+// 994-1065) select the GPU planner's choice; results are identical.
+template <class DT> class TileAccumulator {};
+template <class DT> class TileAccumulatorMap {};
+
+// A coordinate: indices plus the per-mode max index ("shape") the
+// linearisers use (coordinate.hpp:502-782).
+class CoOrdinate {
+  std::vector<int> coords_;
+  std::vector<int> max_indices_;
+
+ public:
+  using iterator = std::vector<int>::iterator;
+  using const_iterator = std::vector<int>::const_iterator;
+  CoOrdinate() = default;
+  CoOrdinate(int dimensionality, int *coords) : coords_(coords, coords + dimensionality) {}
+  CoOrdinate(std::vector<int> const &data, std::vector<int> shape = std::vector<int>())
+      : coords_(data), max_indices_(std::move(shape)) {}
+  CoOrdinate(std::initializer_list<int> l) : coords_(l) {}
+  iterator begin() { return coords_.begin(); }
+  iterator end() { return coords_.end(); }
+  const_iterator begin() const { return coords_.begin(); }
+  const_iterator end() const { return coords_.end(); }
+  int get_index(int dim) const { return coords_[dim]; }
+  int get_dimensionality() const { return int(coords_.size()); }
+  void set_shape(std::vector<int> shape) { max_indices_ = std::move(shape); }
+  const std::vector<int> &get_shape() const { return max_indices_; }
+  bool operator==(const CoOrdinate &o) const { return coords_ == o.coords_; }
+  std::string to_string() const {
+    std::string s;
+    for (int c : coords_) s += std::to_string(c) + " ";
+    return s;
+  }
+};
+
+template <class DT> class NNZ {
+  DT data_;
+  CoOrdinate coords_;
+
+ public:
+  NNZ(DT data, CoOrdinate coords) : data_(data), coords_(std::move(coords)) {}
+  NNZ(DT data, int dimensionality, int *coords) : data_(data), coords_(dimensionality, coords) {}
+  // A random nonzero inside `shape` (index_tensors.hpp:168-183).
+  NNZ(int dimensionality, int *shape) {
+    std::random_device rd;
+    std::mt19937 gen(rd());
+    std::uniform_real_distribution<> u(0, 1);
+    std::vector<int> c;
+    for (int i = 0; i < dimensionality; i++) c.push_back(std::uniform_int_distribution<>(0, shape[i])(gen));
+    data_ = DT(u(gen));
+    coords_ = CoOrdinate(c);
+  }
+  DT get_data() const { return data_; }
+  CoOrdinate &get_coords() { return coords_; }
+  const CoOrdinate &get_coords() const { return coords_; }
+  int get_index(int dim) const { return coords_.get_index(dim); }
+};
+
+// The contraction result: entries in SoA-free form, coordinates row-major
+// (nnz x dimensionality int32) and values. Order is unspecified, as the
+// reference's per-thread list concatenation leaves it (contract.hpp:906-909).
+template <class DT> class ListTensor {
+  std::vector<int32_t> coords_;
+  std::vector<DT> values_;
+  int dimensionality_ = 0;
+
+ public:
+  ListTensor(int dimensionality = 0, int /*thread_id*/ = 0) : dimensionality_(dimensionality) {}
+  int compute_nnz_count() const { return int(values_.size()); }
+  int run_through_nnz() const { return int(values_.size()); }
+  int get_dimensionality() const { return dimensionality_; }
+  size_t size() const { return values_.size(); }
+  const int32_t *coords(size_t i) const { return coords_.data() + i * size_t(dimensionality_); }
+  DT value(size_t i) const { return values_[i]; }
+  const std::vector<int32_t> &coord_data() const { return coords_; }
+  const std::vector<DT> &values() const { return values_; }
+  void push_nnz(DT data, const int32_t *coords) {
+    coords_.insert(coords_.end(), coords, coords + dimensionality_);
+    values_.push_back(data);
+  }
+  // Appends other's entries (the reference's version loses entries after an
+  // empty list, index_tensors.hpp:115-125).
+  void concatenate(ListTensor &other) {
+    coords_.insert(coords_.end(), other.coords_.begin(), other.coords_.end());
+    values_.insert(values_.end(), other.values_.begin(), other.values_.end());
+  }
+  // Fills from a device result (used by Tensor::fastcc_multiply).
+  void take(fcc_result *r) {
+    int32_t order = 0;
+    int64_t n = 0;
+    fcc_result_info(r, &order, &n, nullptr);
+    dimensionality_ = order;
+    coords_.assign(size_t(n) * size_t(order), 0);
+    std::vector<double> v(static_cast<size_t>(n));
+    int st = fcc_result_copy_to_host(r, order ? coords_.data() : nullptr, order, 1, v.data());
+    if (st != FCC_OK) throw fcc::Error(st, "fcc_result_copy_to_host failed");
+    values_.assign(v.begin(), v.end());
+  }
+};
+
+template <class DT> class Tensor {
+  std::vector<NNZ<DT>> nonzeros;
+  std::vector<int> shape_store;
+  int *shape = nullptr;
+  int dimensionality = 42;
+
+ public:
+  using iterator = typename std::vector<NNZ<DT>>::iterator;
+  iterator begin() { return nonzeros.begin(); }
+  iterator end() { return nonzeros.end(); }
+  Tensor(std::string fname, bool has_header);  // read.hpp
+  Tensor(int size = 0) { nonzeros.reserve(size_t(size)); }
+  // `size` random nonzeros inside `shape` (contract.hpp:58-65).
+  Tensor(int size, int dims, int *shape_) : dimensionality(dims) {
+    shape_store.assign(shape_, shape_ + dims);
+    shape = shape_store.data();
+    nonzeros.reserve(size_t(size));
+    for (int i = 0; i < size; i++) nonzeros.emplace_back(dims, shape);
+  }
+  std::vector<NNZ<DT>> &get_nonzeros() { return nonzeros; }
+  int get_size() const { return int(nonzeros.size()); }
+  void delete_old_values() { nonzeros.clear(); }
+  void write(std::string fname);  // read.hpp
+  void _infer_dimensionality() {
+    if (!nonzeros.empty()) dimensionality = nonzeros[0].get_coords().get_dimensionality();
+  }
+  int get_dimensionality() {
+    if (dimensionality == 42) _infer_dimensionality();
+    return dimensionality;
+  }
+  // Per-mode max index, also set on every coordinate (contract.hpp:124-144).
+  void _infer_shape() {
+    if (nonzeros.empty()) return;
+    shape_store.assign(size_t(dimensionality), 0);
+    for (auto &z : nonzeros)
+      for (int i = 0; i < dimensionality; i++)
+        if (z.get_coords().get_index(i) > shape_store[i]) shape_store[i] = z.get_coords().get_index(i);
+    shape = shape_store.data();
+    for (auto &z : nonzeros) z.get_coords().set_shape(shape_store);
+  }
+  int *get_shape_ref() {
+    if (dimensionality == 42) {
+      _infer_dimensionality();
+      _infer_shape();
+    }
+    return shape;
+  }
+
+  // The reference's call (contract.hpp:824-827). AccType selects nothing on
+  // the GPU (both accumulators give the same result); tile_size is accepted
+  // for signature compatibility.
+  template <class AccType, class RES, class RIGHT>
+  ListTensor<RES> fastcc_multiply(Tensor<RIGHT> &other, CoOrdinate left_contr, CoOrdinate right_contr,
+                                  int tile_size = 100) {
+    static_assert(std::is_floating_point<RES>::value, "RES must be float or double");
+    if (left_contr.get_dimensionality() != right_contr.get_dimensionality())
+      throw fcc::Error(FCC_ERR_ARG, "contracted mode lists differ in length");
+    std::vector<int32_t> ca(left_contr.begin(), left_contr.end()), cb(right_contr.begin(), right_contr.end());
+    auto pack = [](auto &t, std::vector<int32_t> &coords, std::vector<double> &vals, std::vector<int32_t> &mx) {
+      const int d = t.get_dimensionality();
+      int *sh = t.get_shape_ref();
+      mx.assign(size_t(d), 0);
+      if (sh)
+        for (int m = 0; m < d; m++) mx[m] = sh[m];
+      auto &nz = t.get_nonzeros();
+      coords.resize(nz.size() * size_t(d));
+      vals.resize(nz.size());
+      for (size_t i = 0; i < nz.size(); i++) {
+        for (int m = 0; m < d; m++) coords[i * size_t(d) + m] = nz[i].get_coords().get_index(m);
+        vals[i] = double(nz[i].get_data());
+      }
+      return d;
+    };
+    std::vector<int32_t> cA, cB, mA, mB;
+    std::vector<double> vA, vB;
+    const int dA = pack(*this, cA, vA, mA);
+    const int dB = pack(other, cB, vB, mB);
+    fcc_tensor A{dA, int64_t(vA.size()), mA.data(), cA.data(), dA, 1, vA.data(), FCC_HOST};
+    fcc_tensor B{dB, int64_t(vB.size()), mB.data(), cB.data(), dB, 1, vB.data(), FCC_HOST};
+    fcc_options o;
+    fcc_options_default(&o);
+    o.tile_size = tile_size;
+    std::lock_guard<std::mutex> lock(fcc::context_mutex());
+    fcc_ctx *ctx = fcc::default_context();
+    fcc_result *r = nullptr;
+    int st = fcc_contract(ctx, &A, &B, ca.data(), cb.data(), int32_t(ca.size()), &o, &r);
+    if (st != FCC_OK) throw fcc::Error(st, std::string("fcc_contract: ") + fcc_last_error(ctx));
+    ListTensor<RES> out(dA + dB - 2 * int(ca.size()));
+    try {
+      out.take(r);
+    } catch (...) {
+      fcc_result_free(r);
+      throw;
+    }
+    fcc_result_free(r);
+    return out;
+  }
+};
+
+#endif
