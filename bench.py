@@ -341,6 +341,7 @@ def main():
     alg_bytes = 2 * nnz * (4 * 3 + 8) + out_nnz * (4 * out_order + 8)
     kms = statistics.mean(contract_ms)
     achieved = alg_bytes / (kms / 1000.0) / 1e9
+    fma_peak = F.fp64_fma_rate(local)  # measured now, on this GPU
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -351,7 +352,10 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": MEASURED_TRAFFIC,
                      "kernel": "k_contract_dense", "kernel_ms": kms, "algorithmic_bytes": alg_bytes,
-                     "peak_kind": peak_kind},
+                     "peak_kind": peak_kind,
+                     "fp64": {"achieved": products / (kms / 1000.0), "peak": fma_peak, "unit": "FMA/s",
+                              "frac": products / (kms / 1000.0) / fma_peak,
+                              "note": "every multiply-add is one FP64 FMA; peak measured by fcc_diag_fp64_fma_rate"}},
         "e2e": {"value": products * ws / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "gpu_launches": launches,

@@ -265,6 +265,15 @@ def launch_count():
     return int(lib().fcc_launch_count())
 
 
+def fp64_fma_rate(device=0):
+    """Measured FP64 FMA instructions per second of the device."""
+    r = ctypes.c_double()
+    rc = lib().fcc_diag_fp64_fma_rate(ctypes.c_int32(device), ctypes.byref(r))
+    if rc != 0:
+        raise FccError(rc, "fcc_diag_fp64_fma_rate failed")
+    return r.value
+
+
 # ----------------------------------------------------------- generator ----
 
 def synth_coo(seed, extents, zipf_s=None, nnz=1000, lognormal=False):

@@ -208,6 +208,11 @@ int fcc_contract_noalloc(const fcc_tensor *A, const fcc_tensor *B, const int32_t
 /* Diagnostics: kernels this process has launched through the library so far. */
 int64_t fcc_launch_count(void);
 
+/* Diagnostics: measured FP64 FMA rate of a device (FMA instructions per
+ * second over all SMs), the compute roofline of the tile kernels, whose every
+ * multiply-add is one FP64 FMA. device < 0: the current device. */
+int fcc_diag_fp64_fma_rate(int32_t device, double *fma_per_second);
+
 #ifdef __cplusplus
 }
 #endif
