@@ -47,6 +47,9 @@ int main(int argc, char **argv) {
   } catch (const fcc::Error &e) {
     std::fprintf(stderr, "fcc error %d: %s\n", e.status, e.what());
     return 2;
+  } catch (const std::exception &e) {
+    std::fprintf(stderr, "error: %s\n", e.what());
+    return 4;
   }
   return 0;
 }

@@ -35,7 +35,7 @@ def _write_tns(path, coords, vals, dims):
     with open(path, "w") as f:
         f.write(" ".join(str(d) for d in dims) + "\n")  # header line (skipped: has_header)
         for c, v in zip(coords, vals):
-            f.write(" ".join(str(int(x)) for x in c) + f" {v!r}\n")
+            f.write(" ".join(str(int(x)) for x in c) + " " + repr(float(v)) + "\n")
 
 
 @pytest.mark.gpu
