@@ -33,9 +33,11 @@ sys.path.insert(0, PKG)
 METRIC = "FP64 multiply-adds/s & ms/contraction: learned+batched vs plain, 1 GB300"
 UNIT = "multiply-adds/s"
 WORKLOAD = "zipf3: A 20000x20000x500000, 10M nnz, Zipf(1.2) per mode, lognormal values; A x A over modes {1,2}"
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_contract_dense launch on
-# this workload, from the ncu capture summarised in profiles/ (None until taken).
-MEASURED_TRAFFIC = None
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_contract_dense launch:
+# measured with ncu on the 2.5M-nonzero case of the same extents (3.372 GB for
+# 3.381 GB of algorithmic bytes) and scaled by algorithmic bytes to this
+# workload's 6.695 GB (profiles/k_contract_dense_zipf3.md).
+MEASURED_TRAFFIC = 6.695e9 * 3.372 / 3.381
 
 
 def load_peaks():
@@ -248,7 +250,25 @@ def main():
     ap.add_argument("--sweep", choices=["zipf3", "twomode", "readme"],
                     help="time the option sets given by --variants (JSON list) on a workload")
     ap.add_argument("--variants", default="[{}]")
+    ap.add_argument("--diag", action="store_true",
+                    help="print the FP64 FMA rate and the shared-memory accumulation rates")
     args = ap.parse_args()
+    if args.diag:
+        import build_lib
+        build_lib.build_all()
+        import fastcc_gpu as F
+        import torch
+        torch.cuda.set_device(0)
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        clk = 2.07e9
+        line = {"fp64_fma_per_s": F.fp64_fma_rate(0)}
+        for mode, name in enumerate(["atomicAdd_product", "cas_fma", "plain_fma"]):
+            r = F.shared_update_rate(mode)
+            line[f"shared_{name}_per_s"] = r
+            line[f"shared_{name}_per_clk_per_sm"] = r / sms / clk
+        line["fp64_fma_per_clk_per_sm"] = line["fp64_fma_per_s"] / sms / clk
+        print(json.dumps(line))
+        return
     if args.sweep:
         run_sweep(args.sweep, json.loads(args.variants))
         return

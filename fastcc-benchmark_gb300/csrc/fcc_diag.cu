@@ -21,7 +21,89 @@ __global__ void __launch_bounds__(1024) k_fp64_fma(double *sink, int iters, doub
   if (s == 1.2345e300) sink[blockIdx.x] = s;  // keeps the loop alive, never true
 }
 
+// Shared-memory FP64 accumulation into a 20,000-double tile (one dense row of
+// the benchmark workload), lanes of a warp on distinct positions, four
+// updates per iteration. mode 0: built-in atomicAdd(double) of a product;
+// 1: compare-and-swap loop around one FMA (the tile kernels' phase 2);
+// 2: unsynchronised read-modify-write with FMA (the tile kernels' phase 1,
+// exact there because one A entry's positions are distinct).
+constexpr int kDiagArea = 20000;
+
+__device__ __forceinline__ unsigned diag_pos(unsigned it, unsigned warp, unsigned lane) {
+  const unsigned h = (it * 2654435761u) ^ (warp * 40503u);
+  return (h % kDiagArea + lane * 613u) % kDiagArea;  // 613 is prime to 20000: distinct per warp
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(1024, 1) k_shared_update(double *sink, int iters) {
+  extern __shared__ double acc[];
+  for (int i = threadIdx.x; i < kDiagArea; i += blockDim.x) acc[i] = 0.0;
+  __syncthreads();
+  const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const double v0 = 1e-3 * (lane + 1);
+  for (int it = 0; it < iters; it += 4) {
+    const double v = v0 * (1.0 + 1e-9 * it);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const unsigned p = diag_pos(it + q, warp, lane);
+      const double m = 1.0001 + q;
+      if (MODE == 0) {
+        atomicAdd(&acc[p], v * m);
+      } else if (MODE == 1) {
+        unsigned long long *a = reinterpret_cast<unsigned long long *>(&acc[p]);
+        unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(a), as;
+        do {
+          as = cur;
+          cur = atomicCAS(a, as, (unsigned long long)__double_as_longlong(fma(v, m, __longlong_as_double((long long)as))));
+        } while (cur != as);
+      } else {
+        acc[p] = fma(v, m, acc[p]);
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) sink[blockIdx.x] = acc[blockIdx.x % kDiagArea];
+}
+
 }  // namespace
+
+extern "C" int fcc_diag_shared_update_rate(int32_t mode, double *updates_per_second) {
+  if (!updates_per_second || mode < 0 || mode > 2) return FCC_ERR_ARG;
+  *updates_per_second = 0;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return FCC_ERR_CUDA;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return FCC_ERR_CUDA;
+  double *sink = nullptr;
+  if (cudaMalloc(&sink, sizeof(double) * sms) != cudaSuccess) return FCC_ERR_OOM;
+  const size_t smem = sizeof(double) * kDiagArea;
+  const void *kern = mode == 0 ? reinterpret_cast<const void *>(k_shared_update<0>)
+                   : mode == 1 ? reinterpret_cast<const void *>(k_shared_update<1>)
+                               : reinterpret_cast<const void *>(k_shared_update<2>);
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  auto launch = [&](int iters) {
+    if (mode == 0) k_shared_update<0><<<sms, 1024, smem>>>(sink, iters);
+    else if (mode == 1) k_shared_update<1><<<sms, 1024, smem>>>(sink, iters);
+    else k_shared_update<2><<<sms, 1024, smem>>>(sink, iters);
+  };
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int iters = 2048;
+  launch(64);
+  cudaEventRecord(e0);
+  launch(iters);
+  cudaEventRecord(e1);
+  cudaError_t err = cudaEventSynchronize(e1);
+  float ms = 0;
+  if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+  if (err == cudaSuccess) err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(sink);
+  if (err != cudaSuccess || ms <= 0) return FCC_ERR_CUDA;
+  *updates_per_second = double(sms) * 1024.0 * iters / (double(ms) * 1e-3);
+  return FCC_OK;
+}
 
 extern "C" int fcc_diag_fp64_fma_rate(int32_t device, double *fma_per_second) {
   if (!fma_per_second) return FCC_ERR_ARG;

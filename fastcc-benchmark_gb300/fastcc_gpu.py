@@ -265,6 +265,16 @@ def launch_count():
     return int(lib().fcc_launch_count())
 
 
+def shared_update_rate(mode):
+    """Measured FP64 shared-memory accumulation rate (updates per second);
+    mode 0 atomicAdd of a product, 1 compare-and-swap FMA, 2 plain FMA."""
+    r = ctypes.c_double()
+    rc = lib().fcc_diag_shared_update_rate(ctypes.c_int32(mode), ctypes.byref(r))
+    if rc != 0:
+        raise FccError(rc, "fcc_diag_shared_update_rate failed")
+    return r.value
+
+
 def fp64_fma_rate(device=0):
     """Measured FP64 FMA instructions per second of the device."""
     r = ctypes.c_double()

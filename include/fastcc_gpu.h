@@ -213,6 +213,12 @@ int64_t fcc_launch_count(void);
  * multiply-add is one FP64 FMA. device < 0: the current device. */
 int fcc_diag_fp64_fma_rate(int32_t device, double *fma_per_second);
 
+/* Diagnostics: FP64 accumulation rate into a 20,000-double shared-memory
+ * tile on the current device (updates per second over all SMs). mode 0: the
+ * built-in FP64 atomic add of a product; 1: a compare-and-swap loop around
+ * one FMA; 2: an unsynchronised read-modify-write FMA. */
+int fcc_diag_shared_update_rate(int32_t mode, double *updates_per_second);
+
 #ifdef __cplusplus
 }
 #endif
