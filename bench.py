@@ -207,6 +207,33 @@ def run_profile_case(name):
             r.free()
 
 
+def run_sweep_batched(variants, reps):
+    """The batched workload: each option set timed on one fcc_contract_batch
+    call (median of reps, per-phase times)."""
+    import torch
+
+    import fastcc_gpu as F
+    import workloads
+    inst = workloads.batched(seed=1, count=256)
+    cuda = lambda t: F.Tensor(torch.from_numpy(t.coords).cuda(), torch.from_numpy(t.values).cuda(), t.max_index)
+    As = [cuda(w["a"]) for w in inst]
+    Bs = [cuda(w["b"]) for w in inst]
+    torch.cuda.synchronize()
+    with F.Context(0) as ctx:
+        for v in variants:
+            opts = F.Options(timing=1, **v)
+            ph = []
+            for rep in range(reps + 1):
+                r, _ = ctx.contract_batch(As, Bs, [1, 3], [1, 2], opts)
+                n = r.nnz
+                r.free()
+                if rep:
+                    ph.append(ctx.timings())
+            med = {k: statistics.median(p[k] for p in ph) for k in ph[0]}
+            print(json.dumps({"workload": "batched", "options": v, "outputs": n,
+                              "phases_ms": {k: round(x, 3) for k, x in med.items()}}), flush=True)
+
+
 def run_sweep(name, variants, reps=3):
     """Times option sets on one workload (device-resident, median of reps),
     one JSON line per option set."""
@@ -216,6 +243,9 @@ def run_sweep(name, variants, reps=3):
     build_lib.build_all()
     import fastcc_gpu as F
     import workloads
+    if name == "batched":
+        run_sweep_batched(variants, reps)
+        return
     w = {"zipf3": workloads.zipf3, "twomode": workloads.twomode, "readme": workloads.readme}[name]()
     a, b = w["a"], w["b"]
     A = F.Tensor(torch.from_numpy(a.coords).cuda(), torch.from_numpy(a.values).cuda(), a.max_index)
@@ -237,6 +267,113 @@ def run_sweep(name, variants, reps=3):
                               "contract_ms": statistics.median(con)}), flush=True)
 
 
+def run_batched(steps, warmup, stream, local):
+    """The batched workload: 256 contractions of the readme pattern with
+    uneven sizes. Times, per step, 256 sequential plain contractions and one
+    batched call (fcc_contract_batch) on device-resident operands, and the
+    same pair end to end (pinned host operands in, every output copied back).
+    Returns the JSON sub-object."""
+    import numpy as np
+    import torch
+
+    import fastcc_gpu as F
+    import workloads
+    inst = workloads.batched(seed=1, count=256)
+    dev = [(F.Tensor(torch.from_numpy(w["a"].coords).cuda(), torch.from_numpy(w["a"].values).cuda(),
+                     w["a"].max_index),
+            F.Tensor(torch.from_numpy(w["b"].coords).cuda(), torch.from_numpy(w["b"].values).cuda(),
+                     w["b"].max_index)) for w in inst]
+    As, Bs = [d[0] for d in dev], [d[1] for d in dev]
+    ctr_a, ctr_b = inst[0]["ctr_a"], inst[0]["ctr_b"]
+    torch.cuda.synchronize()
+    ctx = F.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+
+    def plain():
+        n = p = 0
+        for a, b in dev:
+            r = ctx.contract(a, b, ctr_a, ctr_b)
+            n += r.nnz
+            p += r.products
+            r.free()
+        return n, p
+
+    def batched():
+        r, counts = ctx.contract_batch(As, Bs, ctr_a, ctr_b)
+        n, p = r.nnz, r.products
+        r.free()
+        return n, p
+
+    def timed(fn, steps=steps):
+        for _ in range(warmup):
+            out = fn()
+        torch.cuda.synchronize()
+        l0 = F.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps, out, (F.launch_count() - l0) // steps
+
+    ms_plain, (n_plain, prods), l_plain = timed(plain)
+    ms_batch, (n_batch, prods_b), l_batch = timed(batched)
+    assert n_plain == n_batch and prods == prods_b, "batched and plain results differ in size"
+
+    # end to end: pinned host operands, outputs copied to pinned host buffers
+    host = []
+    for w in inst:
+        pa = (torch.from_numpy(w["a"].coords).pin_memory(), torch.from_numpy(w["a"].values).pin_memory())
+        pb = (torch.from_numpy(w["b"].coords).pin_memory(), torch.from_numpy(w["b"].values).pin_memory())
+        host.append((F.Tensor(pa[0].numpy(), pa[1].numpy(), w["a"].max_index),
+                     F.Tensor(pb[0].numpy(), pb[1].numpy(), w["b"].max_index), pa, pb))
+    HA, HB = [h[0] for h in host], [h[1] for h in host]
+    order = 4  # the instance, then i, j, k
+    out_c = torch.empty((order, n_batch), dtype=torch.int32).pin_memory()
+    out_v = torch.empty(n_batch, dtype=torch.float64).pin_memory()
+    oc, ov = out_c.numpy(), out_v.numpy()
+
+    def plain_e2e():
+        off = 0
+        for a, b, _, _ in host:
+            r = ctx.contract(a, b, ctr_a, ctr_b)
+            r.to_numpy_soa(oc[1:, off:], ov[off:])
+            off += r.nnz
+            r.free()
+        return off, 0
+
+    def batched_e2e():
+        r, counts = ctx.contract_batch(HA, HB, ctr_a, ctr_b)
+        r.to_numpy_soa(oc, ov)
+        n = r.nnz
+        r.free()
+        return n, 0
+
+    e2e_steps = max(1, min(steps, 3))
+    ms_plain_e2e, _, _ = timed(plain_e2e, e2e_steps)
+    ms_batch_e2e, _, _ = timed(batched_e2e, e2e_steps)
+    in_bytes = sum(h[2][0].numel() * 4 + h[2][1].numel() * 8 + h[3][0].numel() * 4 + h[3][1].numel() * 8
+                   for h in host)
+    ctx.close()
+    count = len(inst)
+    return {
+        "workload": "256 contractions a(i,c0,j,c1) x b(k,c0,c1), nnz(a) log-uniform [1e3, 2e6], "
+                    "nnz(b) = nnz(a)/2, extents uniform [32, 1024], Zipf s uniform [1.0, 1.5]",
+        "contractions": count, "multiply_adds": prods, "outputs": n_batch,
+        "plain": {"ms_per_contraction": ms_plain / count, "multiply_adds_per_s": prods / (ms_plain / 1000.0),
+                  "launches_per_step": l_plain,
+                  "e2e_ms_per_contraction": ms_plain_e2e / count},
+        "batched": {"ms_per_contraction": ms_batch / count, "multiply_adds_per_s": prods / (ms_batch / 1000.0),
+                    "launches_per_step": l_batch,
+                    "e2e_ms_per_contraction": ms_batch_e2e / count},
+        "speedup": ms_plain / ms_batch, "e2e_speedup": ms_plain_e2e / ms_batch_e2e,
+        "e2e_h2d_bytes_per_step": in_bytes,
+        "e2e_d2h_bytes_per_step": {"plain": n_batch * ((order - 1) * 4 + 8), "batched": n_batch * (order * 4 + 8)},
+        "steps": steps, "e2e_steps": e2e_steps, "warmup": warmup,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -247,9 +384,12 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--profile", choices=["zipf3-small", "twomode-small", "readme"],
                     help="one warm-up and one timed contraction of a small case, for ncu captures")
-    ap.add_argument("--sweep", choices=["zipf3", "twomode", "readme"],
+    ap.add_argument("--sweep", choices=["zipf3", "twomode", "readme", "batched"],
                     help="time the option sets given by --variants (JSON list) on a workload")
     ap.add_argument("--variants", default="[{}]")
+    ap.add_argument("--batched", action="store_true",
+                    help="print only the batched comparison (256 plain contractions vs one batched call)")
+    ap.add_argument("--no-batched", action="store_true", help="leave the batched comparison out")
     ap.add_argument("--diag", action="store_true",
                     help="print the FP64 FMA rate and the shared-memory accumulation rates")
     args = ap.parse_args()
@@ -279,6 +419,18 @@ def main():
         return
     if args.profile:
         run_profile_case(args.profile)
+        return
+    if args.batched:
+        import torch
+
+        import build_lib
+        build_lib.build_all()
+        torch.cuda.set_device(local)
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        out = run_batched(args.steps, args.warmup, stream, local)
+        if rank == 0:
+            print(json.dumps(out))
         return
 
     import numpy as np
@@ -382,6 +534,8 @@ def main():
         "clocks": clk,
         "phases_ms": {k: round(v, 4) for k, v in phases.items()},
     }
+    if not args.no_batched:
+        line["batched"] = run_batched(min(args.steps, 5), 3, stream, local)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         # bounded sample: grow it (halve `every`) until one run takes >= 8 s
         every = 256

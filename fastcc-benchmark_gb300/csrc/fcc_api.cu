@@ -13,7 +13,9 @@
 namespace fcc {
 void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
               const int32_t *ctrB, int k, const fcc_options &opt, fcc_result *res, i64 *products,
-              bool count_only);
+              bool count_only, const u32 *group_lb, u32 ngroups);
+void contract_batch(Runtime *ctx, int n, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                    const int32_t *ctrB, int k, const fcc_options &opt, fcc_result *res, i64 *counts);
 }
 
 namespace {
@@ -170,7 +172,23 @@ int fcc_contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const i
     fcc::Runtime rt = runtime_of(ctx);
     std::unique_ptr<fcc_result> r(new fcc_result());
     r->ctx = ctx;
-    fcc::contract(&rt, A, B, ctrA, ctrB, k, o, r.get(), nullptr, false);
+    fcc::contract(&rt, A, B, ctrA, ctrB, k, o, r.get(), nullptr, false, nullptr, 0);
+    *out = r.release();
+  });
+}
+
+int fcc_contract_batch(fcc_ctx *ctx, int32_t n, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                       const int32_t *ctrB, int32_t k, const fcc_options *opts, fcc_result **out,
+                       int64_t *counts) {
+  if (!ctx || !out) return FCC_ERR_ARG;
+  *out = nullptr;
+  fcc_options o;
+  if (opts) o = *opts; else fcc_options_default(&o);
+  return guarded(ctx, [&] {
+    fcc::Runtime rt = runtime_of(ctx);
+    std::unique_ptr<fcc_result> r(new fcc_result());
+    r->ctx = ctx;
+    fcc::contract_batch(&rt, n, A, B, ctrA, ctrB, k, o, r.get(), counts);
     *out = r.release();
   });
 }
@@ -182,7 +200,7 @@ int fcc_count_products(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, c
   if (opts) o = *opts; else fcc_options_default(&o);
   return guarded(ctx, [&] {
     fcc::Runtime rt = runtime_of(ctx);
-    fcc::contract(&rt, A, B, ctrA, ctrB, k, o, nullptr, products, true);
+    fcc::contract(&rt, A, B, ctrA, ctrB, k, o, nullptr, products, true, nullptr, 0);
   });
 }
 

@@ -43,10 +43,19 @@ struct LinSpec {
   int32_t max_index[FCC_MAX_ORDER];
 };
 
+// Division by a divisor fixed for a whole launch: q = n / d for n, d < 2^32
+// as the high half of n * m, m = ceil(2^64 / d) (the round-up method of
+// Granlund and Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994). Exact while n * d < 2^64: the error term
+// n * (m - 2^64/d) / 2^64 < n / 2^64 stays below 1/d. m = 0 encodes d = 1.
+__host__ __device__ __forceinline__ u64 magic_for(u64 d) { return d <= 1 ? 0 : (~0ull) / d + 1; }
+__device__ __forceinline__ u32 div_magic(u32 n, u64 m) { return m ? u32(__umul64hi(u64(n), m)) : n; }
+
 struct Decode {
   int na, nb;
   int narrow;  // every radix and both spans < 2^32
   u64 ra[FCC_MAX_ORDER], rb[FCC_MAX_ORDER];
+  u64 ma[FCC_MAX_ORDER], mb[FCC_MAX_ORDER];  // magic_for(ra[e]), magic_for(rb[e])
   const u32 *inv_col;  // renumbered B column -> B external index (NULL: identity)
 };
 
@@ -88,14 +97,14 @@ __device__ __forceinline__ void emit(const Out &o, const Decode &d, u64 idx, u64
   if (d.narrow) {
     u32 r = u32(row);
     for (int e = d.na - 1; e > 0; --e) {
-      u32 rad = u32(d.ra[e]), q = r / rad;
+      u32 rad = u32(d.ra[e]), q = div_magic(r, d.ma[e]);
       __stcs(&c[e * o.stride + idx], r - q * rad);
       r = q;
     }
     if (d.na > 0) __stcs(&c[idx], r);
     u32 s = u32(col);
     for (int e = d.nb - 1; e > 0; --e) {
-      u32 rad = u32(d.rb[e]), q = s / rad;
+      u32 rad = u32(d.rb[e]), q = div_magic(s, d.mb[e]);
       __stcs(&c[(d.na + e) * o.stride + idx], s - q * rad);
       s = q;
     }
@@ -234,28 +243,86 @@ __global__ void k_compact_a(const u32 *__restrict__ flag, const u32 *__restrict_
 
 // ------------------------------------------------------------ planning ----
 
-__global__ void k_tile_flags(const u64 *__restrict__ rowA, i64 n, u64 TL, u32 *__restrict__ flag) {
-  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x)
-    flag[i] = (i == 0 || rowA[i] / TL != rowA[i - 1] / TL) ? 1u : 0u;
+// Tiles are made of the rows that occur (A's external indices with at least
+// one matched entry), not of index ranges: row ranks come from a prefix sum
+// over row changes of the row-sorted entries, and a tile holds up to TL
+// consecutive ranks of one group. A group is a range of rows sharing
+// row / gdiv (the instance of a batched contraction, whose column span lb[g]
+// may be narrower than the whole B span); without groups (gdiv == 0) there is
+// one group with the whole span.
+struct RowGroups {
+  u64 gdiv;       // 0: no groups
+  const u32 *lb;  // per group: column span (B external columns in use)
+  u64 area;       // tile capacity in positions; TL of group g = area / lb[g]
+  u64 TL;         // > 0: fixed rows per tile for every group
+  u64 LB;         // column span without groups
+};
+
+__device__ __forceinline__ u32 group_of(const RowGroups &g, u64 row) { return g.gdiv ? u32(row / g.gdiv) : 0u; }
+__device__ __forceinline__ u64 group_lb(const RowGroups &g, u32 grp) { return g.gdiv ? u64(g.lb[grp]) : g.LB; }
+__device__ __forceinline__ u64 group_tl(const RowGroups &g, u32 grp) {
+  if (g.TL) return g.TL;
+  const u64 lb = group_lb(g, grp);
+  return lb >= g.area ? 1 : g.area / lb;
 }
 
+// rank[e] = rank of entry e's row among the distinct rows; urow[rank] = row;
+// gfirst[g] = rank of group g's first row. rflag: row changes, rexcl: their
+// exclusive prefix sum.
+__global__ void k_row_rank(const u64 *__restrict__ rowA, const u32 *__restrict__ rflag,
+                           const u32 *__restrict__ rexcl, i64 n, RowGroups g, u32 *__restrict__ rank,
+                           u64 *__restrict__ urow, u32 *__restrict__ gfirst) {
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
+    const u32 r = rexcl[i] + rflag[i] - 1u;
+    rank[i] = r;
+    if (rflag[i]) {
+      urow[r] = rowA[i];
+      const u32 grp = group_of(g, rowA[i]);
+      if (i == 0 || group_of(g, rowA[i - 1]) != grp) gfirst[grp] = r;
+    }
+  }
+}
+
+// slot[e] = position of e's row inside its tile; flag[e] = 1 where a tile starts.
+__global__ void k_row_tiles(const u64 *__restrict__ rowA, const u32 *__restrict__ rflag,
+                            const u32 *__restrict__ rank, i64 n, RowGroups g, const u32 *__restrict__ gfirst,
+                            u32 *__restrict__ slot, u32 *__restrict__ flag) {
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
+    const u32 grp = group_of(g, rowA[i]);
+    const u32 s = u32(u64(rank[i] - gfirst[grp]) % group_tl(g, grp));
+    slot[i] = s;
+    flag[i] = (rflag[i] && s == 0) ? 1u : 0u;
+  }
+}
+
+// Per tile: first entry, first row rank and column span.
 __global__ void k_tile_write(const u64 *__restrict__ rowA, const u32 *__restrict__ flag,
-                             const u32 *__restrict__ idx, i64 n, u64 TL, u64 *__restrict__ row0,
-                             u32 *__restrict__ abeg) {
+                             const u32 *__restrict__ idx, const u32 *__restrict__ rank, i64 n, RowGroups g,
+                             u32 *__restrict__ abeg, u32 *__restrict__ rank0, u32 *__restrict__ lb) {
   for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
     if (flag[i]) {
-      row0[idx[i]] = (rowA[i] / TL) * TL;
-      abeg[idx[i]] = u32(i);
+      const u32 t = idx[i];
+      abeg[t] = u32(i);
+      rank0[t] = rank[i];
+      lb[t] = u32(group_lb(g, group_of(g, rowA[i])));
     }
     if (i == n - 1) abeg[idx[i] + flag[i]] = u32(n);
   }
 }
 
+// Row count of each tile, from its last entry's rank.
+__global__ void k_tile_nrows(const u32 *__restrict__ ntiles_p, const u32 *__restrict__ abeg,
+                             const u32 *__restrict__ rank, const u32 *__restrict__ rank0, u32 *__restrict__ nrows) {
+  const u32 ntiles = *ntiles_p;
+  for (i64 t = i64(blockIdx.x) * blockDim.x + threadIdx.x; t < ntiles; t += i64(gridDim.x) * blockDim.x)
+    nrows[t] = rank[abeg[t + 1] - 1] - rank0[t] + 1;
+}
+
 // Per tile: work items, split flag, output bound and (hash) region size.
 __global__ void k_tile_items(const u32 *__restrict__ ntiles_p, i64 nmax, const u32 *__restrict__ abeg,
-                             const u64 *__restrict__ P, u64 pmax, u64 area, int hash_mode,
-                             u32 *__restrict__ nitems, u32 *__restrict__ split, u64 *__restrict__ cap,
-                             u64 *__restrict__ hsz) {
+                             const u64 *__restrict__ P, u64 pmax, const u32 *__restrict__ nrows,
+                             const u32 *__restrict__ lb, u64 LB, int hash_mode, u32 *__restrict__ nitems,
+                             u32 *__restrict__ split, u64 *__restrict__ cap, u64 *__restrict__ hsz) {
   const u32 ntiles = *ntiles_p;
   for (i64 t = i64(blockIdx.x) * blockDim.x + threadIdx.x; t < nmax; t += i64(gridDim.x) * blockDim.x) {
     if (t >= ntiles) {
@@ -264,6 +331,7 @@ __global__ void k_tile_items(const u32 *__restrict__ ntiles_p, i64 nmax, const u
     }
     const u64 prod = P[abeg[t + 1]] - P[abeg[t]];
     const u64 items = (prod + pmax - 1) / pmax;
+    const u64 area = u64(nrows[t]) * (lb ? u64(lb[t]) : LB);  // rows x LB fits 64 bits (host check)
     const u64 bound = prod < area ? prod : area;
     nitems[t] = u32(items);
     split[t] = items > 1 ? 1u : 0u;
@@ -364,7 +432,7 @@ constexpr u64 kNegZero = 0x8000000000000000ull;
 
 struct ProdSrc {
   const u64 *P;        // multiply-add prefix per compacted A entry (nA2 + 1)
-  const u64 *rowA;     // A external (row) index
+  const u32 *slotA;    // the entry's row inside its tile
   const u32 *sbA;      // first B entry of the entry's segment
   const double *valA;
   const double *valB;
@@ -411,7 +479,7 @@ __device__ __forceinline__ u64 coverage(const u64 *__restrict__ P, u32 e, u64 p0
 template <class ColT, class KeyT, class Add>
 __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__restrict__ colB, u32 alo,
                                                u32 ahi, u32 e0, u64 q0, u64 q1, u64 p0, u64 p1, u64 skip,
-                                               u64 row0, u64 LB, Add &add) {
+                                               u64 LB, Add &add) {
   const u32 lane = threadIdx.x & 31;
   u32 e = e0;
   if (e == kNoEntry) {
@@ -442,7 +510,7 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
     u32 b0 = 0;
     if (n > 0) {
       va = __ldg(&s.valA[el]);
-      base = KeyT((__ldg(&s.rowA[el]) - row0) * LB);
+      base = KeyT(u64(__ldg(&s.slotA[el])) * LB);
       b0 = __ldg(&s.sbA[el]) + u32(sg - pl);
     }
     while (stream) {  // warp-wide runs
@@ -504,7 +572,7 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
 // chunk starts are searched for.
 template <class ColT, class KeyT, class Add>
 __device__ __forceinline__ void products_item(const ProdSrc &s, const ColT *colB, u32 alo, u32 ahi, u64 p0,
-                                              u64 p1, u64 row0, u64 LB, u32 *s_chunk, Add &add) {
+                                              u64 p1, u64 LB, u32 *s_chunk, Add &add) {
   const u32 lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   const u64 np = p1 - p0;
   u64 chunk = np / (4 * nwarps);
@@ -517,7 +585,7 @@ __device__ __forceinline__ void products_item(const ProdSrc &s, const ColT *colB
     if (c >= nch) break;
     const u64 q0 = p0 + u64(c) * chunk;
     const u64 q1 = min(q0 + chunk, p1);
-    products_chunk<ColT, KeyT>(s, colB, alo, ahi, kNoEntry, q0, q1, p0, p1, kNoSkip, row0, LB, add);
+    products_chunk<ColT, KeyT>(s, colB, alo, ahi, kNoEntry, q0, q1, p0, p1, kNoSkip, LB, add);
   }
 }
 
@@ -585,7 +653,7 @@ __device__ void build_item_plan(const u64 *__restrict__ P, u32 alo, u32 ahi, u64
 
 template <bool kSentinel, class Add>
 __device__ void dense_item(const ProdSrc &s, const u32 *__restrict__ colB, u32 alo, u32 ahi, u64 p0, u64 p1,
-                           u64 row0, u32 LB, double *acc, u32 *mask, ItemPlan &pl, Add &add) {
+                           u32 LB, double *acc, u32 *mask, ItemPlan &pl, Add &add) {
   build_item_plan(s.P, alo, ahi, p0, p1, pl);
   const u32 tid = threadIdx.x, lane = tid & 31;
   const u32 nlong = min(pl.nlong, kListMax);
@@ -594,7 +662,7 @@ __device__ void dense_item(const ProdSrc &s, const u32 *__restrict__ colB, u32 a
     const u64 pb = __ldg(&s.P[e]);
     const u64 lo = max(pb, p0), hi = min(__ldg(&s.P[e + 1]), p1);
     const double va = __ldg(&s.valA[e]);
-    const u32 base = u32(__ldg(&s.rowA[e]) - row0) * LB;
+    const u32 base = __ldg(&s.slotA[e]) * LB;
     const u32 b0 = __ldg(&s.sbA[e]) + u32(lo - pb);
     const u32 n = u32(hi - lo);
     for (u32 o = 0; o < n; o += blockDim.x * kCtaPer) {
@@ -627,7 +695,7 @@ __device__ void dense_item(const ProdSrc &s, const u32 *__restrict__ colB, u32 a
     if (c >= nch) break;
     const u64 q0 = p0 + u64(c) * chunk;
     const u64 q1 = min(q0 + chunk, p1);
-    products_chunk<u32, u32>(s, colB, alo, ahi, pl.start[c], q0, q1, p0, p1, u64(kCtaRun), row0, LB, add);
+    products_chunk<u32, u32>(s, colB, alo, ahi, pl.start[c], q0, q1, p0, p1, u64(kCtaRun), LB, add);
   }
 }
 
@@ -635,14 +703,17 @@ struct DenseArgs {
   const Item *items;
   u32 nitems;
   u32 *counter;
-  const u64 *tile_row0;
   const u32 *tile_abeg;
+  const u32 *tile_rank0;  // first row rank
+  const u32 *tile_lb;     // column span
+  const u32 *tile_nrows;
+  const u64 *urow;        // row rank -> A external index
   const int *split_of_tile;
   const u32 *split_tiles;
   u32 nsplit;
   ProdSrc src;
   const u32 *colB;
-  u32 LB, area, words;
+  u32 area, words;        // tile capacity (positions, mask words)
   u32 hot;  // renumbered columns [0, hot) are accumulated per warp (row tiles only)
   double *gacc;
   u32 *gmask;
@@ -681,15 +752,19 @@ __device__ __forceinline__ u32 block_excl_u32(u32 v, u32 *s_warp, u32 *total) {
   return before + incl - v;
 }
 
-// Emits every touched position of a dense tile with its value and resets it
-// (mask words to 0; values to 0.0, or -0.0 with kSentinel). Pass 1 counts the
-// touched positions of each 32-position group, one prefix sum over the groups
-// reserves the output range, pass 2 writes each group's outputs contiguously.
-// s_cnt holds `words` (<= 4 * blockDim.x) entries.
+// Emits every touched position among the first `used` of a dense tile with
+// its value and resets it (mask words to 0; values to 0.0, or -0.0 with
+// kSentinel). Position p holds row urow[rank0 + p / LB], column p % LB
+// (lbm = magic_for(LB)). Pass 1 counts the touched positions of each
+// 32-position group, one prefix sum over the groups reserves the output
+// range, pass 2 writes each group's outputs contiguously. s_cnt holds
+// ceil(used / 32) (<= 4 * blockDim.x) entries.
 template <bool kSentinel>
-__device__ void drain_dense(double *acc, u32 *mask, u32 area, u32 words, u32 LB, u64 row0, const Out &out,
-                            const Decode &dec, u32 *err, u32 *s_cnt, u32 *s_warp, u64 *s_base) {
+__device__ void drain_dense(double *acc, u32 *mask, u32 used, u32 LB, u64 lbm, const u64 *__restrict__ urow,
+                            u32 rank0, const Out &out, const Decode &dec, u32 *err, u32 *s_cnt, u32 *s_warp,
+                            u64 *s_base) {
   const u32 tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const u32 words = (used + 31) / 32, area = used;
   for (u32 w = warp; w < words; w += nwarps) {
     const u32 b = group_mask<kSentinel>(acc, mask, area, w);
     if (lane == 0) s_cnt[w] = __popc(b);
@@ -723,7 +798,8 @@ __device__ void drain_dense(double *acc, u32 *mask, u32 area, u32 words, u32 LB,
       const u32 pos = w * 32 + lane;
       const double v = acc[pos];
       acc[pos] = reset;
-      if (write) emit(out, dec, base + s_cnt[w] + __popc(b & lt), row0 + pos / LB, pos % LB, v);
+      const u32 slot = div_magic(pos, lbm);
+      if (write) emit(out, dec, base + s_cnt[w] + __popc(b & lt), __ldg(&urow[rank0 + slot]), pos - slot * LB, v);
     }
     if (!kSentinel) {
       __syncwarp();
@@ -734,8 +810,9 @@ __device__ void drain_dense(double *acc, u32 *mask, u32 area, u32 words, u32 LB,
 
 // Adds a partial tile into its global split-tile buffer and resets it.
 template <bool kSentinel>
-__device__ void flush_dense(double *acc, u32 *mask, u32 area, u32 words, double *gacc, u32 *gmask) {
+__device__ void flush_dense(double *acc, u32 *mask, u32 used, double *gacc, u32 *gmask) {
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const u32 words = (used + 31) / 32, area = used;
   const double reset = kSentinel ? __longlong_as_double((long long)kNegZero) : 0.0;
   for (u32 w = warp; w < words; w += nwarps) {
     const u32 pos = w * 32 + lane;
@@ -851,9 +928,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
     if (it >= a.nitems) break;
     const Item item = a.items[it];
     const u32 t = item.tile;
-    const u64 row0 = a.tile_row0[t];
-    dense_item<kSentinel>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, row0, a.LB, acc,
-                          mask, plan, add);
+    const u32 LB = a.tile_lb[t], used = a.tile_nrows[t] * LB;
+    dense_item<kSentinel>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, LB, acc, mask,
+                          plan, add);
     __syncthreads();
     if (a.hot) {
       merge_hot_dense<kSentinel>(acc, mask, priv, pmask, a.hot);
@@ -861,11 +938,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
     }
     const int sidx = a.split_of_tile[t];
     if (sidx < 0)
-      drain_dense<kSentinel>(acc, mask, a.area, a.words, a.LB, row0, a.out, a.dec, a.err, s_cnt, s_warp,
-                             &s_base);
+      drain_dense<kSentinel>(acc, mask, used, LB, magic_for(LB), a.urow, a.tile_rank0[t], a.out, a.dec, a.err,
+                             s_cnt, s_warp, &s_base);
     else
-      flush_dense<kSentinel>(acc, mask, a.area, a.words, a.gacc + u64(sidx) * a.area,
-                             a.gmask + u64(sidx) * a.words);
+      flush_dense<kSentinel>(acc, mask, used, a.gacc + u64(sidx) * a.area, a.gmask + u64(sidx) * a.words);
     __syncthreads();
   }
 }
@@ -875,9 +951,10 @@ __global__ void __launch_bounds__(kTileThreads) k_merge_dense(DenseArgs a) {
   __shared__ u32 s_cnt[1024];
   __shared__ u64 s_base;
   for (u32 s = blockIdx.x; s < a.nsplit; s += gridDim.x) {
-    const u64 row0 = a.tile_row0[a.split_tiles[s]];
-    drain_dense<false>(a.gacc + u64(s) * a.area, a.gmask + u64(s) * a.words, a.area, a.words, a.LB, row0,
-                       a.out, a.dec, a.err, s_cnt, s_warp, &s_base);
+    const u32 t = a.split_tiles[s];
+    const u32 LB = a.tile_lb[t];
+    drain_dense<false>(a.gacc + u64(s) * a.area, a.gmask + u64(s) * a.words, a.tile_nrows[t] * LB, LB,
+                       magic_for(LB), a.urow, a.tile_rank0[t], a.out, a.dec, a.err, s_cnt, s_warp, &s_base);
     __syncthreads();
   }
 }
@@ -889,7 +966,8 @@ struct HashArgs {
   const Item *items;
   u32 nitems;
   u32 *counter;
-  const u64 *tile_row0;
+  const u32 *tile_rank0;  // first row rank
+  const u64 *urow;        // row rank -> A external index
   const u32 *tile_abeg;
   const int *split_of_tile;
   const u32 *split_tiles;
@@ -910,9 +988,11 @@ struct HashArgs {
 };
 
 // Emits occupied slots of an open-addressing table, coalesced per warp, and
-// resets them.
-__device__ void drain_hash(u64 *keys, double *vals, u64 nslots, u64 LB, u32 TL, u64 row0,
-                           const Out &out, const Decode &dec, u32 *err, u32 *s_wcnt, u64 *s_base) {
+// resets them. Key k holds row urow[rank0 + k / LB], column k % LB (column k
+// of row urow[rank0] when TL == 1).
+__device__ void drain_hash(u64 *keys, double *vals, u64 nslots, u64 LB, u32 TL, u32 rank0,
+                           const u64 *__restrict__ urow, const Out &out, const Decode &dec, u32 *err,
+                           u32 *s_wcnt, u64 *s_base) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   const u64 spw = ((nslots + nwarps - 1) / nwarps + 31) & ~u64(31);
   const u64 s0 = min(nslots, u64(warp) * spw), s1 = min(nslots, s0 + spw);
@@ -942,8 +1022,9 @@ __device__ void drain_hash(u64 *keys, double *vals, u64 nslots, u64 LB, u32 TL, 
     const u32 bal = __ballot_sync(kFull, occ);
     if (occ) {
       const double v = vals[s];
-      u64 row = row0, col = key;
-      if (TL > 1) { row = row0 + key / LB; col = key % LB; }
+      u64 slot = 0, col = key;
+      if (TL > 1) { slot = key / LB; col = key % LB; }
+      const u64 row = __ldg(&urow[rank0 + slot]);
       if (write) emit(out, dec, run + __popc(bal & lt), row, col, v);
     }
     if (s < s1) { keys[s] = kEmptyKey; vals[s] = 0.0; }
@@ -1027,12 +1108,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_hash(HashArgs<ColT> a)
     if (it >= a.nitems) break;
     const Item item = a.items[it];
     const u32 t = item.tile;
-    const u64 row0 = a.tile_row0[t];
     const u64 np = item.p1 - item.p0;
     u32 hsl = 64;
     while (u64(hsl) < 2 * np && hsl < a.slots) hsl <<= 1;
     HashAdd add{hk, hv, hsl - 1, a.err, priv + size_t(warp) * a.hot, pmask + size_t(warp) * pw, a.hot};
-    products_item<ColT, u64>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, row0, a.LB,
+    products_item<ColT, u64>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, a.LB,
                              &s_chunk, add);
     __syncthreads();
     if (a.hot) {  // per-warp hot columns -> the table (their keys were counted in np)
@@ -1052,7 +1132,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_hash(HashArgs<ColT> a)
     }
     const int sidx = a.split_of_tile[t];
     if (sidx < 0) {
-      drain_hash(hk, hv, hsl, a.LB, a.TL, row0, a.out, a.dec, a.err, s_wcnt, &s_base);
+      drain_hash(hk, hv, hsl, a.LB, a.TL, a.tile_rank0[t], a.urow, a.out, a.dec, a.err, s_wcnt, &s_base);
     } else {
       const u64 off = a.hoff[t], hs = a.hsz[t];
       for (u32 s = tid; s < hsl; s += blockDim.x) {
@@ -1075,7 +1155,7 @@ __global__ void __launch_bounds__(kTileThreads) k_merge_hash(HashArgs<ColT> a) {
   for (u32 s = blockIdx.x; s < a.nsplit; s += gridDim.x) {
     const u32 t = a.split_tiles[s];
     const u64 off = a.hoff[t];
-    drain_hash(a.gkeys + off, a.gvals + off, a.hsz[t], a.LB, a.TL, a.tile_row0[t], a.out, a.dec,
+    drain_hash(a.gkeys + off, a.gvals + off, a.hsz[t], a.LB, a.TL, a.tile_rank0[t], a.urow, a.out, a.dec,
                a.err, s_wcnt, &s_base);
     __syncthreads();
   }
@@ -1174,7 +1254,7 @@ const double *upload_values(Runtime *ctx, const fcc_tensor *t) {
 }
 
 // Device scalar block: slot numbers in a u64 array.
-enum Scalar { S_NSEG = 0, S_NA2, S_NTILES, S_NITEMS, S_NSPLIT, S_CAP, S_HASH, S_CURSOR, S_COUNTER,
+enum Scalar { S_NSEG = 0, S_NA2, S_NTILES, S_NITEMS, S_NSPLIT, S_CAP, S_HASH, S_CURSOR, S_COUNTER, S_NROWS,
               S_PTOTAL, S_ERR, S_TINY, S_HOT, S_COUNT };
 
 // Copies the scalar block and the error word to pinned host memory, waits,
@@ -1235,10 +1315,12 @@ struct Timing {
 // The whole contraction. count_only stops after the segment lookup and
 // returns the multiply-add count in *products. res (NULL when count_only)
 // receives the output; its buffers come from ctx->pool, or are the caller's
-// buffers of ctx when ctx->pool is NULL.
+// buffers of ctx when ctx->pool is NULL. group_lb (ngroups entries, may be
+// NULL) makes A's leading external index a group index: rows of group g use
+// B columns [0, group_lb[g]) only, and dense tiles are sized per group.
 void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
               const int32_t *ctrB, int k, const fcc_options &opt, fcc_result *res, i64 *products,
-              bool count_only) {
+              bool count_only, const u32 *group_lb, u32 ngroups) {
   check_tensor(A, "A");
   check_tensor(B, "B");
   if (k < 0 || k > A->order || k > B->order) throw Error{FCC_ERR_ARG, "bad number of contracted modes"};
@@ -1387,7 +1469,19 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   u64 pmax = opt.products_per_item > 0 ? u64(opt.products_per_item) : (dense ? (u64(1) << 20) : u64(hslots / 2));
   if (!dense && pmax > hslots / 2) pmax = hslots / 2;
   if (dense && pmax > u64(kListMax) * kCtaRun) pmax = u64(kListMax) * kCtaRun;
-  const u64 area = TL * LB;
+  // Row groups (batched contractions): dense tiles hold rows of one group,
+  // group_tl rows of the group's own column span each.
+  const bool grouped = dense && group_lb && ngroups > 0;
+  u64 area = TL * LB;
+  if (grouped) {
+    area = 0;
+    for (u32 g = 0; g < ngroups; g++) {
+      const u64 lb = std::max<u32>(group_lb[g], 1u);
+      if (lb > LB) throw Error{FCC_ERR_CUDA, "group column span exceeds the B span"};
+      const u64 tl = opt.rows_per_tile > 0 ? TL : std::max<u64>(1, dense_cap / lb);
+      area = std::max(area, tl * lb);
+    }
+  }
   const int threads = opt.tile_threads > 0 ? opt.tile_threads : kTileThreads;
   if (threads != 512 && threads != 1024) throw Error{FCC_ERR_ARG, "tile_threads must be 512 or 1024"};
   if (opt.hot_columns < -1 || (opt.hot_columns > 0 && opt.hot_columns % 32))
@@ -1395,7 +1489,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
 
   // Hot columns (row tiles only): frequency of each B column, most frequent first.
   const u32 hot_want = opt.hot_columns > 0 ? u32(opt.hot_columns) : 128u;
-  const bool hot_try = TL == 1 && opt.hot_columns > 0 && LB <= (u64(1) << 26) && LB >= 2 * u64(hot_want);
+  const bool hot_try = !grouped && TL == 1 && opt.hot_columns > 0 && LB <= (u64(1) << 26) && LB >= 2 * u64(hot_want);
   u32 *colmap = nullptr, *inv_col = nullptr;
   if (hot_try) {
     const int lbits = bits_for(LB - 1);
@@ -1416,18 +1510,42 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     FCC_LAUNCH_CHECK();
   }
 
-  u32 *tflag = ar.get_n<u32>(nA2), *tidx = ar.get_n<u32>(nA2);
-  k_tile_flags<<<grid_for(nA2, 256), 256, 0, st>>>(rowA, nA2, TL, tflag);
+  // ---- tiles over the rows that occur ----
+  RowGroups rg{};
+  rg.LB = LB;
+  rg.area = dense_cap;
+  rg.TL = (grouped && opt.rows_per_tile <= 0) ? 0 : TL;
+  const u32 ng = grouped ? ngroups : 1u;
+  if (grouped) {
+    rg.gdiv = sa.span / sa.lin.ext_radix[0];
+    u32 *d_lb = ar.get_n<u32>(ng);
+    FCC_CUDA(cudaMemcpyAsync(d_lb, group_lb, sizeof(u32) * ng, cudaMemcpyHostToDevice, st));
+    rg.lb = d_lb;
+  }
+  u32 *rflag = ar.get_n<u32>(nA2), *rexcl = ar.get_n<u32>(nA2), *rank = ar.get_n<u32>(nA2);
+  u64 *urow = ar.get_n<u64>(nA2);
+  u32 *gfirst = ar.get_n<u32>(ng);
+  k_flag_change<<<grid_for(nA2, 256), 256, 0, st>>>(rowA, nA2, rflag);
+  FCC_LAUNCH_CHECK();
+  scan_exclusive(rflag, rexcl, nA2, sc32(S_NROWS), ar, st);
+  k_row_rank<<<grid_for(nA2, 256), 256, 0, st>>>(rowA, rflag, rexcl, nA2, rg, rank, urow, gfirst);
+  FCC_LAUNCH_CHECK();
+  u32 *slotA = ar.get_n<u32>(nA2), *tflag = ar.get_n<u32>(nA2), *tidx = ar.get_n<u32>(nA2);
+  k_row_tiles<<<grid_for(nA2, 256), 256, 0, st>>>(rowA, rflag, rank, nA2, rg, gfirst, slotA, tflag);
   FCC_LAUNCH_CHECK();
   scan_exclusive(tflag, tidx, nA2, sc32(S_NTILES), ar, st);
-  u64 *tile_row0 = ar.get_n<u64>(nA2);
-  u32 *tile_abeg = ar.get_n<u32>(nA2 + 1);
-  k_tile_write<<<grid_for(nA2, 256), 256, 0, st>>>(rowA, tflag, tidx, nA2, TL, tile_row0, tile_abeg);
+  u32 *tile_abeg = ar.get_n<u32>(nA2 + 1), *tile_rank0 = ar.get_n<u32>(nA2);
+  u32 *tile_lb = ar.get_n<u32>(nA2), *tile_nrows = ar.get_n<u32>(nA2);
+  k_tile_write<<<grid_for(nA2, 256), 256, 0, st>>>(rowA, tflag, tidx, rank, nA2, rg, tile_abeg, tile_rank0,
+                                                   tile_lb);
+  FCC_LAUNCH_CHECK();
+  k_tile_nrows<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), tile_abeg, rank, tile_rank0, tile_nrows);
   FCC_LAUNCH_CHECK();
   u32 *t_items = ar.get_n<u32>(nA2), *t_split = ar.get_n<u32>(nA2);
   u64 *t_cap = ar.get_n<u64>(nA2), *t_hsz = ar.get_n<u64>(nA2);
-  k_tile_items<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), nA2, tile_abeg, P, pmax, area, dense ? 0 : 1,
-                                                   t_items, t_split, t_cap, t_hsz);
+  k_tile_items<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), nA2, tile_abeg, P, pmax, tile_nrows,
+                                                   dense ? tile_lb : nullptr, LB, dense ? 0 : 1, t_items, t_split,
+                                                   t_cap, t_hsz);
   FCC_LAUNCH_CHECK();
   u32 *item_off = ar.get_n<u32>(nA2), *split_idx = ar.get_n<u32>(nA2);
   u64 *t_hoff = ar.get_n<u64>(nA2);
@@ -1489,13 +1607,13 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       FCC_LAUNCH_CHECK();
     }
   }
-  const ProdSrc src{P, rowA, sbA, valA, valB};
+  const ProdSrc src{P, slotA, sbA, valA, valB};
   Decode dec{};
   dec.inv_col = hot ? inv_col : nullptr;
   dec.na = sa.lin.n_ext;
   dec.nb = sb.lin.n_ext;
-  for (int e = 0; e < dec.na; e++) dec.ra[e] = sa.lin.ext_radix[e];
-  for (int e = 0; e < dec.nb; e++) dec.rb[e] = sb.lin.ext_radix[e];
+  for (int e = 0; e < dec.na; e++) dec.ra[e] = sa.lin.ext_radix[e], dec.ma[e] = magic_for(dec.ra[e]);
+  for (int e = 0; e < dec.nb; e++) dec.rb[e] = sb.lin.ext_radix[e], dec.mb[e] = magic_for(dec.rb[e]);
   dec.narrow = (sa.span <= 0xFFFFFFFFull && sb.span <= 0xFFFFFFFFull) ? 1 : 0;
 
   // Output capacity: the planner's upper bound, limited to half of the free
@@ -1531,9 +1649,9 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
         FCC_CUDA(cudaMemsetAsync(gacc, 0, sizeof(double) * nsplit * area, st));
         FCC_CUDA(cudaMemsetAsync(gmask, 0, sizeof(u32) * nsplit * words, st));
       }
-      DenseArgs a{items, nitems, counter, tile_row0, tile_abeg, split_of_tile, split_tiles, nsplit,
-                  src, static_cast<const u32 *>(colB), u32(LB), u32(area), u32(words), hot, gacc, gmask, o, dec,
-                  ctx->d_err};
+      DenseArgs a{items, nitems, counter, tile_abeg, tile_rank0, tile_lb, tile_nrows, urow, split_of_tile,
+                  split_tiles, nsplit, src, static_cast<const u32 *>(colB), u32(area), u32(words), hot, gacc, gmask,
+                  o, dec, ctx->d_err};
       const size_t smem = ((size_t(area) * 8 + (sentinel ? 0 : size_t(words) * 4) + 15) & ~size_t(15)) +
                           size_t(nwarps) * hot * 8 + size_t(nwarps) * (hot / 32) * 4;
       const void *kern;
@@ -1564,7 +1682,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       const size_t smem = size_t(hslots) * 16 + size_t(nwarps) * hot * 8 + size_t(nwarps) * (hot / 32) * 4;
       auto launch = [&](auto colptr) {
         using ColT = std::remove_const_t<std::remove_pointer_t<decltype(colptr)>>;
-        HashArgs<ColT> a{items, nitems, counter, tile_row0, tile_abeg, split_of_tile, split_tiles, nsplit,
+        HashArgs<ColT> a{items, nitems, counter, tile_rank0, urow, tile_abeg, split_of_tile, split_tiles, nsplit,
                          src, colptr, LB, u32(TL), hslots, hot, t_hoff, t_hsz, gkeys, gvals, o, dec, ctx->d_err};
         const void *kern = threads == 512 ? reinterpret_cast<const void *>(k_contract_hash<ColT, 512>)
                                           : reinterpret_cast<const void *>(k_contract_hash<ColT, 1024>);

@@ -9,7 +9,7 @@
 namespace fcc {
 void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
               const int32_t *ctrB, int k, const fcc_options &opt, fcc_result *res, i64 *products,
-              bool count_only);
+              bool count_only, const u32 *group_lb, u32 ngroups);
 }
 
 namespace {
@@ -103,7 +103,7 @@ extern "C" int fcc_contract_noalloc(const fcc_tensor *A, const fcc_tensor *B, co
     o.timing = 0;
     o.capacity_hint = 0;
     fcc::i64 products = 0;
-    fcc::contract(&rt, A, B, ctrA, ctrB, k, o, &res, &products, false);
+    fcc::contract(&rt, A, B, ctrA, ctrB, k, o, &res, &products, false, nullptr, 0);
     *out_nnz = res.nnz;
     if (out_products) *out_products = products;
     return FCC_OK;

@@ -77,6 +77,8 @@ def lib():
                                    ctypes.POINTER(Options), ctypes.POINTER(vp)]
         L.fcc_count_products.argtypes = [vp, ctypes.POINTER(_CTensor), ctypes.POINTER(_CTensor), vp, vp,
                                          i32, ctypes.POINTER(Options), ctypes.POINTER(i64)]
+        L.fcc_contract_batch.argtypes = [vp, i32, ctypes.POINTER(_CTensor), ctypes.POINTER(_CTensor), vp, vp,
+                                         i32, ctypes.POINTER(Options), ctypes.POINTER(vp), vp]
         L.fcc_result_info.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i64), ctypes.POINTER(i64)]
         L.fcc_result_device.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(i64), ctypes.POINTER(vp)]
         L.fcc_result_copy_to_host.argtypes = [vp, vp, i64, i64, vp]
@@ -221,6 +223,28 @@ class Context:
                                 int(ca.size), ctypes.byref(o), ctypes.byref(out))
         self._check(rc)
         return Result(self, out.value)
+
+    def contract_batch(self, As, Bs, ctr_a, ctr_b, opts=None):
+        """n independent products As[t] x Bs[t] in one pipeline
+        (fcc_contract_batch). Returns (Result, counts): the result's mode 0 is
+        the instance, counts[t] the entries of instance t."""
+        if len(As) != len(Bs) or not As:
+            raise ValueError("As and Bs must be non-empty and of one length")
+        ca = np.ascontiguousarray(ctr_a, dtype=np.int32)
+        cb = np.ascontiguousarray(ctr_b, dtype=np.int32)
+        if ca.shape != cb.shape:
+            raise ValueError("contracted mode lists differ in length")
+        n = len(As)
+        ta = (_CTensor * n)(*[a._struct() for a in As])
+        tb = (_CTensor * n)(*[b._struct() for b in Bs])
+        counts = np.zeros(n, np.int64)
+        out = ctypes.c_void_p()
+        o = opts if opts is not None else Options()
+        rc = lib().fcc_contract_batch(self._h, n, ta, tb, ca.ctypes.data if ca.size else None,
+                                      cb.ctypes.data if cb.size else None, int(ca.size), ctypes.byref(o),
+                                      ctypes.byref(out), counts.ctypes.data)
+        self._check(rc)
+        return Result(self, out.value), counts
 
     def fastcc_multiply(self, a, b, ctr_a, ctr_b, tile_size=100, accumulator=ACC_AUTO):
         """Mirror of Tensor<DT>::fastcc_multiply<AccType, RES>(other, left_contr,

@@ -168,6 +168,25 @@ int fcc_count_products(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B,
 int fcc_abi_version(void);
 
 /*
+ * Batched contraction: n independent products A[t] x B[t] of one mode
+ * pattern (every A[t] of one order, every B[t] of one order, the same ctrA,
+ * ctrB, k), run as ONE pipeline: one index build, one tile plan and one
+ * persistent tile-kernel launch for the whole batch. The reference has no
+ * batched call; it replaces n calls of Tensor<DT>::fastcc_multiply
+ * (contract.hpp:824-912) and gives, per instance, exactly their entries.
+ *
+ * The result has one more mode than a single product: mode 0 is the
+ * instance t, followed by t's output coordinates in fcc_contract's order.
+ * Entries of all instances are interleaved in no particular order; counts
+ * (n int64, may be NULL) receives each instance's entry count. Limits:
+ * order(A) <= 6, order(B) <= 7, and per operand at most 2^31-1 nonzeros
+ * over the batch. opts->radix_mode is ignored: radices are shared.
+ */
+int fcc_contract_batch(fcc_ctx *ctx, int32_t n, const fcc_tensor *A, const fcc_tensor *B,
+                       const int32_t *ctrA, const int32_t *ctrB, int32_t k, const fcc_options *opts,
+                       fcc_result **out, int64_t *counts);
+
+/*
  * fcc_contract_noalloc - the contraction for callers that cannot allocate
  * device memory. It has no counterpart in the reference (whose CPU code
  * allocates freely).
