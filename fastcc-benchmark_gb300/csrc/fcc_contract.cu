@@ -610,8 +610,9 @@ struct ItemPlan {
   u32 ea, eb, nlong, nchunk, next;
   u64 chunk;
   u32 list[kListMax];
-  u32 start[kChunkMax];
+  u32 start[kChunkMax];  // also the drain's row cache (kRowCache u64)
 };
+constexpr u32 kRowCache = kChunkMax / 2;
 
 __device__ void build_item_plan(const u64 *__restrict__ P, u32 alo, u32 ahi, u64 p0, u64 p1, ItemPlan &pl) {
   const u32 tid = threadIdx.x, nwarps = blockDim.x >> 5;
@@ -762,9 +763,14 @@ __device__ __forceinline__ u32 block_excl_u32(u32 v, u32 *s_warp, u32 *total) {
 template <bool kSentinel>
 __device__ void drain_dense(double *acc, u32 *mask, u32 used, u32 LB, u64 lbm, const u64 *__restrict__ urow,
                             u32 rank0, const Out &out, const Decode &dec, u32 *err, u32 *s_cnt, u32 *s_warp,
-                            u64 *s_base) {
+                            u64 *s_base, u64 *s_rows) {
   const u32 tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   const u32 words = (used + 31) / 32, area = used;
+  // the tile's rows, staged once (the barrier after pass 1 publishes them)
+  const u32 nrows = div_magic(used, lbm);
+  const bool cached = nrows <= kRowCache;
+  if (cached)
+    for (u32 i = tid; i < nrows; i += blockDim.x) s_rows[i] = __ldg(&urow[rank0 + i]);
   for (u32 w = warp; w < words; w += nwarps) {
     const u32 b = group_mask<kSentinel>(acc, mask, area, w);
     if (lane == 0) s_cnt[w] = __popc(b);
@@ -799,7 +805,8 @@ __device__ void drain_dense(double *acc, u32 *mask, u32 used, u32 LB, u64 lbm, c
       const double v = acc[pos];
       acc[pos] = reset;
       const u32 slot = div_magic(pos, lbm);
-      if (write) emit(out, dec, base + s_cnt[w] + __popc(b & lt), __ldg(&urow[rank0 + slot]), pos - slot * LB, v);
+      const u64 row = cached ? s_rows[slot] : __ldg(&urow[rank0 + slot]);
+      if (write) emit(out, dec, base + s_cnt[w] + __popc(b & lt), row, pos - slot * LB, v);
     }
     if (!kSentinel) {
       __syncwarp();
@@ -939,7 +946,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
     const int sidx = a.split_of_tile[t];
     if (sidx < 0)
       drain_dense<kSentinel>(acc, mask, used, LB, magic_for(LB), a.urow, a.tile_rank0[t], a.out, a.dec, a.err,
-                             s_cnt, s_warp, &s_base);
+                             s_cnt, s_warp, &s_base, reinterpret_cast<u64 *>(plan.start));  // plan is idle
     else
       flush_dense<kSentinel>(acc, mask, used, a.gacc + u64(sidx) * a.area, a.gmask + u64(sidx) * a.words);
     __syncthreads();
@@ -950,11 +957,12 @@ __global__ void __launch_bounds__(kTileThreads) k_merge_dense(DenseArgs a) {
   __shared__ u32 s_warp[32];
   __shared__ u32 s_cnt[1024];
   __shared__ u64 s_base;
+  __shared__ u64 s_rows[kRowCache];
   for (u32 s = blockIdx.x; s < a.nsplit; s += gridDim.x) {
     const u32 t = a.split_tiles[s];
     const u32 LB = a.tile_lb[t];
     drain_dense<false>(a.gacc + u64(s) * a.area, a.gmask + u64(s) * a.words, a.tile_nrows[t] * LB, LB,
-                       magic_for(LB), a.urow, a.tile_rank0[t], a.out, a.dec, a.err, s_cnt, s_warp, &s_base);
+                       magic_for(LB), a.urow, a.tile_rank0[t], a.out, a.dec, a.err, s_cnt, s_warp, &s_base, s_rows);
     __syncthreads();
   }
 }
@@ -968,6 +976,7 @@ struct HashArgs {
   u32 *counter;
   const u32 *tile_rank0;  // first row rank
   const u64 *urow;        // row rank -> A external index
+  const u32 *tile_nrows;
   const u32 *tile_abeg;
   const int *split_of_tile;
   const u32 *split_tiles;
@@ -990,10 +999,14 @@ struct HashArgs {
 // Emits occupied slots of an open-addressing table, coalesced per warp, and
 // resets them. Key k holds row urow[rank0 + k / LB], column k % LB (column k
 // of row urow[rank0] when TL == 1).
-__device__ void drain_hash(u64 *keys, double *vals, u64 nslots, u64 LB, u32 TL, u32 rank0,
+__device__ void drain_hash(u64 *keys, double *vals, u64 nslots, u64 LB, u32 TL, u32 rank0, u32 nrows,
                            const u64 *__restrict__ urow, const Out &out, const Decode &dec, u32 *err,
-                           u32 *s_wcnt, u64 *s_base) {
+                           u32 *s_wcnt, u64 *s_base, u64 *s_rows) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  // the tile's rows, staged once (the barrier after the count publishes them)
+  const bool cached = nrows <= kRowCache;
+  if (cached)
+    for (u32 i = tid; i < nrows; i += blockDim.x) s_rows[i] = __ldg(&urow[rank0 + i]);
   const u64 spw = ((nslots + nwarps - 1) / nwarps + 31) & ~u64(31);
   const u64 s0 = min(nslots, u64(warp) * spw), s1 = min(nslots, s0 + spw);
   u32 c = 0;
@@ -1024,7 +1037,7 @@ __device__ void drain_hash(u64 *keys, double *vals, u64 nslots, u64 LB, u32 TL, 
       const double v = vals[s];
       u64 slot = 0, col = key;
       if (TL > 1) { slot = key / LB; col = key % LB; }
-      const u64 row = __ldg(&urow[rank0 + slot]);
+      const u64 row = cached ? s_rows[slot] : __ldg(&urow[rank0 + slot]);
       if (write) emit(out, dec, run + __popc(bal & lt), row, col, v);
     }
     if (s < s1) { keys[s] = kEmptyKey; vals[s] = 0.0; }
@@ -1094,6 +1107,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_hash(HashArgs<ColT> a)
   __shared__ u32 s_item, s_chunk;
   __shared__ u32 s_wcnt[32];
   __shared__ u64 s_base;
+  __shared__ u64 s_rows[kRowCache];
   const int tid = threadIdx.x;
   for (u32 i = tid; i < a.slots; i += blockDim.x) { hk[i] = kEmptyKey; hv[i] = 0.0; }
   for (u32 i = tid; i < nwarps * a.hot; i += blockDim.x) priv[i] = 0.0;
@@ -1132,7 +1146,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_hash(HashArgs<ColT> a)
     }
     const int sidx = a.split_of_tile[t];
     if (sidx < 0) {
-      drain_hash(hk, hv, hsl, a.LB, a.TL, a.tile_rank0[t], a.urow, a.out, a.dec, a.err, s_wcnt, &s_base);
+      drain_hash(hk, hv, hsl, a.LB, a.TL, a.tile_rank0[t], a.tile_nrows[t], a.urow, a.out, a.dec, a.err, s_wcnt,
+                 &s_base, s_rows);
     } else {
       const u64 off = a.hoff[t], hs = a.hsz[t];
       for (u32 s = tid; s < hsl; s += blockDim.x) {
@@ -1152,11 +1167,12 @@ template <class ColT>
 __global__ void __launch_bounds__(kTileThreads) k_merge_hash(HashArgs<ColT> a) {
   __shared__ u32 s_wcnt[32];
   __shared__ u64 s_base;
+  __shared__ u64 s_rows[kRowCache];
   for (u32 s = blockIdx.x; s < a.nsplit; s += gridDim.x) {
     const u32 t = a.split_tiles[s];
     const u64 off = a.hoff[t];
-    drain_hash(a.gkeys + off, a.gvals + off, a.hsz[t], a.LB, a.TL, a.tile_rank0[t], a.urow, a.out, a.dec,
-               a.err, s_wcnt, &s_base);
+    drain_hash(a.gkeys + off, a.gvals + off, a.hsz[t], a.LB, a.TL, a.tile_rank0[t], a.tile_nrows[t], a.urow,
+               a.out, a.dec, a.err, s_wcnt, &s_base, s_rows);
     __syncthreads();
   }
 }
@@ -1682,7 +1698,8 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       const size_t smem = size_t(hslots) * 16 + size_t(nwarps) * hot * 8 + size_t(nwarps) * (hot / 32) * 4;
       auto launch = [&](auto colptr) {
         using ColT = std::remove_const_t<std::remove_pointer_t<decltype(colptr)>>;
-        HashArgs<ColT> a{items, nitems, counter, tile_rank0, urow, tile_abeg, split_of_tile, split_tiles, nsplit,
+        HashArgs<ColT> a{items, nitems, counter, tile_rank0, urow, tile_nrows, tile_abeg, split_of_tile, split_tiles,
+                         nsplit,
                          src, colptr, LB, u32(TL), hslots, hot, t_hoff, t_hsz, gkeys, gvals, o, dec, ctx->d_err};
         const void *kern = threads == 512 ? reinterpret_cast<const void *>(k_contract_hash<ColT, 512>)
                                           : reinterpret_cast<const void *>(k_contract_hash<ColT, 1024>);
