@@ -207,6 +207,124 @@ def run_profile_case(name):
             r.free()
 
 
+class _Dev:
+    """A device pointer for torch.as_tensor (CUDA array interface)."""
+
+    def __init__(self, ptr, n, typestr):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False),
+                                         "version": 3, "strides": None}
+
+
+def fingerprint(r):
+    """Order-independent digest of a device result: (entries, sum of hashed
+    coordinates mod 2^64, sum of values, sum of |values|)."""
+    import torch
+    cptr, stride, vptr = r.device_pointers()
+    n = r.nnz
+    if n == 0:
+        return 0, 0, 0.0, 0.0
+    v = torch.as_tensor(_Dev(vptr, n, "<f8"), device="cuda")
+    h = torch.zeros(n, dtype=torch.int64, device="cuda")
+    for m in range(r.order):
+        c = torch.as_tensor(_Dev(cptr + 4 * m * stride, n, "<i4"), device="cuda").long()
+        h = h * 1000003 + c + 1  # int64 arithmetic wraps: a hash mod 2^64
+    return n, int(h.sum().item()), float(v.sum().item()), float(v.abs().sum().item())
+
+
+def run_sched_eval(model_path, reps=3):
+    """Held-out evaluation of the learned schedule: seeds the cost model was
+    not trained on, shapes of the two-mode and batched workloads. Per case:
+    the autotuner's best uniform schedule against FCC_SCHED_LEARNED (median
+    total time over reps), with identical output digests required. Then the
+    batched workload end to end: 256 plain contractions, each with its
+    autotuned options, against one batched call with the learned schedule."""
+    import numpy as np
+    import torch
+
+    import fastcc_gpu as F
+    import workloads
+    model = np.fromfile(model_path, np.float32)
+    ctx = F.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    cuda = lambda t: F.Tensor(torch.from_numpy(t.coords).cuda(), torch.from_numpy(t.values).cuda(), t.max_index)
+
+    def timed(call, opts):
+        ts, fp = [], None
+        for rep in range(reps + 1):
+            r = call(opts)
+            if rep == 0:
+                fp = fingerprint(r)
+            r.free()
+            if rep:
+                ts.append(ctx.timings()["total"])
+        return statistics.median(ts), fp
+
+    def same(fa, fb):
+        return fa[0] == fb[0] and fa[1] == fb[1] and abs(fa[2] - fb[2]) <= 1e-9 * max(fa[3], 1e-300)
+
+    cases = []
+    for seed in (101, 102):
+        w = workloads.twomode(seed=seed)
+        A = cuda(w["a"])
+        cases.append((f"twomode seed {seed}", lambda o, A=A, w=w: ctx.contract(A, A, w["ctr_a"], w["ctr_b"], o),
+                      lambda base, A=A, w=w: ctx.autotune(A, A, w["ctr_a"], w["ctr_b"], base, reps)))
+    inst = workloads.batched(seed=101, count=256)
+    As = [cuda(x["a"]) for x in inst]
+    Bs = [cuda(x["b"]) for x in inst]
+    cases.append(("batched seed 101", lambda o: ctx.contract_batch(As, Bs, [1, 3], [1, 2], o)[0],
+                  lambda base: ctx.autotune_batch(As, Bs, [1, 3], [1, 2], base, reps)))
+    torch.cuda.synchronize()
+    out = []
+    for name, call, tune in cases:
+        best, _ = tune(F.Options(timing=1))
+        t_auto, fp_auto = timed(call, best)
+        t_rule, fp_rule = timed(call, F.Options(timing=1))
+        ctx.sched_set_model(model)
+        t_learn, fp_learn = timed(call, F.Options(timing=1, schedule=F.SCHED_LEARNED))
+        cls = np.bincount(ctx.sched_last_tiles(features=False, cost=False)["cls"], minlength=F.NUM_CLASSES)
+        ctx.sched_set_model(None)
+        line = {"case": name, "autotuned": F.Context.options_dict(best), "autotuned_ms": t_auto, "rule_ms": t_rule,
+                "learned_ms": t_learn, "learned_vs_autotuned": t_auto / t_learn,
+                "learned_tiles_per_class": [int(c) for c in cls],
+                "identical_output": same(fp_auto, fp_learn) and same(fp_auto, fp_rule), "outputs": fp_auto[0]}
+        print(json.dumps(line), flush=True)
+        out.append(line)
+    # batched + learned against 256 autotuned plain contractions
+    plain_opts = []
+    for a, b in zip(As, Bs):
+        best, _ = ctx.autotune(a, b, [1, 3], [1, 2], F.Options(timing=1), 1)
+        plain_opts.append(best)
+    for a, b, o in zip(As, Bs, plain_opts):  # warm-up
+        ctx.contract(a, b, [1, 3], [1, 2], o).free()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for a, b, o in zip(As, Bs, plain_opts):
+        ctx.contract(a, b, [1, 3], [1, 2], o).free()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    ctx.sched_set_model(model)
+    lo = F.Options(schedule=F.SCHED_LEARNED)
+    ctx.contract_batch(As, Bs, [1, 3], [1, 2], lo)[0].free()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        ctx.contract_batch(As, Bs, [1, 3], [1, 2], lo)[0].free()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batch_ms = e0.elapsed_time(e1) / reps
+    line = {"case": "batched seed 101: 256 autotuned plain contractions vs one batched learned call",
+            "plain_autotuned_ms_per_contraction": plain_ms / 256,
+            "batched_learned_ms_per_contraction": batch_ms / 256, "speedup": plain_ms / batch_ms}
+    print(json.dumps(line), flush=True)
+    out.append(line)
+    ctx.close()
+    return out
+
+
 def run_sweep_batched(variants, reps):
     """The batched workload: each option set timed on one fcc_contract_batch
     call (median of reps, per-phase times)."""
@@ -387,6 +505,8 @@ def main():
     ap.add_argument("--sweep", choices=["zipf3", "twomode", "readme", "batched"],
                     help="time the option sets given by --variants (JSON list) on a workload")
     ap.add_argument("--variants", default="[{}]")
+    ap.add_argument("--sched-eval", metavar="MODEL", default=None,
+                    help="held-out evaluation of a cost model file against the autotuner")
     ap.add_argument("--batched", action="store_true",
                     help="print only the batched comparison (256 plain contractions vs one batched call)")
     ap.add_argument("--no-batched", action="store_true", help="leave the batched comparison out")
@@ -411,6 +531,11 @@ def main():
         return
     if args.sweep:
         run_sweep(args.sweep, json.loads(args.variants))
+        return
+    if args.sched_eval:
+        import build_lib
+        build_lib.build_all()
+        run_sched_eval(args.sched_eval)
         return
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_setup()

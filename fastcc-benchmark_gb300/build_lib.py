@@ -22,7 +22,7 @@ INCLUDE = os.path.join(ROOT, "include")
 GPU_LIB = os.path.join(BUILD, "libfastcc_gpu.so")
 SYNTH_LIB = os.path.join(BUILD, "libfastcc_synth.so")
 
-CU_SOURCES = ["fcc_prims.cu", "fcc_contract.cu", "fcc_api.cu", "fcc_noalloc.cu", "fcc_diag.cu", "fcc_batch.cu"]
+CU_SOURCES = ["fcc_prims.cu", "fcc_contract.cu", "fcc_api.cu", "fcc_noalloc.cu", "fcc_diag.cu", "fcc_batch.cu", "fcc_sched.cu"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -32,6 +32,7 @@ fcc::Runtime runtime_of(fcc_ctx *ctx) {
   rt.ev = ctx->ev;
   rt.phase_ms = ctx->phase_ms;
   rt.pool = ctx->pool;
+  rt.sched = &ctx->sched;
   return rt;
 }
 
@@ -60,6 +61,8 @@ void set_thread_error(const std::string &msg) { g_last_error = msg; }
 }  // namespace fcc
 
 extern "C" {
+
+static_assert(sizeof(fcc_options) == 80, "fcc_options layout is part of the ABI");
 
 int fcc_abi_version(void) { return FCC_ABI_VERSION; }
 
@@ -146,6 +149,7 @@ int fcc_ctx_destroy(fcc_ctx *ctx) {
   for (auto &e : ctx->ev)
     if (e) cudaEventDestroy(e);
   if (ctx->d_err) cudaFree(ctx->d_err);
+  if (ctx->sched.model) cudaFree(ctx->sched.model);
   if (ctx->h_scalars) cudaFreeHost(ctx->h_scalars);
   if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -190,6 +194,129 @@ int fcc_contract_batch(fcc_ctx *ctx, int32_t n, const fcc_tensor *A, const fcc_t
     r->ctx = ctx;
     fcc::contract_batch(&rt, n, A, B, ctrA, ctrB, k, o, r.get(), counts);
     *out = r.release();
+  });
+}
+
+}  // extern "C"
+
+namespace {
+
+// Shape signature of a problem for the autotuner's cache: orders, contracted
+// modes, and log2 buckets of the nonzero counts and mode extents.
+std::string tune_signature(int n, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                           const int32_t *ctrB, int32_t k) {
+  auto lg = [](int64_t v) { int b = 0; while (v > 1) { v >>= 1; b++; } return b; };
+  std::string s = "n" + std::to_string(n) + ":";
+  for (int side = 0; side < 2; side++) {
+    const fcc_tensor *T = side ? B : A;
+    int64_t nnz = 0;
+    std::vector<int32_t> mx(size_t(std::max(T[0].order, 0)), 0);
+    for (int t = 0; t < n; t++) {
+      nnz += T[t].nnz;
+      for (int m = 0; m < T[0].order && T[t].max_index; m++) mx[size_t(m)] = std::max(mx[size_t(m)], T[t].max_index[m]);
+    }
+    s += "o" + std::to_string(T[0].order) + "z" + std::to_string(lg(nnz));
+    for (int32_t v : mx) s += "e" + std::to_string(lg(int64_t(v) + 1));
+    s += "|";
+  }
+  for (int i = 0; i < k; i++) s += std::to_string(ctrA[i]) + "-" + std::to_string(ctrB[i]) + ",";
+  return s;
+}
+
+// Times each candidate schedule with `run` (a full contraction with
+// opts.timing = 1) and keeps the fastest.
+template <class Run>
+void autotune(fcc_ctx *ctx, const std::string &sig, const fcc_options &base, int reps, Run &&run,
+              fcc_options *best, double *best_ms) {
+  auto hit = ctx->tuned.find(sig);
+  if (hit != ctx->tuned.end()) {
+    *best = hit->second.first;
+    if (best_ms) *best_ms = hit->second.second;
+    return;
+  }
+  std::vector<fcc_options> cand;
+  auto add = [&](int schedule, int threads, int fill) {
+    fcc_options o = base;
+    o.accumulator = FCC_ACC_AUTO;
+    o.hash_slots = 0;
+    o.schedule = schedule;
+    o.tile_threads = threads;
+    o.dense_fill_log2 = fill;
+    cand.push_back(o);
+  };
+  for (int threads : {512, 1024}) {
+    add(FCC_SCHED_RULE, threads, 0);
+    add(FCC_SCHED_RULE, threads, 6);
+    add(FCC_SCHED_FORCE + FCC_CLASS_DENSE, threads, 0);
+  }
+  for (int c = FCC_CLASS_HASH_L; c < FCC_NUM_CLASSES; c++) add(FCC_SCHED_FORCE + c, 0, 0);
+  double best_t = 1e300;
+  fcc_options best_o = base;
+  for (fcc_options o : cand) {
+    o.timing = 1;
+    double t = 0;
+    bool ok = true;
+    for (int r = 0; r <= reps && ok; r++) {  // the first run warms up
+      try {
+        run(o);
+      } catch (const fcc::Error &e) {
+        // a class this problem cannot use, or whose split buffers do not fit
+        if (e.status != FCC_ERR_ARG && e.status != FCC_ERR_OOM) throw;
+        ok = false;
+        break;
+      }
+      if (r > 0) t += ctx->phase_ms[FCC_PHASE_TOTAL];
+    }
+    if (!ok) continue;
+    t /= std::max(reps, 1);
+    if (t < best_t) {
+      best_t = t;
+      best_o = o;
+    }
+  }
+  if (best_t == 1e300) throw fcc::Error{FCC_ERR_ARG, "no schedule can run this problem"};
+  best_o.timing = base.timing;
+  ctx->tuned[sig] = {best_o, best_t};
+  *best = best_o;
+  if (best_ms) *best_ms = best_t;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fcc_autotune(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA, const int32_t *ctrB,
+                 int32_t k, const fcc_options *base, int32_t reps, fcc_options *best, double *best_ms) {
+  if (!ctx || !A || !B || !best || k < 0 || (k > 0 && (!ctrA || !ctrB))) return FCC_ERR_ARG;
+  fcc_options o;
+  if (base) o = *base; else fcc_options_default(&o);
+  return guarded(ctx, [&] {
+    const std::string sig = tune_signature(1, A, B, ctrA, ctrB, k);
+    autotune(ctx, sig, o, std::max(reps, 1), [&](const fcc_options &c) {
+      fcc::Runtime rt = runtime_of(ctx);
+      std::unique_ptr<fcc_result> r(new fcc_result());
+      r->ctx = ctx;
+      fcc::contract(&rt, A, B, ctrA, ctrB, k, c, r.get(), nullptr, false, nullptr, 0);
+      fcc_result_free(r.release());
+    }, best, best_ms);
+  });
+}
+
+int fcc_autotune_batch(fcc_ctx *ctx, int32_t n, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                       const int32_t *ctrB, int32_t k, const fcc_options *base, int32_t reps, fcc_options *best,
+                       double *best_ms) {
+  if (!ctx || n < 1 || !A || !B || !best || k < 0 || (k > 0 && (!ctrA || !ctrB))) return FCC_ERR_ARG;
+  fcc_options o;
+  if (base) o = *base; else fcc_options_default(&o);
+  return guarded(ctx, [&] {
+    const std::string sig = tune_signature(n, A, B, ctrA, ctrB, k);
+    autotune(ctx, sig, o, std::max(reps, 1), [&](const fcc_options &c) {
+      fcc::Runtime rt = runtime_of(ctx);
+      std::unique_ptr<fcc_result> r(new fcc_result());
+      r->ctx = ctx;
+      fcc::contract_batch(&rt, n, A, B, ctrA, ctrB, k, c, r.get(), nullptr);
+      fcc_result_free(r.release());
+    }, best, best_ms);
   });
 }
 

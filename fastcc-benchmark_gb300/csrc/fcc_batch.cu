@@ -107,10 +107,10 @@ void concat_operand(Runtime *ctx, int n, const fcc_tensor *T, int shift, int ins
   c.max_index[size_t(inst_last)] = n - 1;
   if (total == 0) return;
   void *p = nullptr;
-  FCC_CUDA(cudaMallocFromPoolAsync(&p, sizeof(int32_t) * size_t(total) * order_out, ctx->pool, st));
+  p = pool_alloc(ctx->pool, sizeof(int32_t) * size_t(total) * order_out, st);
   frees.push_back(p);
   c.coords = static_cast<int32_t *>(p);
-  FCC_CUDA(cudaMallocFromPoolAsync(&p, sizeof(double) * size_t(total), ctx->pool, st));
+  p = pool_alloc(ctx->pool, sizeof(double) * size_t(total), st);
   frees.push_back(p);
   c.values = static_cast<double *>(p);
   // host instances: coordinates staged in one pooled buffer, values copied
@@ -121,7 +121,7 @@ void concat_operand(Runtime *ctx, int n, const fcc_tensor *T, int shift, int ins
       host_elems += (T[t].nnz - 1) * T[t].stride_nnz + i64(order - 1) * T[t].stride_mode + 1;
   int32_t *stage = nullptr;
   if (host_elems > 0) {
-    FCC_CUDA(cudaMallocFromPoolAsync(&p, sizeof(int32_t) * size_t(host_elems), ctx->pool, st));
+    p = pool_alloc(ctx->pool, sizeof(int32_t) * size_t(host_elems), st);
     frees.push_back(p);
     stage = static_cast<int32_t *>(p);
   }
@@ -142,7 +142,7 @@ void concat_operand(Runtime *ctx, int n, const fcc_tensor *T, int shift, int ins
       so += ext;
     }
   }
-  FCC_CUDA(cudaMallocFromPoolAsync(&p, sizeof(PackSrc) * size_t(n), ctx->pool, st));
+  p = pool_alloc(ctx->pool, sizeof(PackSrc) * size_t(n), st);
   frees.push_back(p);
   PackSrc *dsrc = static_cast<PackSrc *>(p);
   FCC_CUDA(cudaMemcpyAsync(dsrc, src.data(), sizeof(PackSrc) * size_t(n), cudaMemcpyHostToDevice, st));
@@ -203,7 +203,7 @@ void contract_batch(Runtime *ctx, int n, const fcc_tensor *A, const fcc_tensor *
   if (counts) {
     unsigned long long *dc = nullptr;
     void *p = nullptr;
-    FCC_CUDA(cudaMallocFromPoolAsync(&p, sizeof(unsigned long long) * size_t(n), ctx->pool, ctx->stream));
+    p = pool_alloc(ctx->pool, sizeof(unsigned long long) * size_t(n), ctx->stream);
     frees.push_back(p);
     dc = static_cast<unsigned long long *>(p);
     FCC_CUDA(cudaMemsetAsync(dc, 0, sizeof(unsigned long long) * size_t(n), ctx->stream));

@@ -318,56 +318,136 @@ __global__ void k_tile_nrows(const u32 *__restrict__ ntiles_p, const u32 *__rest
     nrows[t] = rank[abeg[t + 1] - 1] - rank0[t] + 1;
 }
 
-// Per tile: work items, split flag, output bound and (hash) region size.
-__global__ void k_tile_items(const u32 *__restrict__ ntiles_p, i64 nmax, const u32 *__restrict__ abeg,
-                             const u64 *__restrict__ P, u64 pmax, const u32 *__restrict__ nrows,
-                             const u32 *__restrict__ lb, u64 LB, int hash_mode, u32 *__restrict__ nitems,
-                             u32 *__restrict__ split, u64 *__restrict__ cap, u64 *__restrict__ hsz) {
+// Tile classes (FCC_CLASS_*): per class whether it may run, its multiply-adds
+// per work item and whether it is a hash class.
+struct ClassTable {
+  u32 enabled[FCC_NUM_CLASSES];
+  u32 hash[FCC_NUM_CLASSES];
+  u64 pmax[FCC_NUM_CLASSES];
+  int forced;     // >= 0: every tile takes this class
+  int fill_log2;  // rule: dense only when multiply-adds >= area >> fill_log2 (0: whenever it fits)
+};
+
+__device__ __forceinline__ u64 tile_area(const u32 *nrows, const u32 *lb, u64 LB, u32 t) {
+  return u64(nrows[t]) * (lb ? u64(lb[t]) : LB);
+}
+
+// cls[t]: the class of tile t. Forced, or from the predicted costs (pred,
+// FCC_NUM_CLASSES per tile, lowest among the enabled classes wins; a tile
+// larger than a class's work item is split, as under a forced class), or the
+// rule: dense when enabled and filled enough, else the smallest hash table
+// holding the tile, else the largest. ckey/corder: sort keys for the
+// class-order permutation (padding tiles sort last).
+__global__ void k_tile_class(const u32 *__restrict__ ntiles_p, i64 nmax, const u32 *__restrict__ abeg,
+                             const u64 *__restrict__ P, const u32 *__restrict__ nrows, const u32 *__restrict__ lb,
+                             u64 LB, ClassTable ct, const float *__restrict__ pred, u32 *__restrict__ cls,
+                             u64 *__restrict__ ckey, u32 *__restrict__ corder) {
   const u32 ntiles = *ntiles_p;
   for (i64 t = i64(blockIdx.x) * blockDim.x + threadIdx.x; t < nmax; t += i64(gridDim.x) * blockDim.x) {
+    corder[t] = u32(t);
     if (t >= ntiles) {
-      nitems[t] = 0; split[t] = 0; cap[t] = 0; hsz[t] = 0;
+      ckey[t] = 7;
       continue;
     }
     const u64 prod = P[abeg[t + 1]] - P[abeg[t]];
-    const u64 items = (prod + pmax - 1) / pmax;
-    const u64 area = u64(nrows[t]) * (lb ? u64(lb[t]) : LB);  // rows x LB fits 64 bits (host check)
-    const u64 bound = prod < area ? prod : area;
-    nitems[t] = u32(items);
-    split[t] = items > 1 ? 1u : 0u;
-    cap[t] = bound;
-    u64 h = 0;
-    if (hash_mode && items > 1) {
-      h = 64;
-      while (h < 2 * bound) h <<= 1;
+    int c = ct.forced;
+    if (c < 0 && pred) {
+      float best = 3.4e38f;
+      for (int k = 0; k < FCC_NUM_CLASSES; k++) {
+        if (!ct.enabled[k]) continue;
+        const float v = pred[t * FCC_NUM_CLASSES + k];
+        if (v < best) { best = v; c = k; }
+      }
     }
-    hsz[t] = h;
+    if (c < 0) {
+      const u64 area = tile_area(nrows, lb, LB, u32(t));
+      if (ct.enabled[FCC_CLASS_DENSE] && (ct.fill_log2 == 0 || prod >= (area >> ct.fill_log2))) {
+        c = FCC_CLASS_DENSE;
+      } else {
+        c = FCC_CLASS_HASH_L;
+        for (int k = FCC_NUM_CLASSES - 1; k > FCC_CLASS_HASH_L; k--)
+          if (ct.enabled[k] && prod <= ct.pmax[k]) { c = k; break; }
+        if (!ct.enabled[c]) c = FCC_CLASS_DENSE;  // only dense is enabled
+      }
+    }
+    cls[t] = u32(c);
+    ckey[t] = u64(c);
   }
 }
 
-__global__ void k_item_write(const u32 *__restrict__ ntiles_p, const u32 *__restrict__ abeg,
-                             const u64 *__restrict__ P, const u32 *__restrict__ item_off, u64 pmax,
-                             Item *__restrict__ items, const u32 *__restrict__ split,
-                             const u32 *__restrict__ split_idx, int *__restrict__ split_of_tile,
-                             u32 *__restrict__ split_tiles) {
+// Per tile in class order (position i, tile corder[i]): work items, split
+// flags (dense / hash), output bound and (split hash tiles) global region size.
+__global__ void k_tile_items(const u32 *__restrict__ ntiles_p, i64 nmax, const u32 *__restrict__ corder,
+                             const u32 *__restrict__ cls, const u32 *__restrict__ abeg, const u64 *__restrict__ P,
+                             const u32 *__restrict__ nrows, const u32 *__restrict__ lb, u64 LB, ClassTable ct,
+                             u32 *__restrict__ nitems, u32 *__restrict__ split_d, u32 *__restrict__ split_h,
+                             u64 *__restrict__ cap, u64 *__restrict__ hsz) {
   const u32 ntiles = *ntiles_p;
-  for (i64 t = i64(blockIdx.x) * blockDim.x + threadIdx.x; t < ntiles; t += i64(gridDim.x) * blockDim.x) {
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < nmax; i += i64(gridDim.x) * blockDim.x) {
+    if (i >= ntiles) {
+      nitems[i] = 0; split_d[i] = 0; split_h[i] = 0; cap[i] = 0; hsz[i] = 0;
+      continue;
+    }
+    const u32 t = corder[i], c = cls[t];
+    const u64 prod = P[abeg[t + 1]] - P[abeg[t]];
+    const u64 items = (prod + ct.pmax[c] - 1) / ct.pmax[c];
+    const u64 area = tile_area(nrows, lb, LB, t);  // rows x LB fits 64 bits (host check)
+    const u64 bound = prod < area ? prod : area;
+    nitems[i] = u32(items);
+    split_d[i] = (!ct.hash[c] && items > 1) ? 1u : 0u;
+    split_h[i] = (ct.hash[c] && items > 1) ? 1u : 0u;
+    cap[i] = bound;
+    u64 h = 0;
+    if (ct.hash[c] && items > 1) {
+      h = 64;
+      while (h < 2 * bound) h <<= 1;
+    }
+    hsz[i] = h;
+  }
+}
+
+// First item of each class (ckey sorted by class; out[c] stays ~0 for a class
+// without tiles).
+__global__ void k_class_bounds(const u32 *__restrict__ ntiles_p, const u64 *__restrict__ ckey,
+                               const u32 *__restrict__ item_off, u64 *__restrict__ out) {
+  const u32 ntiles = *ntiles_p;
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < ntiles; i += i64(gridDim.x) * blockDim.x)
+    if (i == 0 || ckey[i] != ckey[i - 1]) out[ckey[i]] = item_off[i];
+}
+
+__global__ void k_item_write(const u32 *__restrict__ ntiles_p, const u32 *__restrict__ corder,
+                             const u32 *__restrict__ cls, const u32 *__restrict__ abeg, const u64 *__restrict__ P,
+                             const u32 *__restrict__ item_off, ClassTable ct, Item *__restrict__ items,
+                             const u32 *__restrict__ split_d, const u32 *__restrict__ split_h,
+                             const u32 *__restrict__ split_d_idx, const u32 *__restrict__ split_h_idx,
+                             int *__restrict__ split_of_tile, u32 *__restrict__ split_tiles_d,
+                             u32 *__restrict__ split_tiles_h, const u64 *__restrict__ hoff_i,
+                             const u64 *__restrict__ hsz_i, u64 *__restrict__ hoff_t, u64 *__restrict__ hsz_t) {
+  const u32 ntiles = *ntiles_p;
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < ntiles; i += i64(gridDim.x) * blockDim.x) {
+    const u32 t = corder[i];
+    const u64 pmax = ct.pmax[cls[t]];
     const u64 b = P[abeg[t]], e = P[abeg[t + 1]];
-    u32 o = item_off[t];
+    u32 o = item_off[i];
     for (u64 p = b; p < e; p += pmax) {
       Item it;
       it.p0 = p;
       it.p1 = (e - p > pmax) ? p + pmax : e;
-      it.tile = u32(t);
+      it.tile = t;
       it.pad = 0;
       items[o++] = it;
     }
-    if (split[t]) {
-      split_of_tile[t] = int(split_idx[t]);
-      split_tiles[split_idx[t]] = u32(t);
-    } else {
-      split_of_tile[t] = -1;
+    split_of_tile[t] = -1;
+    if (split_d[i]) {
+      split_of_tile[t] = int(split_d_idx[i]);
+      split_tiles_d[split_d_idx[i]] = t;
     }
+    if (split_h[i]) {
+      split_of_tile[t] = int(split_h_idx[i]);
+      split_tiles_h[split_h_idx[i]] = t;
+    }
+    hoff_t[t] = hoff_i[i];
+    hsz_t[t] = hsz_i[i];
   }
 }
 
@@ -721,6 +801,7 @@ struct DenseArgs {
   Out out;
   Decode dec;
   u32 *err;
+  u64 *item_cyc;  // per item: SM cycles from fetch to drained (NULL: not recorded)
 };
 
 // The touched mask of positions [32w, 32w+32) of a dense tile, in every lane.
@@ -929,6 +1010,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
     for (u32 i = tid; i < nwarps * (a.hot / 32); i += blockDim.x) pmask[i] = 0u;
   DenseAdd<kSentinel> add{acc, mask, priv + size_t(warp) * a.hot, pmask + size_t(warp) * (a.hot / 32), a.hot};
   for (;;) {
+    const long long c0 = clock64();
     if (tid == 0) s_item = atomicAdd(a.counter, 1u);
     __syncthreads();
     const u32 it = s_item;
@@ -950,6 +1032,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
     else
       flush_dense<kSentinel>(acc, mask, used, a.gacc + u64(sidx) * a.area, a.gmask + u64(sidx) * a.words);
     __syncthreads();
+    if (a.item_cyc && tid == 0) a.item_cyc[it] = u64(clock64() - c0);
   }
 }
 
@@ -994,6 +1077,7 @@ struct HashArgs {
   Out out;
   Decode dec;
   u32 *err;
+  u64 *item_cyc;  // per item: SM cycles from fetch to drained (NULL: not recorded)
 };
 
 // Emits occupied slots of an open-addressing table, coalesced per warp, and
@@ -1095,8 +1179,10 @@ struct HashAdd {
   }
 };
 
+// kThreads 256 runs four CTAs per SM (small tables): independent items
+// overlap their barriers and memory latency.
 template <class ColT, int kThreads>
-__global__ void __launch_bounds__(kThreads, 1) k_contract_hash(HashArgs<ColT> a) {
+__global__ void __launch_bounds__(kThreads, kThreads == 256 ? 4 : 1) k_contract_hash(HashArgs<ColT> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   // layout: hk[slots] | hv[slots] | priv[nwarps*hot] | pmask[nwarps*hot/32]
   u64 *hk = reinterpret_cast<u64 *>(smem);
@@ -1113,6 +1199,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_hash(HashArgs<ColT> a)
   for (u32 i = tid; i < nwarps * a.hot; i += blockDim.x) priv[i] = 0.0;
   for (u32 i = tid; i < nwarps * pw; i += blockDim.x) pmask[i] = 0u;
   for (;;) {
+    const long long c0 = clock64();
     if (tid == 0) {
       s_item = atomicAdd(a.counter, 1u);
       s_chunk = 0;
@@ -1160,6 +1247,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_hash(HashArgs<ColT> a)
       }
     }
     __syncthreads();
+    if (a.item_cyc && tid == 0) a.item_cyc[it] = u64(clock64() - c0);
   }
 }
 
@@ -1180,6 +1268,14 @@ __global__ void __launch_bounds__(kTileThreads) k_merge_hash(HashArgs<ColT> a) {
 // ------------------------------------------------------- host pipeline ----
 
 namespace {
+
+struct HostClass {
+  bool hash;
+  int threads;
+  u32 slots;  // hash table slots
+  u64 pmax;   // multiply-adds per work item
+  bool enabled;
+};
 
 struct Side {
   int order = 0;
@@ -1271,7 +1367,8 @@ const double *upload_values(Runtime *ctx, const fcc_tensor *t) {
 
 // Device scalar block: slot numbers in a u64 array.
 enum Scalar { S_NSEG = 0, S_NA2, S_NTILES, S_NITEMS, S_NSPLIT, S_CAP, S_HASH, S_CURSOR, S_COUNTER, S_NROWS,
-              S_PTOTAL, S_ERR, S_TINY, S_HOT, S_COUNT };
+              S_PTOTAL, S_ERR, S_TINY, S_HOT, S_NSPLIT_H, S_CLS0, S_CLS_END = S_CLS0 + FCC_NUM_CLASSES, S_COUNT };
+static_assert(S_COUNT <= 32, "the pinned scalar block holds 32 entries");
 
 // Copies the scalar block and the error word to pinned host memory, waits,
 // and raises the error bits that are not recoverable.
@@ -1287,10 +1384,11 @@ void read_scalars(Runtime *ctx, u64 *d_sc) {
 
 u32 scalar32(Runtime *ctx, int s) { return u32(ctx->h_scalars[s] & 0xFFFFFFFFu); }
 
-int grid_tiles(Runtime *ctx, const void *kernel, int threads, size_t smem, u32 nitems) {
+int grid_tiles(Runtime *ctx, const void *kernel, int threads, size_t smem, u32 nitems, int *ctas_per_sm) {
   int per_sm = 0;
   FCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
   if (per_sm < 1) throw Error{FCC_ERR_CUDA, "tile kernel does not fit on an SM"};
+  *ctas_per_sm = per_sm;
   i64 g = i64(per_sm) * ctx->num_sms;
   if (g > i64(nitems)) g = nitems;
   return int(std::max<i64>(g, 1));
@@ -1476,15 +1574,55 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     throw Error{FCC_ERR_ARG, "rows_per_tile x B external span exceeds the dense tile capacity"};
   if (!dense && (unsigned __int128)TL * LB > (unsigned __int128)(~0ull) - 1)
     throw Error{FCC_ERR_OVERFLOW, "rows_per_tile x B external span exceeds 64 bits"};
-  u32 hslots = 0;
-  if (!dense) {
-    hslots = opt.hash_slots > 0 ? u32(opt.hash_slots) : 8192u;
-    if (hslots & (hslots - 1)) throw Error{FCC_ERR_ARG, "hash_slots must be a power of two"};
-    if (size_t(hslots) * 16 > smem_cap || hslots < 64) throw Error{FCC_ERR_ARG, "hash_slots out of range"};
+  // ---- tile classes ----
+  // Every output tile runs in one class: the shared-memory dense tile, or an
+  // open-addressing hash table of 8192 slots (512 threads, one CTA per SM),
+  // 4096 or 2048 slots (256 threads, several CTAs per SM, so that small tiles
+  // overlap their barriers and memory latency). The schedule picks a class
+  // per tile; the items of one class run in one persistent launch.
+  const bool custom_hash = opt.hash_slots > 0 || (opt.tile_threads > 0 && opt.accumulator == FCC_ACC_HASH);
+  HostClass hc[FCC_NUM_CLASSES];
+  hc[FCC_CLASS_DENSE] = {false, opt.tile_threads > 0 ? opt.tile_threads : kTileThreads, 0u, 0, dense};
+  hc[FCC_CLASS_HASH_L] = {true, opt.tile_threads > 0 ? opt.tile_threads : 512,
+                          opt.hash_slots > 0 ? u32(opt.hash_slots) : 8192u, 0, opt.accumulator != FCC_ACC_DENSE};
+  hc[FCC_CLASS_HASH_M] = {true, 256, 4096u, 0, opt.accumulator != FCC_ACC_DENSE && !custom_hash};
+  hc[FCC_CLASS_HASH_S] = {true, 256, 2048u, 0, opt.accumulator != FCC_ACC_DENSE && !custom_hash};
+  if (opt.accumulator == FCC_ACC_HASH) hc[FCC_CLASS_DENSE].enabled = false;
+  if (hc[FCC_CLASS_DENSE].threads != 512 && hc[FCC_CLASS_DENSE].threads != 1024) {
+    if (opt.accumulator != FCC_ACC_HASH && hc[FCC_CLASS_DENSE].threads != 256)
+      throw Error{FCC_ERR_ARG, "tile_threads must be 256, 512 or 1024"};
+    if (opt.accumulator == FCC_ACC_DENSE) throw Error{FCC_ERR_ARG, "tile_threads 256 is for the hash accumulator"};
+    hc[FCC_CLASS_DENSE].enabled = false;
+    hc[FCC_CLASS_DENSE].threads = kTileThreads;
   }
-  u64 pmax = opt.products_per_item > 0 ? u64(opt.products_per_item) : (dense ? (u64(1) << 20) : u64(hslots / 2));
-  if (!dense && pmax > hslots / 2) pmax = hslots / 2;
-  if (dense && pmax > u64(kListMax) * kCtaRun) pmax = u64(kListMax) * kCtaRun;
+  {
+    const int t = hc[FCC_CLASS_HASH_L].threads;
+    if (t != 256 && t != 512 && t != 1024) throw Error{FCC_ERR_ARG, "tile_threads must be 256, 512 or 1024"};
+    const u32 hs = hc[FCC_CLASS_HASH_L].slots;
+    if (hs & (hs - 1)) throw Error{FCC_ERR_ARG, "hash_slots must be a power of two"};
+    if (size_t(hs) * 16 > smem_cap || hs < 64) throw Error{FCC_ERR_ARG, "hash_slots out of range"};
+  }
+  {
+    u64 pd = opt.products_per_item > 0 ? u64(opt.products_per_item) : (u64(1) << 20);
+    hc[FCC_CLASS_DENSE].pmax = std::min<u64>(pd, u64(kListMax) * kCtaRun);
+    for (int c = FCC_CLASS_HASH_L; c < FCC_NUM_CLASSES; c++) {
+      const u64 cap = hc[c].slots / 2;
+      hc[c].pmax = opt.products_per_item > 0 ? std::min<u64>(u64(opt.products_per_item), cap) : cap;
+    }
+  }
+  int forced = -1;
+  if (opt.accumulator == FCC_ACC_DENSE) forced = FCC_CLASS_DENSE;
+  else if (opt.accumulator == FCC_ACC_AUTO && opt.schedule >= FCC_SCHED_FORCE) forced = opt.schedule - FCC_SCHED_FORCE;
+  if (opt.schedule < 0 || opt.schedule >= FCC_SCHED_FORCE + FCC_NUM_CLASSES)
+    throw Error{FCC_ERR_ARG, "bad schedule"};
+  if (forced >= 0 && !hc[forced].enabled)
+    throw Error{FCC_ERR_ARG, forced == FCC_CLASS_DENSE
+                                 ? "dense accumulator: B external span exceeds the shared-memory tile"
+                                 : "the forced hash class is disabled by hash_slots or tile_threads"};
+  if (custom_hash && forced < 0 && opt.accumulator == FCC_ACC_HASH) forced = FCC_CLASS_HASH_L;
+  if (opt.dense_fill_log2 < 0 || opt.dense_fill_log2 > 40) throw Error{FCC_ERR_ARG, "dense_fill_log2 out of range"};
+  const bool learned = forced < 0 && opt.schedule == FCC_SCHED_LEARNED && ctx->sched && ctx->sched->model;
+  const bool want_record = opt.timing == 2 && ctx->sched;
   // Row groups (batched contractions): dense tiles hold rows of one group,
   // group_tl rows of the group's own column span each.
   const bool grouped = dense && group_lb && ngroups > 0;
@@ -1498,8 +1636,6 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       area = std::max(area, tl * lb);
     }
   }
-  const int threads = opt.tile_threads > 0 ? opt.tile_threads : kTileThreads;
-  if (threads != 512 && threads != 1024) throw Error{FCC_ERR_ARG, "tile_threads must be 512 or 1024"};
   if (opt.hot_columns < -1 || (opt.hot_columns > 0 && opt.hot_columns % 32))
     throw Error{FCC_ERR_ARG, "hot_columns must be -1, 0 or a positive multiple of 32"};
 
@@ -1557,43 +1693,92 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   FCC_LAUNCH_CHECK();
   k_tile_nrows<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), tile_abeg, rank, tile_rank0, tile_nrows);
   FCC_LAUNCH_CHECK();
-  u32 *t_items = ar.get_n<u32>(nA2), *t_split = ar.get_n<u32>(nA2);
-  u64 *t_cap = ar.get_n<u64>(nA2), *t_hsz = ar.get_n<u64>(nA2);
-  k_tile_items<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), nA2, tile_abeg, P, pmax, tile_nrows,
-                                                   dense ? tile_lb : nullptr, LB, dense ? 0 : 1, t_items, t_split,
-                                                   t_cap, t_hsz);
+
+  // ---- class per tile ----
+  ClassTable ctab{};
+  for (int c = 0; c < FCC_NUM_CLASSES; c++) {
+    ctab.enabled[c] = hc[c].enabled ? 1u : 0u;
+    ctab.pmax[c] = hc[c].pmax;
+    ctab.hash[c] = hc[c].hash ? 1u : 0u;
+  }
+  ctab.forced = forced;
+  ctab.fill_log2 = opt.dense_fill_log2;
+  const u32 *lb_or_null = dense ? tile_lb : nullptr;
+  float *feat = nullptr, *pred = nullptr;
+  if (learned || want_record) {
+    feat = ar.get_n<float>(size_t(nA2) * FCC_SCHED_FEATURES);
+    tile_features(st, sc32(S_NTILES), u32(nA2), tile_abeg, P, tile_nrows, lb_or_null, LB, feat);
+  }
+  if (learned) {
+    pred = ar.get_n<float>(size_t(nA2) * FCC_NUM_CLASSES);
+    predict_costs(st, sc32(S_NTILES), u32(nA2), feat, ctx->sched->model, pred);
+  }
+  u32 *cls = ar.get_n<u32>(nA2);
+  u64 *ckey = ar.get_n<u64>(nA2);
+  u32 *corder = ar.get_n<u32>(nA2);
+  k_tile_class<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), nA2, tile_abeg, P, tile_nrows, lb_or_null, LB,
+                                                   ctab, pred, cls, ckey, corder);
   FCC_LAUNCH_CHECK();
-  u32 *item_off = ar.get_n<u32>(nA2), *split_idx = ar.get_n<u32>(nA2);
+  // tiles in class order (stable), so that each class's items are contiguous
+  radix_sort_pairs(ckey, corder, nA2, 3, ar, st);
+
+  u32 *t_items = ar.get_n<u32>(nA2), *t_split_d = ar.get_n<u32>(nA2), *t_split_h = ar.get_n<u32>(nA2);
+  u64 *t_cap = ar.get_n<u64>(nA2), *t_hsz = ar.get_n<u64>(nA2);
+  k_tile_items<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), nA2, corder, cls, tile_abeg, P, tile_nrows,
+                                                   lb_or_null, LB, ctab, t_items, t_split_d, t_split_h, t_cap, t_hsz);
+  FCC_LAUNCH_CHECK();
+  u32 *item_off = ar.get_n<u32>(nA2), *split_d_idx = ar.get_n<u32>(nA2), *split_h_idx = ar.get_n<u32>(nA2);
   u64 *t_hoff = ar.get_n<u64>(nA2);
   scan_exclusive(t_items, item_off, nA2, sc32(S_NITEMS), ar, st);
-  scan_exclusive(t_split, split_idx, nA2, sc32(S_NSPLIT), ar, st);
+  scan_exclusive(t_split_d, split_d_idx, nA2, sc32(S_NSPLIT), ar, st);
+  scan_exclusive(t_split_h, split_h_idx, nA2, sc32(S_NSPLIT_H), ar, st);
   scan_exclusive(t_cap, t_cap, nA2, d_sc + S_CAP, ar, st);
   scan_exclusive(t_hsz, t_hoff, nA2, d_sc + S_HASH, ar, st);
+  FCC_CUDA(cudaMemsetAsync(d_sc + S_CLS0, 0xFF, sizeof(u64) * FCC_NUM_CLASSES, st));  // ~0: class unused
+  k_class_bounds<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), ckey, item_off, d_sc + S_CLS0);
+  FCC_LAUNCH_CHECK();
   read_scalars(ctx, d_sc);
   const u32 nitems = scalar32(ctx, S_NITEMS);
-  const u32 nsplit = scalar32(ctx, S_NSPLIT);
+  const u32 nsplit_d = scalar32(ctx, S_NSPLIT);
+  const u32 nsplit_h = scalar32(ctx, S_NSPLIT_H);
   const u64 cap_total = ctx->h_scalars[S_CAP];
   const u64 hash_total = ctx->h_scalars[S_HASH];
+  u32 cbeg[FCC_NUM_CLASSES + 1], ccount[FCC_NUM_CLASSES];
+  {
+    u32 next = nitems;
+    for (int c = FCC_NUM_CLASSES - 1; c >= 0; c--) {
+      const u64 b = ctx->h_scalars[S_CLS0 + c];
+      if (b == ~0ull) { cbeg[c] = next; ccount[c] = 0; continue; }
+      cbeg[c] = u32(b);
+      ccount[c] = next - u32(b);
+      next = u32(b);
+    }
+  }
 
-  Item *items = ar.get_n<Item>(nitems);
+  Item *items = ar.get_n<Item>(std::max<u32>(nitems, 1));
   int *split_of_tile = ar.get_n<int>(nA2);
-  u32 *split_tiles = ar.get_n<u32>(std::max<u32>(nsplit, 1));
-  k_item_write<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), tile_abeg, P, item_off, pmax, items, t_split,
-                                                   split_idx, split_of_tile, split_tiles);
+  u32 *split_tiles_d = ar.get_n<u32>(std::max<u32>(nsplit_d, 1));
+  u32 *split_tiles_h = ar.get_n<u32>(std::max<u32>(nsplit_h, 1));
+  u64 *hoff_t = ar.get_n<u64>(nA2), *hsz_t = ar.get_n<u64>(nA2);
+  k_item_write<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), corder, cls, tile_abeg, P, item_off, ctab, items,
+                                                   t_split_d, t_split_h, split_d_idx, split_h_idx, split_of_tile,
+                                                   split_tiles_d, split_tiles_h, t_hoff, t_hsz, hoff_t, hsz_t);
   FCC_LAUNCH_CHECK();
   const u64 words = dense ? (area + 31) / 32 : 0;
   double *gacc = nullptr;
   u32 *gmask = nullptr;
   u64 *gkeys = nullptr;
   double *gvals = nullptr;
-  if (dense && nsplit > 0) {
-    gacc = ar.get_n<double>(size_t(nsplit) * area);
-    gmask = ar.get_n<u32>(size_t(nsplit) * words);
+  if (nsplit_d > 0) {
+    gacc = ar.get_n<double>(size_t(nsplit_d) * area);
+    gmask = ar.get_n<u32>(size_t(nsplit_d) * words);
   }
-  if (!dense && nsplit > 0) {
+  if (nsplit_h > 0) {
     gkeys = ar.get_n<u64>(hash_total);
     gvals = ar.get_n<double>(hash_total);
   }
+  u64 *item_cyc = want_record ? ar.get_n<u64>(std::max<u32>(nitems, 1)) : nullptr;
+  u32 *counters = ar.get_n<u32>(FCC_NUM_CLASSES);
   tm.mark(3);
 
   // ---- contract + drain ----
@@ -1603,20 +1788,24 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   // make a product round to -0.0.
   const bool tiny = (ctx->h_scalars[S_TINY] & 1) != 0;
   const u32 ntiles = scalar32(ctx, S_NTILES);
-  bool sentinel = dense && !tiny && opt.dense_mode != FCC_DENSE_BITMASK &&
-                  (opt.dense_mode == FCC_DENSE_SENTINEL || ptotal >= u64(ntiles) * area / 4);
+  const bool sentinel = dense && !tiny && opt.dense_mode != FCC_DENSE_BITMASK &&
+                        (opt.dense_mode == FCC_DENSE_SENTINEL || ptotal >= u64(ntiles) * area / 4);
+  auto class_smem = [&](int c, u32 hot_n) -> size_t {
+    const size_t nw = size_t(hc[c].threads / 32);
+    const size_t base = hc[c].hash ? size_t(hc[c].slots) * 16
+                                   : ((size_t(area) * 8 + (sentinel ? 0 : size_t(words) * 4) + 15) & ~size_t(15));
+    return base + nw * hot_n * 8 + nw * (hot_n / 32) * 4;
+  };
   // Per-warp hot columns on request (hot_columns > 0) when the private copies
-  // fit next to the tile. Not automatic: measured on the 10M-nonzero Zipf(1.2)
-  // benchmark tensor they cost more than the contention they remove, because
-  // its heavy segments spread over all columns.
+  // fit next to every tile class in use. Not automatic: measured on the
+  // 10M-nonzero Zipf(1.2) benchmark tensor they cost more than the contention
+  // they remove, because its heavy segments spread over all columns.
   u32 hot = 0;
-  const u32 nwarps = u32(threads / 32);
-  if (hot_try) {
-    const bool want = opt.hot_columns > 0;
-    const size_t base_smem = dense ? ((size_t(area) * 8 + (sentinel ? 0 : size_t(words) * 4) + 15) & ~size_t(15))
-                                   : size_t(hslots) * 16;
-    const size_t priv = size_t(nwarps) * hot_want * 8 + size_t(nwarps) * (hot_want / 32) * 4;
-    if (want && base_smem + priv <= (dense ? dense_dyn_cap : smem_cap)) {
+  if (hot_try && opt.hot_columns > 0) {
+    bool fits = true;
+    for (int c = 0; c < FCC_NUM_CLASSES; c++)
+      if (ccount[c] && class_smem(c, hot_want) > (hc[c].hash ? smem_cap : dense_dyn_cap)) fits = false;
+    if (fits) {
       hot = hot_want;
       if (colb32) k_apply_colmap<u32><<<grid_for(nB, 256), 256, 0, st>>>(static_cast<u32 *>(colB), nB, colmap);
       else k_apply_colmap<u64><<<grid_for(nB, 256), 256, 0, st>>>(static_cast<u64 *>(colB), nB, colmap);
@@ -1642,14 +1831,13 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   u64 cap = std::max<u64>(std::min(cap_total, budget), 1);
   if (opt.capacity_hint > 0) cap = std::min<u64>(cap, u64(opt.capacity_hint));
 
+  int ctas_per_sm[FCC_NUM_CLASSES] = {};
   if (!ctx->pool) cap = ctx->out_cap;  // caller buffers: their capacity, no retry
   for (int attempt = 0;; attempt++) {
     i64 stride = i64(cap);
     if (ctx->pool) {
-      FCC_CUDA(cudaMallocFromPoolAsync(reinterpret_cast<void **>(&res->d_vals), sizeof(double) * cap, ctx->pool, st));
-      if (out_order > 0)
-        FCC_CUDA(cudaMallocFromPoolAsync(reinterpret_cast<void **>(&res->d_coords),
-                                         sizeof(u32) * cap * out_order, ctx->pool, st));
+      res->d_vals = static_cast<double *>(pool_alloc(ctx->pool, sizeof(double) * cap, st));
+      if (out_order > 0) res->d_coords = static_cast<u32 *>(pool_alloc(ctx->pool, sizeof(u32) * cap * out_order, st));
     } else {
       res->d_vals = ctx->out_vals;
       res->d_coords = ctx->out_coords;
@@ -1657,66 +1845,77 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     }
     res->cap = stride;
     Out o{res->d_coords, stride, res->d_vals, cap, d_sc + S_CURSOR};
-    FCC_CUDA(cudaMemsetAsync(d_sc + S_CURSOR, 0, sizeof(u64) * 2, st));  // cursor + item counter
+    FCC_CUDA(cudaMemsetAsync(d_sc + S_CURSOR, 0, sizeof(u64), st));
+    FCC_CUDA(cudaMemsetAsync(counters, 0, sizeof(u32) * FCC_NUM_CLASSES, st));
     FCC_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(u32), st));
-    u32 *counter = sc32(S_COUNTER);
-    if (dense) {
-      if (nsplit > 0) {
-        FCC_CUDA(cudaMemsetAsync(gacc, 0, sizeof(double) * nsplit * area, st));
-        FCC_CUDA(cudaMemsetAsync(gmask, 0, sizeof(u32) * nsplit * words, st));
-      }
-      DenseArgs a{items, nitems, counter, tile_abeg, tile_rank0, tile_lb, tile_nrows, urow, split_of_tile,
-                  split_tiles, nsplit, src, static_cast<const u32 *>(colB), u32(area), u32(words), hot, gacc, gmask,
-                  o, dec, ctx->d_err};
-      const size_t smem = ((size_t(area) * 8 + (sentinel ? 0 : size_t(words) * 4) + 15) & ~size_t(15)) +
-                          size_t(nwarps) * hot * 8 + size_t(nwarps) * (hot / 32) * 4;
+    if (nsplit_d > 0) {
+      FCC_CUDA(cudaMemsetAsync(gacc, 0, sizeof(double) * nsplit_d * area, st));
+      FCC_CUDA(cudaMemsetAsync(gmask, 0, sizeof(u32) * nsplit_d * words, st));
+    }
+    if (nsplit_h > 0) {
+      FCC_CUDA(cudaMemsetAsync(gkeys, 0xFF, sizeof(u64) * hash_total, st));
+      FCC_CUDA(cudaMemsetAsync(gvals, 0, sizeof(double) * hash_total, st));
+    }
+    DenseArgs da{items + cbeg[FCC_CLASS_DENSE], ccount[FCC_CLASS_DENSE], counters + FCC_CLASS_DENSE, tile_abeg,
+                 tile_rank0, tile_lb, tile_nrows, urow, split_of_tile, split_tiles_d, nsplit_d, src,
+                 static_cast<const u32 *>(colB), u32(area), u32(words), hot, gacc, gmask, o, dec, ctx->d_err,
+                 item_cyc ? item_cyc + cbeg[FCC_CLASS_DENSE] : nullptr};
+    if (ccount[FCC_CLASS_DENSE]) {
+      const int threads = hc[FCC_CLASS_DENSE].threads;
+      const size_t smem = class_smem(FCC_CLASS_DENSE, hot);
       const void *kern;
       if (threads == 512) kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true, 512>)
                                           : reinterpret_cast<const void *>(k_contract_dense<false, 512>);
       else kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true, 1024>)
                            : reinterpret_cast<const void *>(k_contract_dense<false, 1024>);
       FCC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-      const int grid = grid_tiles(ctx, kern, threads, smem, nitems);
+      const int grid = grid_tiles(ctx, kern, threads, smem, da.nitems, &ctas_per_sm[FCC_CLASS_DENSE]);
       if (threads == 512) {
-        if (sentinel) k_contract_dense<true, 512><<<grid, 512, smem, st>>>(a);
-        else k_contract_dense<false, 512><<<grid, 512, smem, st>>>(a);
+        if (sentinel) k_contract_dense<true, 512><<<grid, 512, smem, st>>>(da);
+        else k_contract_dense<false, 512><<<grid, 512, smem, st>>>(da);
       } else {
-        if (sentinel) k_contract_dense<true, 1024><<<grid, 1024, smem, st>>>(a);
-        else k_contract_dense<false, 1024><<<grid, 1024, smem, st>>>(a);
+        if (sentinel) k_contract_dense<true, 1024><<<grid, 1024, smem, st>>>(da);
+        else k_contract_dense<false, 1024><<<grid, 1024, smem, st>>>(da);
       }
       FCC_LAUNCH_CHECK();
-      tm.mark(4);
-      if (nsplit > 0) {
-        k_merge_dense<<<std::min<u32>(nsplit, u32(ctx->num_sms) * 2), kTileThreads, 0, st>>>(a);
-        FCC_LAUNCH_CHECK();
-      }
-    } else {
-      if (nsplit > 0) {
-        FCC_CUDA(cudaMemsetAsync(gkeys, 0xFF, sizeof(u64) * hash_total, st));
-        FCC_CUDA(cudaMemsetAsync(gvals, 0, sizeof(double) * hash_total, st));
-      }
-      const size_t smem = size_t(hslots) * 16 + size_t(nwarps) * hot * 8 + size_t(nwarps) * (hot / 32) * 4;
-      auto launch = [&](auto colptr) {
-        using ColT = std::remove_const_t<std::remove_pointer_t<decltype(colptr)>>;
-        HashArgs<ColT> a{items, nitems, counter, tile_rank0, urow, tile_nrows, tile_abeg, split_of_tile, split_tiles,
-                         nsplit,
-                         src, colptr, LB, u32(TL), hslots, hot, t_hoff, t_hsz, gkeys, gvals, o, dec, ctx->d_err};
-        const void *kern = threads == 512 ? reinterpret_cast<const void *>(k_contract_hash<ColT, 512>)
-                                          : reinterpret_cast<const void *>(k_contract_hash<ColT, 1024>);
-        FCC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        const int grid = grid_tiles(ctx, kern, threads, smem, nitems);
-        if (threads == 512) k_contract_hash<ColT, 512><<<grid, 512, smem, st>>>(a);
-        else k_contract_hash<ColT, 1024><<<grid, 1024, smem, st>>>(a);
-        FCC_LAUNCH_CHECK();
-        tm.mark(4);
-        if (nsplit > 0) {
-          k_merge_hash<ColT><<<std::min<u32>(nsplit, u32(ctx->num_sms) * 2), kTileThreads, 0, st>>>(a);
-          FCC_LAUNCH_CHECK();
-        }
-      };
-      if (colb32) launch(static_cast<const u32 *>(colB));
-      else launch(static_cast<const u64 *>(colB));
     }
+    auto run_hash = [&](auto colptr) {
+      using ColT = std::remove_const_t<std::remove_pointer_t<decltype(colptr)>>;
+      HashArgs<ColT> ha{nullptr, 0, nullptr, tile_rank0, urow, tile_nrows, tile_abeg, split_of_tile, split_tiles_h,
+                        nsplit_h, src, colptr, LB, u32(grouped ? std::max<u64>(TL, 2) : TL), 0u, hot, hoff_t,
+                        hsz_t, gkeys, gvals, o, dec,
+                        ctx->d_err, nullptr};
+      for (int c = FCC_CLASS_HASH_L; c < FCC_NUM_CLASSES; c++) {
+        if (!ccount[c]) continue;
+        ha.items = items + cbeg[c];
+        ha.nitems = ccount[c];
+        ha.counter = counters + c;
+        ha.slots = hc[c].slots;
+        ha.item_cyc = item_cyc ? item_cyc + cbeg[c] : nullptr;
+        const int threads = hc[c].threads;
+        const size_t smem = class_smem(c, hot);
+        const void *kern = threads == 256   ? reinterpret_cast<const void *>(k_contract_hash<ColT, 256>)
+                           : threads == 512 ? reinterpret_cast<const void *>(k_contract_hash<ColT, 512>)
+                                            : reinterpret_cast<const void *>(k_contract_hash<ColT, 1024>);
+        FCC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        const int grid = grid_tiles(ctx, kern, threads, smem, ha.nitems, &ctas_per_sm[c]);
+        if (threads == 256) k_contract_hash<ColT, 256><<<grid, 256, smem, st>>>(ha);
+        else if (threads == 512) k_contract_hash<ColT, 512><<<grid, 512, smem, st>>>(ha);
+        else k_contract_hash<ColT, 1024><<<grid, 1024, smem, st>>>(ha);
+        FCC_LAUNCH_CHECK();
+      }
+      tm.mark(4);
+      if (nsplit_d > 0) {
+        k_merge_dense<<<std::min<u32>(nsplit_d, u32(ctx->num_sms) * 2), kTileThreads, 0, st>>>(da);
+        FCC_LAUNCH_CHECK();
+      }
+      if (nsplit_h > 0) {
+        k_merge_hash<ColT><<<std::min<u32>(nsplit_h, u32(ctx->num_sms) * 2), kTileThreads, 0, st>>>(ha);
+        FCC_LAUNCH_CHECK();
+      }
+    };
+    if (colb32) run_hash(static_cast<const u32 *>(colB));
+    else run_hash(static_cast<const u64 *>(colB));
     tm.mark(5);
     read_scalars(ctx, d_sc);
     const u64 produced = ctx->h_scalars[S_CURSOR];
@@ -1734,6 +1933,21 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     free_result_buffers(res, st);
     cap = produced;
     tm.next = 4;  // re-time the contraction
+  }
+  if (ctx->sched) {  // per-tile record for fcc_sched_last_tiles
+    SchedIo &io = *ctx->sched;
+    io.ntiles = ntiles;
+    io.features = feat;
+    io.cls = cls;
+    io.cost = nullptr;
+    if (want_record && ntiles > 0) {
+      double *cost = ar.get_n<double>(ntiles);
+      double occ[FCC_NUM_CLASSES];
+      for (int c = 0; c < FCC_NUM_CLASSES; c++) occ[c] = ctas_per_sm[c] > 0 ? double(ctas_per_sm[c]) : 1.0;
+      tile_costs(st, ntiles, corder, cls, item_off, t_items, item_cyc, occ, cost);
+      FCC_CUDA(cudaStreamSynchronize(st));
+      io.cost = cost;
+    }
   }
   tm.finish();
   cleanup.done = true;

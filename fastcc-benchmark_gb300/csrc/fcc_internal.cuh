@@ -7,6 +7,7 @@
 #include <atomic>
 #include <cstdint>
 #include <cstdio>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -85,6 +86,25 @@ class Arena {
 
 // What one contraction runs against: a context's stream, workspace and
 // scratch words, or the fixed scratch of an allocation-free call.
+// Per-context state of the tile scheduler: the learned cost model (device
+// copy) and the last contraction's per-tile record, which lives in the
+// workspace and stays valid until the next contraction on the context.
+struct SchedIo {
+  float *model = nullptr;           // FCC_SCHED_MODEL_FLOATS on the device; NULL: none
+  u32 ntiles = 0;
+  const float *features = nullptr;  // ntiles x FCC_SCHED_FEATURES; NULL unless computed
+  const u32 *cls = nullptr;         // class of each tile
+  const double *cost = nullptr;     // measured cost of each tile (opts.timing = 2), else NULL
+};
+
+// fcc_sched.cu: per-tile features, predicted class costs, measured tile costs.
+void tile_features(cudaStream_t st, const u32 *ntiles_p, u32 nmax, const u32 *abeg, const u64 *P, const u32 *nrows,
+                   const u32 *lb, u64 LB, float *feat);
+void predict_costs(cudaStream_t st, const u32 *ntiles_p, u32 nmax, const float *feat, const float *model,
+                   float *pred);
+void tile_costs(cudaStream_t st, u32 ntiles, const u32 *corder, const u32 *cls, const u32 *item_off,
+                const u32 *t_items, const u64 *item_cyc, const double *occ, double *cost);
+
 struct Runtime {
   explicit Runtime(Arena &a) : arena(a) {}
   Arena &arena;
@@ -100,9 +120,11 @@ struct Runtime {
   i64 out_stride = 0;
   double *out_vals = nullptr;
   u64 out_cap = 0;
+  SchedIo *sched = nullptr;        // NULL: no learned schedule and no per-tile record
 };
 
 void set_thread_error(const std::string &msg);
+void *pool_alloc(cudaMemPool_t pool, size_t bytes, cudaStream_t st);  // fcc_prims.cu
 
 }  // namespace fcc
 
@@ -118,6 +140,8 @@ struct fcc_ctx {
   fcc::u64 *h_scalars = nullptr;   // pinned host scalars for read-backs
   cudaEvent_t ev[FCC_NUM_PHASES + 1] = {};
   double phase_ms[FCC_NUM_PHASES] = {};
+  fcc::SchedIo sched;
+  std::map<std::string, std::pair<fcc_options, double>> tuned;  // autotuner cache: signature -> best
   std::string last_error;
 };
 

@@ -26,11 +26,31 @@ void Arena::begin(cudaStream_t s) {
   if (chunks_.empty() && high_ > 0) {
     size_t sz = (high_ + (size_t(2) << 20) - 1) & ~((size_t(2) << 20) - 1);
     void *p = nullptr;
-    FCC_CUDA(cudaMallocFromPoolAsync(&p, sz, pool_, s));
+    p = pool_alloc(pool_, sz, s);
     chunks_.push_back({static_cast<char *>(p), sz});
   }
   used_ = 0;
   total_used_ = 0;
+}
+
+// Allocation from a stream-ordered pool that keeps freed blocks cached:
+// when a request does not fit, wait for the stream's pending frees, return
+// the pool's unused memory to the device and try once more.
+void *pool_alloc(cudaMemPool_t pool, size_t bytes, cudaStream_t st) {
+  void *p = nullptr;
+  cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, pool, st);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    FCC_CUDA(cudaStreamSynchronize(st));
+    FCC_CUDA(cudaMemPoolTrimTo(pool, 0));
+    e = cudaMallocFromPoolAsync(&p, bytes, pool, st);
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error{e == cudaErrorMemoryAllocation ? FCC_ERR_OOM : FCC_ERR_CUDA,
+                "device allocation of " + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e)};
+  }
+  return p;
 }
 
 void *Arena::get(size_t bytes) {
@@ -50,7 +70,7 @@ void *Arena::get(size_t bytes) {
     if (!chunks_.empty() && chunks_.back().size > sz) sz = chunks_.back().size;
     if (sz < bytes) sz = bytes;
     void *p = nullptr;
-    FCC_CUDA(cudaMallocFromPoolAsync(&p, sz, pool_, stream_));
+    p = pool_alloc(pool_, sz, stream_);
     chunks_.push_back({static_cast<char *>(p), sz});
     used_ = 0;
   }

@@ -22,6 +22,11 @@ ACC_AUTO, ACC_DENSE, ACC_HASH = 0, 1, 2
 RADIX_PER_OPERAND, RADIX_SHARED = 0, 1
 DENSE_AUTO, DENSE_BITMASK, DENSE_SENTINEL = 0, 1, 2
 PHASES = ["upload", "index", "plan", "contract", "merge", "total"]
+CLASS_DENSE, CLASS_HASH_L, CLASS_HASH_M, CLASS_HASH_S = 0, 1, 2, 3
+NUM_CLASSES = 4
+SCHED_RULE, SCHED_LEARNED, SCHED_FORCE = 0, 1, 2
+SCHED_FEATURES, SCHED_HIDDEN = 12, 64
+SCHED_MODEL_FLOATS = 2 * 12 + 12 * 64 + 64 + 64 * 64 + 64 + 64 * 4 + 4
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "hash accumulator full",
           4: "bounded device wait timed out", 5: "CUDA error", 6: "index space exceeds 64 bits",
           7: "no usable sm_103 device", 8: "output buffer too small"}
@@ -47,7 +52,8 @@ class Options(ctypes.Structure):
                 ("hash_slots", ctypes.c_int32), ("timing", ctypes.c_int32),
                 ("pad0", ctypes.c_int32), ("capacity_hint", ctypes.c_int64),
                 ("dense_mode", ctypes.c_int32), ("tile_threads", ctypes.c_int32),
-                ("hot_columns", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
+                ("hot_columns", ctypes.c_int32), ("schedule", ctypes.c_int32),
+                ("dense_fill_log2", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -79,6 +85,18 @@ def lib():
                                          i32, ctypes.POINTER(Options), ctypes.POINTER(i64)]
         L.fcc_contract_batch.argtypes = [vp, i32, ctypes.POINTER(_CTensor), ctypes.POINTER(_CTensor), vp, vp,
                                          i32, ctypes.POINTER(Options), ctypes.POINTER(vp), vp]
+        L.fcc_autotune.argtypes = [vp, ctypes.POINTER(_CTensor), ctypes.POINTER(_CTensor), vp, vp, i32,
+                                   ctypes.POINTER(Options), i32, ctypes.POINTER(Options),
+                                   ctypes.POINTER(ctypes.c_double)]
+        L.fcc_autotune_batch.argtypes = [vp, i32, ctypes.POINTER(_CTensor), ctypes.POINTER(_CTensor), vp, vp,
+                                         i32, ctypes.POINTER(Options), i32, ctypes.POINTER(Options),
+                                         ctypes.POINTER(ctypes.c_double)]
+        L.fcc_sched_set_model.argtypes = [vp, vp, i64]
+        L.fcc_sched_last_tiles.argtypes = [vp, vp, vp, vp, i64, ctypes.POINTER(i64)]
+        L.fcc_mlp_predict.argtypes = [vp, vp, i64, vp, vp]
+        L.fcc_mlp_grad.argtypes = [vp, vp, vp, vp, i64, vp, vp, ctypes.POINTER(ctypes.c_float)]
+        L.fcc_mlp_train.argtypes = [vp, vp, vp, vp, i64, i32, i32, ctypes.c_float, ctypes.c_uint64, vp,
+                                    ctypes.POINTER(ctypes.c_float)]
         L.fcc_result_info.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i64), ctypes.POINTER(i64)]
         L.fcc_result_device.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(i64), ctypes.POINTER(vp)]
         L.fcc_result_copy_to_host.argtypes = [vp, vp, i64, i64, vp]
@@ -266,6 +284,97 @@ class Context:
                                              cb.ctypes.data if cb.size else None, int(ca.size),
                                              ctypes.byref(o), ctypes.byref(n)))
         return n.value
+
+    # ---- autotuner ----
+    def autotune(self, a, b, ctr_a, ctr_b, base=None, reps=2):
+        """Fastest candidate schedule for this problem (fcc_autotune): (Options, ms)."""
+        ca = np.ascontiguousarray(ctr_a, dtype=np.int32)
+        cb = np.ascontiguousarray(ctr_b, dtype=np.int32)
+        ta, tb = a._struct(), b._struct()
+        best, ms = Options(), ctypes.c_double()
+        self._check(lib().fcc_autotune(self._h, ctypes.byref(ta), ctypes.byref(tb),
+                                       ca.ctypes.data if ca.size else None, cb.ctypes.data if cb.size else None,
+                                       int(ca.size), ctypes.byref(base if base is not None else Options()),
+                                       int(reps), ctypes.byref(best), ctypes.byref(ms)))
+        return best, ms.value
+
+    def autotune_batch(self, As, Bs, ctr_a, ctr_b, base=None, reps=2):
+        """fcc_autotune_batch: (Options, ms) for one fcc_contract_batch call."""
+        ca = np.ascontiguousarray(ctr_a, dtype=np.int32)
+        cb = np.ascontiguousarray(ctr_b, dtype=np.int32)
+        n = len(As)
+        ta = (_CTensor * n)(*[x._struct() for x in As])
+        tb = (_CTensor * n)(*[x._struct() for x in Bs])
+        best, ms = Options(), ctypes.c_double()
+        self._check(lib().fcc_autotune_batch(self._h, n, ta, tb, ca.ctypes.data if ca.size else None,
+                                             cb.ctypes.data if cb.size else None, int(ca.size),
+                                             ctypes.byref(base if base is not None else Options()), int(reps),
+                                             ctypes.byref(best), ctypes.byref(ms)))
+        return best, ms.value
+
+    @staticmethod
+    def options_dict(o):
+        return {name: getattr(o, name) for name, _ in Options._fields_ if name not in ("pad0", "reserved")}
+
+    def load_default_model(self):
+        """Installs the cost model shipped with the package (sched_model.f32); False when absent."""
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "sched_model.f32")
+        if not os.path.exists(path):
+            return False
+        self.sched_set_model(np.fromfile(path, np.float32))
+        return True
+
+    # ---- learned tile schedule ----
+    def sched_set_model(self, model):
+        """Installs an FP32 cost model (SCHED_MODEL_FLOATS floats) or removes it (None)."""
+        if model is None:
+            self._check(lib().fcc_sched_set_model(self._h, None, 0))
+            return
+        m = np.ascontiguousarray(model, dtype=np.float32)
+        self._check(lib().fcc_sched_set_model(self._h, m.ctypes.data, int(m.size)))
+
+    def sched_last_tiles(self, features=True, cost=True):
+        """Per-tile record of the last contraction: dict with 'cls' and, when
+        recorded (timing=2), 'features' (ntiles x 12) and 'cost' (ntiles)."""
+        n = ctypes.c_int64()
+        self._check(lib().fcc_sched_last_tiles(self._h, None, None, None, 0, ctypes.byref(n)))
+        nt = n.value
+        cls = np.empty(nt, np.int32)
+        f = np.empty((nt, SCHED_FEATURES), np.float32) if features else None
+        c = np.empty(nt, np.float64) if cost else None
+        self._check(lib().fcc_sched_last_tiles(self._h, f.ctypes.data if f is not None else None, cls.ctypes.data,
+                                               c.ctypes.data if c is not None else None, nt, ctypes.byref(n)))
+        out = {"cls": cls}
+        if f is not None:
+            out["features"] = f
+        if c is not None:
+            out["cost"] = c
+        return out
+
+    def mlp_predict(self, X, model):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        m = np.ascontiguousarray(model, dtype=np.float32)
+        Y = np.empty((X.shape[0], NUM_CLASSES), np.float32)
+        self._check(lib().fcc_mlp_predict(self._h, X.ctypes.data, X.shape[0], m.ctypes.data, Y.ctypes.data))
+        return Y
+
+    def mlp_grad(self, X, Y, M, model):
+        X, Y, M = (np.ascontiguousarray(a, dtype=np.float32) for a in (X, Y, M))
+        m = np.ascontiguousarray(model, dtype=np.float32)
+        g = np.empty(SCHED_MODEL_FLOATS, np.float32)
+        loss = ctypes.c_float()
+        self._check(lib().fcc_mlp_grad(self._h, X.ctypes.data, Y.ctypes.data, M.ctypes.data, X.shape[0],
+                                       m.ctypes.data, g.ctypes.data, ctypes.byref(loss)))
+        return g, loss.value
+
+    def mlp_train(self, X, Y, M, model, epochs=200, batch=4096, lr=1e-3, seed=1):
+        X, Y, M = (np.ascontiguousarray(a, dtype=np.float32) for a in (X, Y, M))
+        m = np.array(model, dtype=np.float32, copy=True)
+        loss = ctypes.c_float()
+        self._check(lib().fcc_mlp_train(self._h, X.ctypes.data, Y.ctypes.data, M.ctypes.data, X.shape[0],
+                                        int(epochs), int(batch), float(lr), int(seed), m.ctypes.data,
+                                        ctypes.byref(loss)))
+        return m, loss.value
 
     def timings(self):
         ms = (ctypes.c_double * 6)()

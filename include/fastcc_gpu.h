@@ -36,7 +36,7 @@ extern "C" {
 #endif
 
 #define FCC_MAX_ORDER 8
-#define FCC_ABI_VERSION 1
+#define FCC_ABI_VERSION 2
 
 typedef enum fcc_status {
   FCC_OK = 0,
@@ -99,8 +99,31 @@ typedef struct fcc_options {
   int32_t tile_threads;       /* threads per tile CTA: 512 (default) or 1024 */
   int32_t hot_columns;        /* per-warp copies of the most frequent B columns in row tiles:
                                  0 or -1 off (default), or a count (multiple of 32) */
-  int32_t reserved[1];
+  int32_t schedule;           /* fcc_schedule: how each output tile picks its class */
+  int32_t dense_fill_log2;    /* FCC_SCHED_RULE: a tile takes the dense class only when its
+                                 multiply-adds >= its area / 2^dense_fill_log2; 0 = whenever
+                                 the tile fits the dense accumulator */
+  int32_t reserved[3];
 } fcc_options;
+
+/* Tile classes: every output tile runs in one of them. The hash classes
+ * differ in table size and CTA shape: the small ones run several CTAs per SM
+ * so that small tiles overlap their barriers and memory latency. */
+enum {
+  FCC_CLASS_DENSE = 0,   /* shared-memory dense tile, 512 threads (tile_threads) */
+  FCC_CLASS_HASH_L = 1,  /* hash, 8192 slots, 512 threads, one CTA per SM */
+  FCC_CLASS_HASH_M = 2,  /* hash, 4096 slots, 256 threads */
+  FCC_CLASS_HASH_S = 3,  /* hash, 2048 slots, 256 threads */
+  FCC_NUM_CLASSES = 4
+};
+
+typedef enum fcc_schedule {
+  FCC_SCHED_RULE = 0,     /* dense when the tile fits it (see dense_fill_log2), else the smallest
+                             hash table that holds the tile without splitting it */
+  FCC_SCHED_LEARNED = 1,  /* per-tile class from the context's cost model (fcc_sched_set_model);
+                             FCC_SCHED_RULE when none is set */
+  FCC_SCHED_FORCE = 2     /* FCC_SCHED_FORCE + class: one class for every tile */
+} fcc_schedule;
 
 /* Touched-position tracking of the dense accumulator. Both emit every touched
  * position, exact zero sums included. The sentinel form is used only when no
@@ -223,6 +246,69 @@ int fcc_contract_noalloc(const fcc_tensor *A, const fcc_tensor *B, const int32_t
                          const int32_t *ctrB, int32_t k, const fcc_options *opts, void *cuda_stream,
                          uint32_t *out_coords, int64_t out_mode_stride, double *out_values,
                          int64_t out_capacity, int64_t *out_nnz, int64_t *out_products);
+
+/*
+ * Autotuner (no counterpart in the reference, whose tile size and
+ * accumulator are fixed by the caller). Times the contraction, reps runs
+ * after one warm-up, under each candidate: the rule (fill threshold 0 or
+ * 2^-6) and the dense class forced, each with 512 and 1024 threads per dense
+ * tile, and each hash class forced. *best receives the fastest candidate
+ * (base's other fields kept) and *best_ms its mean total time. The winner is
+ * cached on ctx under the problem's shape signature (orders, contracted
+ * modes, log2 buckets of the nonzero counts and mode extents): a later call
+ * on a same-shaped problem returns it without running anything.
+ */
+int fcc_autotune(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                 const int32_t *ctrB, int32_t k, const fcc_options *base, int32_t reps, fcc_options *best,
+                 double *best_ms);
+/* The same for a batch (fcc_contract_batch). */
+int fcc_autotune_batch(fcc_ctx *ctx, int32_t n, const fcc_tensor *A, const fcc_tensor *B,
+                       const int32_t *ctrA, const int32_t *ctrB, int32_t k, const fcc_options *base,
+                       int32_t reps, fcc_options *best, double *best_ms);
+
+/*
+ * Learned tile schedule. The reference has no scheduler (its tiles all run
+ * the one accumulator picked by template argument); these calls serve
+ * FCC_SCHED_LEARNED.
+ *
+ * The cost model is an FP32 MLP, FCC_SCHED_FEATURES -> 64 -> 64 ->
+ * FCC_NUM_CLASSES with ReLU, whose outputs are the predicted cost of a tile
+ * in each class (log2 of SM cycles); a tile takes the class of lowest
+ * prediction. Model layout (FCC_SCHED_MODEL_FLOATS floats): mean[12],
+ * scale[12] (inputs are standardised as (x - mean) * scale), W1[12][64],
+ * b1[64], W2[64][64], b2[64], W3[64][4], b3[4]. Features of a tile, in
+ * order: log2(1 + multiply-adds), log2(1 + A entries), log2(rows),
+ * log2(column span), log2(area = rows x span), estimated fill
+ * min(multiply-adds, area) / area, the fractions of its multiply-adds whose
+ * B segment is shorter than 64, 64..1023 and at least 1024 entries long,
+ * log2(1 + mean segment length), log2(1 + longest segment), log2(1 +
+ * multiply-adds per row).
+ */
+#define FCC_SCHED_FEATURES 12
+#define FCC_SCHED_HIDDEN 64
+#define FCC_SCHED_MODEL_FLOATS (2 * 12 + 12 * 64 + 64 + 64 * 64 + 64 + 64 * 4 + 4)
+/* Installs (copies to the device) or, with model NULL, removes the model. */
+int fcc_sched_set_model(fcc_ctx *ctx, const float *model, int64_t n);
+/* Per-tile record of the last contraction on ctx: features (ntiles x 12;
+ * computed with opts.timing = 2 or a learned schedule), class, and with
+ * opts.timing = 2 the measured cost (SM cycles of its work items divided by
+ * the CTAs per SM of its class). Copies min(cap, ntiles) tiles; any pointer
+ * may be NULL; *ntiles receives the tile count. */
+int fcc_sched_last_tiles(fcc_ctx *ctx, float *features, int32_t *cls, double *cost, int64_t cap,
+                         int64_t *ntiles);
+/* The MLP on the device (hand-written FP32 kernels). Host arrays, row-major:
+ * X n x 12, Y and M (mask, 0 or 1) n x 4. Loss: sum M (y' - y)^2 / sum M. */
+int fcc_mlp_predict(fcc_ctx *ctx, const float *X, int64_t n, const float *model, float *Y);
+/* Gradient of the loss over all n rows, in model layout (mean and scale
+ * entries get 0). */
+int fcc_mlp_grad(fcc_ctx *ctx, const float *X, const float *Y, const float *M, int64_t n, const float *model,
+                 float *grad, float *loss);
+/* Adam (beta 0.9 / 0.999), minibatches of `batch` rows reshuffled every
+ * epoch from `seed`; model holds the initial parameters (mean and scale
+ * included, kept as given) and receives the trained ones; *loss gets the
+ * final loss over all rows. */
+int fcc_mlp_train(fcc_ctx *ctx, const float *X, const float *Y, const float *M, int64_t n, int32_t epochs,
+                  int32_t batch, float lr, uint64_t seed, float *model, float *loss);
 
 /* Diagnostics: kernels this process has launched through the library so far. */
 int64_t fcc_launch_count(void);

@@ -1,0 +1,241 @@
+"""The tile scheduler on the GPU.
+
+* MLP kernels (fcc_mlp_predict / fcc_mlp_grad / fcc_mlp_train, FP32) against
+  a float64 torch restatement of the same network and loss, gradients by
+  autograd. Tolerances are FP32 ones, written in each test.
+* Every schedule (rule, each forced class, learned with arbitrary models)
+  gives the oracle's result: the schedule picks kernels, never values.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import fastcc_gpu as F
+import oracle
+import workloads
+from helpers import check_parity
+
+pytestmark = pytest.mark.gpu
+
+NF, NH, NO = F.SCHED_FEATURES, F.SCHED_HIDDEN, F.NUM_CLASSES
+
+
+def _split(m):
+    o = 0
+    out = []
+    for shape in [(NF,), (NF,), (NF, NH), (NH,), (NH, NH), (NH,), (NH, NO), (NO,)]:
+        n = int(np.prod(shape))
+        out.append(m[o:o + n].reshape(shape))
+        o += n
+    return out
+
+
+def torch_loss(model, X, Y, M):
+    import torch
+    m = torch.tensor(np.asarray(model, np.float64), requires_grad=True)
+    mean, scale, W1, b1, W2, b2, W3, b3 = _split(m)
+    x = (torch.tensor(X, dtype=torch.float64) - mean) * scale
+    h1 = torch.relu(x @ W1 + b1)
+    h2 = torch.relu(h1 @ W2 + b2)
+    y = h2 @ W3 + b3
+    Mt = torch.tensor(M, dtype=torch.float64)
+    loss = (Mt * (y - torch.tensor(Y, dtype=torch.float64)) ** 2).sum() / Mt.sum()
+    return m, y, loss
+
+
+def random_model(rng, X=None):
+    parts = [np.zeros(NF) if X is None else X.mean(0), np.ones(NF) if X is None else 1 / (X.std(0) + 1e-3),
+             rng.normal(0, 0.4, (NF, NH)), rng.normal(0, 0.1, NH), rng.normal(0, 0.2, (NH, NH)),
+             rng.normal(0, 0.1, NH), rng.normal(0, 0.2, (NH, NO)), rng.normal(0, 0.1, NO)]
+    return np.concatenate([np.ravel(p) for p in parts]).astype(np.float32)
+
+
+def test_mlp_predict_matches_fp64(ctx):
+    rng = np.random.Generator(np.random.PCG64(11))
+    X = rng.normal(0, 2, (777, NF)).astype(np.float32)
+    model = random_model(rng, X)
+    got = ctx.mlp_predict(X, model)
+    _, want, _ = torch_loss(model, X, np.zeros((777, NO)), np.ones((777, NO)))
+    want = want.detach().numpy()
+    # FP32 accumulation over 64-term dot products: 1e-4 of the output scale
+    assert np.max(np.abs(got - want)) <= 1e-4 * max(1.0, np.max(np.abs(want)))
+
+
+def test_mlp_grad_matches_autograd(ctx):
+    rng = np.random.Generator(np.random.PCG64(12))
+    n = 513
+    X = rng.normal(0, 1.5, (n, NF)).astype(np.float32)
+    Y = rng.normal(10, 3, (n, NO)).astype(np.float32)
+    M = (rng.random((n, NO)) < 0.8).astype(np.float32)
+    model = random_model(rng, X)
+    g, loss = ctx.mlp_grad(X, Y, M, model)
+    m, _, tl = torch_loss(model, X, Y, M)
+    tl.backward()
+    want = m.grad.numpy()
+    assert abs(loss - tl.item()) <= 1e-4 * tl.item()
+    assert np.all(g[:2 * NF] == 0)  # mean and scale are not trained
+    # FP32 sums over n rows: 1e-3 of the largest gradient entry per block
+    o = 2 * NF
+    for block in _split(np.asarray(want))[2:]:
+        k = block.size
+        ref = want[o:o + k]
+        assert np.max(np.abs(g[o:o + k] - ref)) <= 1e-3 * max(np.max(np.abs(ref)), 1e-6), f"block at {o}"
+        o += k
+
+
+def test_mlp_train_fits_a_teacher(ctx):
+    rng = np.random.Generator(np.random.PCG64(13))
+    n = 20000
+    X = rng.normal(0, 1, (n, NF)).astype(np.float32)
+    teacher = random_model(rng)
+    Y = ctx.mlp_predict(X, teacher) + rng.normal(0, 0.01, (n, NO)).astype(np.float32)
+    M = np.ones((n, NO), np.float32)
+    M[rng.random((n, NO)) < 0.1] = 0
+    student = random_model(np.random.Generator(np.random.PCG64(99)), X)
+    _, l0 = ctx.mlp_grad(X, Y, M, student)
+    trained, l1 = ctx.mlp_train(X, Y, M, student, epochs=60, batch=2048, lr=2e-3, seed=5)
+    assert np.array_equal(trained[:2 * NF], student[:2 * NF])
+    assert l1 < l0 / 20, (l0, l1)
+    # the same seed trains the same model
+    again, l2 = ctx.mlp_train(X, Y, M, student, epochs=2, batch=2048, lr=2e-3, seed=5)
+    again2, l3 = ctx.mlp_train(X, Y, M, student, epochs=2, batch=2048, lr=2e-3, seed=5)
+    assert np.array_equal(again, again2)
+
+
+def _cases():
+    w = workloads.readme(seed=21, scale=0.05)
+    yield "readme", [(w["a"], w["b"])], w["ctr_a"], w["ctr_b"], False
+    w = workloads.twomode(seed=22, nnz=60_000, dims=(400, 400, 150, 20))
+    yield "twomode", [(w["a"], w["b"])], w["ctr_a"], w["ctr_b"], False
+    w = workloads.zipf3(seed=23, nnz=80_000, dims=(900, 900, 20_000))
+    yield "zipf3", [(w["a"], w["b"])], w["ctr_a"], w["ctr_b"], False
+    inst = workloads.batched(seed=24, count=6, nnz_lo=100, nnz_hi=2e4, dim_lo=8, dim_hi=64)
+    yield "batched", [(x["a"], x["b"]) for x in inst], [1, 3], [1, 2], True
+
+
+def _run(ctx, pairs, ca, cb, batched, opts):
+    if batched:
+        r, _ = ctx.contract_batch([p[0] for p in pairs], [p[1] for p in pairs], ca, cb, opts)
+    else:
+        r = ctx.contract(pairs[0][0], pairs[0][1], ca, cb, opts)
+    try:
+        return r.to_numpy()
+    finally:
+        r.free()
+
+
+@pytest.mark.parametrize("case", ["readme", "twomode", "zipf3", "batched"])
+def test_every_schedule_gives_the_oracle_result(ctx, case):
+    name, pairs, ca, cb, batched = next(c for c in _cases() if c[0] == case)
+    if batched:
+        want = []
+        for t, (a, b) in enumerate(pairs):
+            o = oracle.fastcc_multiply(a.coords, a.values, a.max_index, b.coords, b.values, b.max_index, ca, cb,
+                                       want_abs=True)
+            want.append(o)
+    else:
+        a, b = pairs[0]
+        want = oracle.fastcc_multiply(a.coords, a.values, a.max_index, b.coords, b.values, b.max_index, ca, cb,
+                                      want_abs=True)
+    rng = np.random.Generator(np.random.PCG64(31))
+    schedules = [dict(schedule=F.SCHED_RULE), dict(schedule=F.SCHED_RULE, dense_fill_log2=3)]
+    schedules += [dict(schedule=F.SCHED_FORCE + c) for c in range(F.NUM_CLASSES)]
+    schedules += [dict(schedule=F.SCHED_LEARNED, products_per_item=p) for p in (0, 50)]
+    ran = 0
+    for sch in schedules:
+        learned = sch["schedule"] == F.SCHED_LEARNED
+        if learned:
+            ctx.sched_set_model(random_model(rng))
+        try:
+            c, v = _run(ctx, pairs, ca, cb, batched, F.Options(**sch))
+        except F.FccError as e:
+            assert sch.get("schedule") == F.SCHED_FORCE and e.status == 1  # dense too wide here
+            continue
+        finally:
+            if learned:
+                ctx.sched_set_model(None)
+        ran += 1
+        if batched:
+            for t, o in enumerate(want):
+                sel = c[:, 0] == t
+                check_parity(c[sel, 1:], v[sel], o["coords"], o["values"], o["abs_sum"])
+        else:
+            check_parity(c, v, want["coords"], want["values"], want["abs_sum"])
+    assert ran >= 6
+
+
+def test_learned_schedule_mixes_classes_and_records_tiles(ctx):
+    # B span 20,000: one row per tile, hub rows with many multiply-adds, tail rows with few
+    w = workloads.zipf3(seed=25, nnz=80_000, dims=(20_000, 20_000, 500_000))
+    rng = np.random.Generator(np.random.PCG64(32))
+    # a model that prefers the dense class for tiles with many multiply-adds
+    m = np.zeros(F.SCHED_MODEL_FLOATS, np.float32)
+    mean, scale, W1, b1, W2, b2, W3, b3 = _split(m)
+    scale[:] = 1.0
+    W1[0, 0] = 1.0            # h1_0 = log2(1 + multiply-adds)
+    W2[0, 0] = 1.0            # h2_0 = h1_0
+    W3[0, F.CLASS_DENSE] = -1.0
+    b3[:] = [0.0, -9.0, -9.0, -9.0]  # predicted log2 costs: hash -9, dense -log2(1 + multiply-adds)
+    ctx.sched_set_model(m)
+    try:
+        r = ctx.contract(w["a"], w["b"], w["ctr_a"], w["ctr_b"], F.Options(schedule=F.SCHED_LEARNED, timing=2))
+        r.free()
+        t = ctx.sched_last_tiles()
+    finally:
+        ctx.sched_set_model(None)
+    cls, feats, cost = t["cls"], t["features"], t["cost"]
+    assert feats.shape == (cls.size, NF) and cost.shape == cls.shape
+    assert np.all(cost > 0)
+    prod = np.exp2(feats[:, 0]) - 1
+    big = prod > 2 ** 9.5
+    assert np.all(cls[big] == F.CLASS_DENSE)
+    assert np.all(cls[prod < 2 ** 8.5] != F.CLASS_DENSE)
+    assert set(np.unique(cls)) > {F.CLASS_DENSE}
+    # features: fractions sum to one, fill within [0, 1]
+    assert np.allclose(feats[:, 6] + feats[:, 7] + feats[:, 8], 1.0, atol=1e-5)
+    assert np.all((feats[:, 5] >= 0) & (feats[:, 5] <= 1))
+
+
+def test_shipped_model_loads(ctx):
+    path = os.path.join(os.path.dirname(F.__file__), "sched_model.f32")
+    if not os.path.exists(path):
+        pytest.skip("no trained model in the package")
+    m = np.fromfile(path, np.float32)
+    assert m.size == F.SCHED_MODEL_FLOATS and np.all(np.isfinite(m))
+    ctx.sched_set_model(m)
+    ctx.sched_set_model(None)
+
+
+def test_autotune_returns_a_cached_schedule_with_the_oracle_result(ctx):
+    w = workloads.twomode(seed=26, nnz=60_000, dims=(400, 400, 150, 20))
+    a, b = w["a"], w["b"]
+    best, ms = ctx.autotune(a, b, w["ctr_a"], w["ctr_b"], reps=1)
+    assert ms > 0 and 0 <= best.schedule < F.SCHED_FORCE + F.NUM_CLASSES
+    again, ms2 = ctx.autotune(a, b, w["ctr_a"], w["ctr_b"], reps=1)  # cached: same answer
+    assert ms2 == ms and F.Context.options_dict(again) == F.Context.options_dict(best)
+    r = ctx.contract(a, b, w["ctr_a"], w["ctr_b"], best)
+    try:
+        c, v = r.to_numpy()
+    finally:
+        r.free()
+    o = oracle.fastcc_multiply(a.coords, a.values, a.max_index, b.coords, b.values, b.max_index, w["ctr_a"],
+                               w["ctr_b"], want_abs=True)
+    check_parity(c, v, o["coords"], o["values"], o["abs_sum"])
+
+
+def test_autotune_batch(ctx):
+    inst = workloads.batched(seed=27, count=5, nnz_lo=100, nnz_hi=2e4, dim_lo=8, dim_hi=64)
+    As, Bs = [x["a"] for x in inst], [x["b"] for x in inst]
+    best, ms = ctx.autotune_batch(As, Bs, [1, 3], [1, 2], reps=1)
+    assert ms > 0
+    r, counts = ctx.contract_batch(As, Bs, [1, 3], [1, 2], best)
+    try:
+        c, v = r.to_numpy()
+    finally:
+        r.free()
+    for t, (a, b) in enumerate(zip(As, Bs)):
+        o = oracle.fastcc_multiply(a.coords, a.values, a.max_index, b.coords, b.values, b.max_index, [1, 3],
+                                   [1, 2], want_abs=True)
+        sel = c[:, 0] == t
+        check_parity(c[sel, 1:], v[sel], o["coords"], o["values"], o["abs_sum"])
