@@ -174,7 +174,7 @@ def run_reference(args, ws, rank):
     print(json.dumps(line))
 
 
-def run_profile_case(name):
+def run_profile_case(name, extra=None):
     """A small case of the same kernels, sized for ncu: inputs above the L2
     size, a few GB on the device in all. Launch order: the warm-up
     contraction's kernels, then the timed one's."""
@@ -197,7 +197,7 @@ def run_profile_case(name):
                                   b.max_index)
     torch.cuda.synchronize()
     with F.Context(0) as ctx:
-        opts = F.Options(timing=1)
+        opts = F.Options(timing=1, **(extra or {}))
         for step in range(2):
             l0 = F.launch_count()
             r = ctx.contract(A, B, w["ctr_a"], w["ctr_b"], opts)
@@ -543,7 +543,7 @@ def main():
         run_reference(args, ws, rank)
         return
     if args.profile:
-        run_profile_case(args.profile)
+        run_profile_case(args.profile, json.loads(args.variants)[0])
         return
     if args.batched:
         import torch

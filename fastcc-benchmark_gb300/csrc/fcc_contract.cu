@@ -68,8 +68,10 @@ struct Out {
 };
 
 struct Item {
-  u64 p0, p1;
-  u32 tile, pad;
+  u64 p0, p1;  // multiply-adds [p0, p1) of the tile
+  u32 tile;
+  u32 ea, eb;  // its A entries: ea holds p0, eb is the first entry starting at or after p1
+  u32 pad;
 };
 
 // ------------------------------------------------------------ helpers ----
@@ -427,15 +429,25 @@ __global__ void k_item_write(const u32 *__restrict__ ntiles_p, const u32 *__rest
   for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < ntiles; i += i64(gridDim.x) * blockDim.x) {
     const u32 t = corder[i];
     const u64 pmax = ct.pmax[cls[t]];
-    const u64 b = P[abeg[t]], e = P[abeg[t + 1]];
+    const u32 alo = abeg[t], ahi = abeg[t + 1];
+    const u64 b = P[alo], e = P[ahi];
     u32 o = item_off[i];
+    u32 ea = alo;
     for (u64 p = b; p < e; p += pmax) {
       Item it;
       it.p0 = p;
       it.p1 = (e - p > pmax) ? p + pmax : e;
       it.tile = t;
+      it.ea = ea;
+      u32 lo = ea, hi = ahi;  // first entry with P[entry] >= p1
+      while (lo < hi) {
+        const u32 mid = (lo + hi) >> 1;
+        if (P[mid] < it.p1) lo = mid + 1; else hi = mid;
+      }
+      it.eb = lo;
       it.pad = 0;
       items[o++] = it;
+      ea = (lo > alo && P[lo] > it.p1) ? lo - 1 : lo;  // the entry holding the next item's p0
     }
     split_of_tile[t] = -1;
     if (split_d[i]) {
@@ -648,27 +660,6 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
   }
 }
 
-// Runs the chunks of one item on the calling CTA (all threads must call);
-// chunk starts are searched for.
-template <class ColT, class KeyT, class Add>
-__device__ __forceinline__ void products_item(const ProdSrc &s, const ColT *colB, u32 alo, u32 ahi, u64 p0,
-                                              u64 p1, u64 LB, u32 *s_chunk, Add &add) {
-  const u32 lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  const u64 np = p1 - p0;
-  u64 chunk = np / (4 * nwarps);
-  chunk = chunk < 256 ? 256 : (chunk > 4096 ? 4096 : chunk);
-  const u64 nch = (np + chunk - 1) / chunk;
-  for (;;) {
-    u32 c = 0;
-    if (lane == 0) c = atomicAdd(s_chunk, 1u);
-    c = __shfl_sync(kFull, c, 0);
-    if (c >= nch) break;
-    const u64 q0 = p0 + u64(c) * chunk;
-    const u64 q1 = min(q0 + chunk, p1);
-    products_chunk<ColT, KeyT>(s, colB, alo, ahi, kNoEntry, q0, q1, p0, p1, kNoSkip, LB, add);
-  }
-}
-
 // ---- dense items in two phases ----
 //
 // Phase 1: an A entry with >= kCtaRun multiply-adds in the item is run by the
@@ -686,33 +677,31 @@ constexpr int kCtaPer = 8;
 constexpr u32 kListMax = 1024;   // items hold at most kListMax * kCtaRun multiply-adds
 constexpr u32 kChunkMax = 2048;
 
-struct ItemPlan {
+template <u32 kLong, u32 kChunks>
+struct PlanT {
+  static constexpr u32 kLongMax = kLong, kChunkCap = kChunks, kRows = kChunks / 2;
   u32 ea, eb, nlong, nchunk, next;
   u64 chunk;
-  u32 list[kListMax];
-  u32 start[kChunkMax];  // also the drain's row cache (kRowCache u64)
+  u32 list[kLong];
+  alignas(16) u32 start[kChunks];  // also the drain's row cache (kRows u64)
 };
-constexpr u32 kRowCache = kChunkMax / 2;
+using ItemPlan = PlanT<kListMax, kChunkMax>;  // dense items: long-entry list, many chunks
+using HashPlan = PlanT<1, 512>;               // hash items (<= 4096 multiply-adds)
+constexpr u32 kRowCache = ItemPlan::kRows;
 
-__device__ void build_item_plan(const u64 *__restrict__ P, u32 alo, u32 ahi, u64 p0, u64 p1, ItemPlan &pl) {
+// ea/eb: the item's entries (Item::ea, Item::eb). Chunks hold at least
+// min_chunk multiply-adds.
+template <class Plan>
+__device__ void build_item_plan(const u64 *__restrict__ P, u32 ea, u32 eb, u64 p0, u64 p1, u64 min_chunk,
+                                Plan &pl) {
   const u32 tid = threadIdx.x, nwarps = blockDim.x >> 5;
   if (tid == 0) {
-    u32 lo = alo, hi = ahi;  // last entry with P[e] <= p0
-    while (hi - lo > 1) {
-      const u32 mid = (lo + hi) >> 1;
-      if (__ldg(&P[mid]) <= p0) lo = mid; else hi = mid;
-    }
-    pl.ea = lo;
-    u32 l2 = lo, h2 = ahi;  // first entry with P[e] >= p1 (P[ahi] >= p1)
-    while (l2 < h2) {
-      const u32 mid = (l2 + h2) >> 1;
-      if (__ldg(&P[mid]) < p1) l2 = mid + 1; else h2 = mid;
-    }
-    pl.eb = l2;
+    pl.ea = ea;
+    pl.eb = eb;
     const u64 np = p1 - p0;
     u64 chunk = np / (4 * nwarps);
-    chunk = chunk < 256 ? 256 : (chunk > 4096 ? 4096 : chunk);
-    if ((np + chunk - 1) / chunk > kChunkMax) chunk = (np + kChunkMax - 1) / kChunkMax;
+    chunk = chunk < min_chunk ? min_chunk : (chunk > 4096 ? 4096 : chunk);
+    if ((np + chunk - 1) / chunk > Plan::kChunkCap) chunk = (np + Plan::kChunkCap - 1) / Plan::kChunkCap;
     pl.chunk = chunk;
     pl.nchunk = u32((np + chunk - 1) / chunk);
     pl.nlong = 0;
@@ -725,7 +714,7 @@ __device__ void build_item_plan(const u64 *__restrict__ P, u32 alo, u32 ahi, u64
     if (hi <= lo) continue;
     if (hi - lo >= kCtaRun) {
       const u32 i = atomicAdd(&pl.nlong, 1u);
-      if (i < kListMax) pl.list[i] = e;
+      if (i < Plan::kLongMax) pl.list[i] = e;
     }
     for (u64 c = (lo - p0 + chunk - 1) / chunk; c < (hi - p0 + chunk - 1) / chunk; c++) pl.start[c] = e;
   }
@@ -734,8 +723,8 @@ __device__ void build_item_plan(const u64 *__restrict__ P, u32 alo, u32 ahi, u64
 
 template <bool kSentinel, class Add>
 __device__ void dense_item(const ProdSrc &s, const u32 *__restrict__ colB, u32 alo, u32 ahi, u64 p0, u64 p1,
-                           u32 LB, double *acc, u32 *mask, ItemPlan &pl, Add &add) {
-  build_item_plan(s.P, alo, ahi, p0, p1, pl);
+                           u32 ea, u32 eb, u32 LB, double *acc, u32 *mask, ItemPlan &pl, Add &add) {
+  build_item_plan(s.P, ea, eb, p0, p1, 256, pl);
   const u32 tid = threadIdx.x, lane = tid & 31;
   const u32 nlong = min(pl.nlong, kListMax);
   for (u32 li = 0; li < nlong; li++) {
@@ -1018,8 +1007,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
     const Item item = a.items[it];
     const u32 t = item.tile;
     const u32 LB = a.tile_lb[t], used = a.tile_nrows[t] * LB;
-    dense_item<kSentinel>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, LB, acc, mask,
-                          plan, add);
+    dense_item<kSentinel>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, item.ea, item.eb, LB,
+                          acc, mask, plan, add);
     __syncthreads();
     if (a.hot) {
       merge_hot_dense<kSentinel>(acc, mask, priv, pmask, a.hot);
@@ -1085,10 +1074,10 @@ struct HashArgs {
 // of row urow[rank0] when TL == 1).
 __device__ void drain_hash(u64 *keys, double *vals, u64 nslots, u64 LB, u32 TL, u32 rank0, u32 nrows,
                            const u64 *__restrict__ urow, const Out &out, const Decode &dec, u32 *err,
-                           u32 *s_wcnt, u64 *s_base, u64 *s_rows) {
+                           u32 *s_wcnt, u64 *s_base, u64 *s_rows, u32 row_cap) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   // the tile's rows, staged once (the barrier after the count publishes them)
-  const bool cached = nrows <= kRowCache;
+  const bool cached = nrows <= row_cap;
   if (cached)
     for (u32 i = tid; i < nrows; i += blockDim.x) s_rows[i] = __ldg(&urow[rank0 + i]);
   const u64 spw = ((nslots + nwarps - 1) / nwarps + 31) & ~u64(31);
@@ -1179,10 +1168,11 @@ struct HashAdd {
   }
 };
 
-// kThreads 256 runs four CTAs per SM (small tables): independent items
-// overlap their barriers and memory latency.
+// kThreads 256 and 128 run four and up to eight CTAs per SM (small tables):
+// independent items overlap their barriers and memory latency.
 template <class ColT, int kThreads>
-__global__ void __launch_bounds__(kThreads, kThreads == 256 ? 4 : 1) k_contract_hash(HashArgs<ColT> a) {
+__global__ void __launch_bounds__(kThreads, kThreads == 128 ? 8 : kThreads == 256 ? 4 : 1)
+    k_contract_hash(HashArgs<ColT> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   // layout: hk[slots] | hv[slots] | priv[nwarps*hot] | pmask[nwarps*hot/32]
   u64 *hk = reinterpret_cast<u64 *>(smem);
@@ -1190,20 +1180,17 @@ __global__ void __launch_bounds__(kThreads, kThreads == 256 ? 4 : 1) k_contract_
   const u32 nwarps = blockDim.x >> 5, warp = threadIdx.x >> 5, pw = a.hot / 32;
   double *priv = hv + a.slots;
   u32 *pmask = reinterpret_cast<u32 *>(priv + size_t(nwarps) * a.hot);
-  __shared__ u32 s_item, s_chunk;
+  __shared__ u32 s_item;
   __shared__ u32 s_wcnt[32];
   __shared__ u64 s_base;
-  __shared__ u64 s_rows[kRowCache];
-  const int tid = threadIdx.x;
+  __shared__ HashPlan plan;
+  const int tid = threadIdx.x, lane = tid & 31;
   for (u32 i = tid; i < a.slots; i += blockDim.x) { hk[i] = kEmptyKey; hv[i] = 0.0; }
   for (u32 i = tid; i < nwarps * a.hot; i += blockDim.x) priv[i] = 0.0;
   for (u32 i = tid; i < nwarps * pw; i += blockDim.x) pmask[i] = 0u;
   for (;;) {
     const long long c0 = clock64();
-    if (tid == 0) {
-      s_item = atomicAdd(a.counter, 1u);
-      s_chunk = 0;
-    }
+    if (tid == 0) s_item = atomicAdd(a.counter, 1u);
     __syncthreads();
     const u32 it = s_item;
     if (it >= a.nitems) break;
@@ -1213,8 +1200,17 @@ __global__ void __launch_bounds__(kThreads, kThreads == 256 ? 4 : 1) k_contract_
     u32 hsl = 64;
     while (u64(hsl) < 2 * np && hsl < a.slots) hsl <<= 1;
     HashAdd add{hk, hv, hsl - 1, a.err, priv + size_t(warp) * a.hot, pmask + size_t(warp) * pw, a.hot};
-    products_item<ColT, u64>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, a.LB,
-                             &s_chunk, add);
+    // chunks of the item's multiply-adds, each starting at a known entry
+    build_item_plan(a.src.P, item.ea, item.eb, item.p0, item.p1, 256, plan);
+    for (;;) {
+      u32 c = 0;
+      if (lane == 0) c = atomicAdd(&plan.next, 1u);
+      c = __shfl_sync(kFull, c, 0);
+      if (c >= plan.nchunk) break;
+      const u64 q0 = item.p0 + u64(c) * plan.chunk, q1 = min(q0 + plan.chunk, item.p1);
+      products_chunk<ColT, u64>(a.src, a.colB, item.ea, item.eb, plan.start[c], q0, q1, item.p0, item.p1, kNoSkip,
+                                a.LB, add);
+    }
     __syncthreads();
     if (a.hot) {  // per-warp hot columns -> the table (their keys were counted in np)
       for (u32 i = tid; i < a.hot; i += blockDim.x) {
@@ -1234,7 +1230,7 @@ __global__ void __launch_bounds__(kThreads, kThreads == 256 ? 4 : 1) k_contract_
     const int sidx = a.split_of_tile[t];
     if (sidx < 0) {
       drain_hash(hk, hv, hsl, a.LB, a.TL, a.tile_rank0[t], a.tile_nrows[t], a.urow, a.out, a.dec, a.err, s_wcnt,
-                 &s_base, s_rows);
+                 &s_base, reinterpret_cast<u64 *>(plan.start), HashPlan::kRows);  // the plan is idle
     } else {
       const u64 off = a.hoff[t], hs = a.hsz[t];
       for (u32 s = tid; s < hsl; s += blockDim.x) {
@@ -1260,7 +1256,7 @@ __global__ void __launch_bounds__(kTileThreads) k_merge_hash(HashArgs<ColT> a) {
     const u32 t = a.split_tiles[s];
     const u64 off = a.hoff[t];
     drain_hash(a.gkeys + off, a.gvals + off, a.hsz[t], a.LB, a.TL, a.tile_rank0[t], a.tile_nrows[t], a.urow,
-               a.out, a.dec, a.err, s_wcnt, &s_base, s_rows);
+               a.out, a.dec, a.err, s_wcnt, &s_base, s_rows, kRowCache);
     __syncthreads();
   }
 }
@@ -1586,18 +1582,20 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   hc[FCC_CLASS_HASH_L] = {true, opt.tile_threads > 0 ? opt.tile_threads : 512,
                           opt.hash_slots > 0 ? u32(opt.hash_slots) : 8192u, 0, opt.accumulator != FCC_ACC_DENSE};
   hc[FCC_CLASS_HASH_M] = {true, 256, 4096u, 0, opt.accumulator != FCC_ACC_DENSE && !custom_hash};
-  hc[FCC_CLASS_HASH_S] = {true, 256, 2048u, 0, opt.accumulator != FCC_ACC_DENSE && !custom_hash};
+  hc[FCC_CLASS_HASH_S] = {true, 128, 2048u, 0, opt.accumulator != FCC_ACC_DENSE && !custom_hash};
   if (opt.accumulator == FCC_ACC_HASH) hc[FCC_CLASS_DENSE].enabled = false;
   if (hc[FCC_CLASS_DENSE].threads != 512 && hc[FCC_CLASS_DENSE].threads != 1024) {
-    if (opt.accumulator != FCC_ACC_HASH && hc[FCC_CLASS_DENSE].threads != 256)
-      throw Error{FCC_ERR_ARG, "tile_threads must be 256, 512 or 1024"};
-    if (opt.accumulator == FCC_ACC_DENSE) throw Error{FCC_ERR_ARG, "tile_threads 256 is for the hash accumulator"};
+    const int t = hc[FCC_CLASS_DENSE].threads;
+    if (opt.accumulator != FCC_ACC_HASH && t != 128 && t != 256)
+      throw Error{FCC_ERR_ARG, "tile_threads must be 128, 256, 512 or 1024"};
+    if (opt.accumulator == FCC_ACC_DENSE) throw Error{FCC_ERR_ARG, "tile_threads 128 and 256 are for the hash accumulator"};
     hc[FCC_CLASS_DENSE].enabled = false;
     hc[FCC_CLASS_DENSE].threads = kTileThreads;
   }
   {
     const int t = hc[FCC_CLASS_HASH_L].threads;
-    if (t != 256 && t != 512 && t != 1024) throw Error{FCC_ERR_ARG, "tile_threads must be 256, 512 or 1024"};
+    if (t != 128 && t != 256 && t != 512 && t != 1024)
+      throw Error{FCC_ERR_ARG, "tile_threads must be 128, 256, 512 or 1024"};
     const u32 hs = hc[FCC_CLASS_HASH_L].slots;
     if (hs & (hs - 1)) throw Error{FCC_ERR_ARG, "hash_slots must be a power of two"};
     if (size_t(hs) * 16 > smem_cap || hs < 64) throw Error{FCC_ERR_ARG, "hash_slots out of range"};
@@ -1894,12 +1892,14 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
         ha.item_cyc = item_cyc ? item_cyc + cbeg[c] : nullptr;
         const int threads = hc[c].threads;
         const size_t smem = class_smem(c, hot);
-        const void *kern = threads == 256   ? reinterpret_cast<const void *>(k_contract_hash<ColT, 256>)
+        const void *kern = threads == 128   ? reinterpret_cast<const void *>(k_contract_hash<ColT, 128>)
+                           : threads == 256 ? reinterpret_cast<const void *>(k_contract_hash<ColT, 256>)
                            : threads == 512 ? reinterpret_cast<const void *>(k_contract_hash<ColT, 512>)
                                             : reinterpret_cast<const void *>(k_contract_hash<ColT, 1024>);
         FCC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
         const int grid = grid_tiles(ctx, kern, threads, smem, ha.nitems, &ctas_per_sm[c]);
-        if (threads == 256) k_contract_hash<ColT, 256><<<grid, 256, smem, st>>>(ha);
+        if (threads == 128) k_contract_hash<ColT, 128><<<grid, 128, smem, st>>>(ha);
+        else if (threads == 256) k_contract_hash<ColT, 256><<<grid, 256, smem, st>>>(ha);
         else if (threads == 512) k_contract_hash<ColT, 512><<<grid, 512, smem, st>>>(ha);
         else k_contract_hash<ColT, 1024><<<grid, 1024, smem, st>>>(ha);
         FCC_LAUNCH_CHECK();

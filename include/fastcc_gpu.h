@@ -96,7 +96,8 @@ typedef struct fcc_options {
                                  smaller hint is not an error: the device counts every output
                                  and the call retries once with the exact count. */
   int32_t dense_mode;         /* fcc_dense_mode: how a dense tile marks touched positions */
-  int32_t tile_threads;       /* threads per tile CTA: 512 (default) or 1024 */
+  int32_t tile_threads;       /* threads per tile CTA: 512 (default) or 1024; 128 or 256 for the
+                                 hash accumulator */
   int32_t hot_columns;        /* per-warp copies of the most frequent B columns in row tiles:
                                  0 or -1 off (default), or a count (multiple of 32) */
   int32_t schedule;           /* fcc_schedule: how each output tile picks its class */
@@ -113,7 +114,7 @@ enum {
   FCC_CLASS_DENSE = 0,   /* shared-memory dense tile, 512 threads (tile_threads) */
   FCC_CLASS_HASH_L = 1,  /* hash, 8192 slots, 512 threads, one CTA per SM */
   FCC_CLASS_HASH_M = 2,  /* hash, 4096 slots, 256 threads */
-  FCC_CLASS_HASH_S = 3,  /* hash, 2048 slots, 256 threads */
+  FCC_CLASS_HASH_S = 3,  /* hash, 2048 slots, 128 threads */
   FCC_NUM_CLASSES = 4
 };
 
