@@ -385,6 +385,58 @@ def run_sweep(name, variants, reps=3):
                               "contract_ms": statistics.median(con)}), flush=True)
 
 
+def run_readme(steps, stream, local):
+    """The README contraction (256x64x256x64, 200k nnz, x 512x64x64, 100k
+    nnz over {1,3} x {1,2}): GPU ms per contraction (device-resident and end to
+    end through the C ABI) next to the CPU oracle on all host cores."""
+    import torch
+
+    import fastcc_gpu as F
+    import workloads
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    w = workloads.readme(seed=1)
+    a, b = w["a"], w["b"]
+    cuda = lambda t: F.Tensor(torch.from_numpy(t.coords).cuda(), torch.from_numpy(t.values).cuda(), t.max_index)
+    A, B = cuda(a), cuda(b)
+    ctx = F.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+
+    def timed(x, y, n):
+        for _ in range(3):
+            ctx.contract(x, y, w["ctr_a"], w["ctr_b"]).free()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            r = ctx.contract(x, y, w["ctr_a"], w["ctr_b"])
+            if x is not A:
+                r.to_numpy()
+            r.free()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    ms = timed(A, B, max(steps, 10))
+    ms_e2e = timed(a, b, 3)
+    r = ctx.contract(A, B, w["ctr_a"], w["ctr_b"])
+    prods, outs = r.products, r.nnz
+    r.free()
+    ctx.close()
+    threads = os.cpu_count() or 1
+    oracle.build()
+    cpu = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        oracle.fastcc_multiply(a.coords, a.values, a.max_index, b.coords, b.values, b.max_index, w["ctr_a"],
+                               w["ctr_b"], tile_size=128, nthreads=threads)
+        cpu.append(time.perf_counter() - t0)
+    cpu_ms = 1000 * statistics.median(cpu)
+    return {"workload": w["name"], "multiply_adds": prods, "outputs": outs, "gpu_ms": ms, "gpu_e2e_ms": ms_e2e,
+            "cpu_oracle_ms": cpu_ms, "cpu_threads": threads, "gpu_vs_cpu": cpu_ms / ms,
+            "gpu_e2e_vs_cpu": cpu_ms / ms_e2e}
+
+
 def run_batched(steps, warmup, stream, local):
     """The batched workload: 256 contractions of the readme pattern with
     uneven sizes. Times, per step, 256 sequential plain contractions and one
@@ -422,6 +474,14 @@ def run_batched(steps, warmup, stream, local):
         r.free()
         return n, p
 
+    learned_opts = F.Options(schedule=F.SCHED_LEARNED)
+
+    def batched_learned():
+        r, counts = ctx.contract_batch(As, Bs, ctr_a, ctr_b, learned_opts)
+        n, p = r.nnz, r.products
+        r.free()
+        return n, p
+
     def timed(fn, steps=steps):
         for _ in range(warmup):
             out = fn()
@@ -438,6 +498,11 @@ def run_batched(steps, warmup, stream, local):
     ms_plain, (n_plain, prods), l_plain = timed(plain)
     ms_batch, (n_batch, prods_b), l_batch = timed(batched)
     assert n_plain == n_batch and prods == prods_b, "batched and plain results differ in size"
+    ms_learned = None
+    if ctx.load_default_model():
+        ms_learned, (n_l, _), _ = timed(batched_learned)
+        assert n_l == n_batch, "learned schedule changed the output size"
+        ctx.sched_set_model(None)
 
     # end to end: pinned host operands, outputs copied to pinned host buffers
     host = []
@@ -485,6 +550,9 @@ def run_batched(steps, warmup, stream, local):
         "batched": {"ms_per_contraction": ms_batch / count, "multiply_adds_per_s": prods / (ms_batch / 1000.0),
                     "launches_per_step": l_batch,
                     "e2e_ms_per_contraction": ms_batch_e2e / count},
+        "batched_learned": None if ms_learned is None else {
+            "ms_per_contraction": ms_learned / count, "multiply_adds_per_s": prods / (ms_learned / 1000.0),
+            "speedup_vs_plain": ms_plain / ms_learned},
         "speedup": ms_plain / ms_batch, "e2e_speedup": ms_plain_e2e / ms_batch_e2e,
         "e2e_h2d_bytes_per_step": in_bytes,
         "e2e_d2h_bytes_per_step": {"plain": n_batch * ((order - 1) * 4 + 8), "batched": n_batch * (order * 4 + 8)},
@@ -661,6 +729,7 @@ def main():
     }
     if not args.no_batched:
         line["batched"] = run_batched(min(args.steps, 5), 3, stream, local)
+        line["readme"] = run_readme(args.steps, stream, local)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         # bounded sample: grow it (halve `every`) until one run takes >= 8 s
         every = 256

@@ -16,6 +16,9 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
               bool count_only, const u32 *group_lb, u32 ngroups);
 void contract_batch(Runtime *ctx, int n, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
                     const int32_t *ctrB, int k, const fcc_options &opt, fcc_result *res, i64 *counts);
+void contract_modes(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                    const int32_t *ctrB, int k, const int32_t *batchA, const int32_t *batchB, int nb,
+                    const fcc_options &opt, fcc_result *res);
 }
 
 namespace {
@@ -177,6 +180,22 @@ int fcc_contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const i
     std::unique_ptr<fcc_result> r(new fcc_result());
     r->ctx = ctx;
     fcc::contract(&rt, A, B, ctrA, ctrB, k, o, r.get(), nullptr, false, nullptr, 0);
+    *out = r.release();
+  });
+}
+
+int fcc_contract_modes(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                       const int32_t *ctrB, int32_t k, const int32_t *batchA, const int32_t *batchB, int32_t nb,
+                       const fcc_options *opts, fcc_result **out) {
+  if (!ctx || !out) return FCC_ERR_ARG;
+  *out = nullptr;
+  fcc_options o;
+  if (opts) o = *opts; else fcc_options_default(&o);
+  return guarded(ctx, [&] {
+    fcc::Runtime rt = runtime_of(ctx);
+    std::unique_ptr<fcc_result> r(new fcc_result());
+    r->ctx = ctx;
+    fcc::contract_modes(&rt, A, B, ctrA, ctrB, k, batchA, batchB, nb, o, r.get());
     *out = r.release();
   });
 }

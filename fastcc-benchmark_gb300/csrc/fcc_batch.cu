@@ -218,3 +218,92 @@ void contract_batch(Runtime *ctx, int n, const fcc_tensor *A, const fcc_tensor *
 }
 
 }  // namespace fcc
+
+// ---- batch modes inside one contraction ----
+//
+// fcc_contract_modes: modes shared by A and B that stay in the output, as in
+// the reference's Tensor<DT>::multiply(other, left_contr, left_batch,
+// right_contr, right_batch) (contract.hpp:284-367), whose output coordinate is
+// (batch coordinates in left_batch order, A's external modes, B's external
+// modes). Run as one contraction of
+//   A' = [A's batch modes in batchA order, A's modes...]
+// with ctrA' = [nb + batchA..., nb + ctrA...] and ctrB' = [batchB..., ctrB...]:
+// A' has the batch copies as its leading external modes, and the batch modes
+// join the contraction key so only equal batch coordinates meet.
+
+namespace fcc {
+namespace {
+
+struct ModeSrc {
+  int m[FCC_MAX_ORDER];
+};
+__global__ void k_gather_modes_v(const int32_t *__restrict__ coords, i64 sn, i64 sm, i64 nnz, int order_out,
+                                 ModeSrc src, int32_t *__restrict__ out) {
+  for (i64 r = i64(blockIdx.x) * blockDim.x + threadIdx.x; r < nnz; r += i64(gridDim.x) * blockDim.x)
+    for (int m = 0; m < order_out; m++) out[i64(m) * nnz + r] = coords[r * sn + i64(src.m[m]) * sm];
+}
+
+}  // namespace
+
+void contract_modes(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                    const int32_t *ctrB, int k, const int32_t *batchA, const int32_t *batchB, int nb,
+                    const fcc_options &opt, fcc_result *res) {
+  if (!A || !B) throw Error{FCC_ERR_ARG, "null operand"};
+  if (nb < 0 || (nb > 0 && (!batchA || !batchB))) throw Error{FCC_ERR_ARG, "bad batch modes"};
+  if (k < 0 || (k > 0 && (!ctrA || !ctrB))) throw Error{FCC_ERR_ARG, "bad contracted modes"};
+  const int dA = A->order, dB = B->order;
+  if (dA + nb > FCC_MAX_ORDER) throw Error{FCC_ERR_ARG, "order(A) + batch modes exceeds FCC_MAX_ORDER"};
+  if (A->nnz < 0 || (A->nnz > 0 && (!A->coords || !A->values)) || !A->max_index)
+    throw Error{FCC_ERR_ARG, "A without coords, values or max_index"};
+  for (int i = 0; i < nb; i++) {
+    if (batchA[i] < 0 || batchA[i] >= dA || batchB[i] < 0 || batchB[i] >= dB)
+      throw Error{FCC_ERR_ARG, "batch mode out of range"};
+    for (int j = 0; j < k; j++)
+      if (ctrA[j] == batchA[i] || ctrB[j] == batchB[i])
+        throw Error{FCC_ERR_ARG, "a mode is both contracted and batch"};
+  }
+  std::vector<void *> frees;
+  struct FreeAll {
+    std::vector<void *> &f;
+    cudaStream_t s;
+    ~FreeAll() {
+      for (void *p : f) cudaFreeAsync(p, s);
+    }
+  } free_all{frees, ctx->stream};
+  cudaStream_t st = ctx->stream;
+  const int dA2 = dA + nb;
+  ModeSrc src{};
+  std::vector<int32_t> mx(static_cast<size_t>(dA2));
+  for (int i = 0; i < nb; i++) src.m[i] = batchA[i];
+  for (int m = 0; m < dA; m++) src.m[nb + m] = m;
+  for (int m = 0; m < dA2; m++) mx[size_t(m)] = A->max_index[src.m[m]];
+  const i64 n = A->nnz;
+  int32_t *coords = nullptr;
+  const double *vals = A->values;
+  if (n > 0) {
+    const int32_t *cin = A->coords;
+    if (A->location == FCC_HOST) {  // stage host operands on the device
+      const i64 ext = (n - 1) * A->stride_nnz + i64(dA - 1) * A->stride_mode + 1;
+      void *p = pool_alloc(ctx->pool, sizeof(int32_t) * size_t(ext), st);
+      frees.push_back(p);
+      FCC_CUDA(cudaMemcpyAsync(p, A->coords, sizeof(int32_t) * size_t(ext), cudaMemcpyHostToDevice, st));
+      cin = static_cast<const int32_t *>(p);
+      p = pool_alloc(ctx->pool, sizeof(double) * size_t(n), st);
+      frees.push_back(p);
+      FCC_CUDA(cudaMemcpyAsync(p, A->values, sizeof(double) * size_t(n), cudaMemcpyHostToDevice, st));
+      vals = static_cast<const double *>(p);
+    }
+    void *p = pool_alloc(ctx->pool, sizeof(int32_t) * size_t(n) * dA2, st);
+    frees.push_back(p);
+    coords = static_cast<int32_t *>(p);
+    k_gather_modes_v<<<grid_for(n, 256), 256, 0, st>>>(cin, A->stride_nnz, A->stride_mode, n, dA2, src, coords);
+    FCC_LAUNCH_CHECK();
+  }
+  fcc_tensor TA{dA2, n, mx.data(), coords, 1, n, vals, FCC_DEVICE};
+  std::vector<int32_t> cA(size_t(nb + k)), cB(size_t(nb + k));
+  for (int i = 0; i < nb; i++) cA[size_t(i)] = nb + batchA[i], cB[size_t(i)] = batchB[i];
+  for (int i = 0; i < k; i++) cA[size_t(nb + i)] = nb + ctrA[i], cB[size_t(nb + i)] = ctrB[i];
+  contract(ctx, &TA, B, cA.data(), cB.data(), nb + k, opt, res, nullptr, false, nullptr, 0);
+}
+
+}  // namespace fcc

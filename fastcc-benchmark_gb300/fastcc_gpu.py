@@ -85,6 +85,8 @@ def lib():
                                          i32, ctypes.POINTER(Options), ctypes.POINTER(i64)]
         L.fcc_contract_batch.argtypes = [vp, i32, ctypes.POINTER(_CTensor), ctypes.POINTER(_CTensor), vp, vp,
                                          i32, ctypes.POINTER(Options), ctypes.POINTER(vp), vp]
+        L.fcc_contract_modes.argtypes = [vp, ctypes.POINTER(_CTensor), ctypes.POINTER(_CTensor), vp, vp, i32, vp,
+                                         vp, i32, ctypes.POINTER(Options), ctypes.POINTER(vp)]
         L.fcc_autotune.argtypes = [vp, ctypes.POINTER(_CTensor), ctypes.POINTER(_CTensor), vp, vp, i32,
                                    ctypes.POINTER(Options), i32, ctypes.POINTER(Options),
                                    ctypes.POINTER(ctypes.c_double)]
@@ -240,6 +242,22 @@ class Context:
                                 ca.ctypes.data if ca.size else None, cb.ctypes.data if cb.size else None,
                                 int(ca.size), ctypes.byref(o), ctypes.byref(out))
         self._check(rc)
+        return Result(self, out.value)
+
+    def contract_modes(self, a, b, ctr_a, ctr_b, batch_a, batch_b, opts=None):
+        """Contraction with batch modes (fcc_contract_modes; the reference's
+        Tensor::multiply(other, left_contr, left_batch, right_contr,
+        right_batch)): output modes = batch modes, A's external, B's external."""
+        arrs = [np.ascontiguousarray(x, dtype=np.int32) for x in (ctr_a, ctr_b, batch_a, batch_b)]
+        if arrs[0].shape != arrs[1].shape or arrs[2].shape != arrs[3].shape:
+            raise ValueError("mode lists differ in length")
+        ta, tb = a._struct(), b._struct()
+        out = ctypes.c_void_p()
+        o = opts if opts is not None else Options()
+        ptr = lambda x: x.ctypes.data if x.size else None
+        self._check(lib().fcc_contract_modes(self._h, ctypes.byref(ta), ctypes.byref(tb), ptr(arrs[0]), ptr(arrs[1]),
+                                             int(arrs[0].size), ptr(arrs[2]), ptr(arrs[3]), int(arrs[2].size),
+                                             ctypes.byref(o), ctypes.byref(out)))
         return Result(self, out.value)
 
     def contract_batch(self, As, Bs, ctr_a, ctr_b, opts=None):

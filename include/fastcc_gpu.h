@@ -192,6 +192,19 @@ int fcc_count_products(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B,
 int fcc_abi_version(void);
 
 /*
+ * Contraction with batch modes: modes batchA[i] of A and batchB[i] of B
+ * (nb pairs) are matched like contracted modes but kept in the output.
+ * Replaces Tensor<DT>::multiply(other, left_contr, left_batch, right_contr,
+ * right_batch) (contract.hpp:284-367) and its _inner_outer_multiply variant
+ * (contract.hpp:1356-1435): output coordinates are the batch modes in
+ * batchA order, then A's other non-contracted modes ascending, then B's.
+ * Needs order(A) + nb <= FCC_MAX_ORDER.
+ */
+int fcc_contract_modes(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                       const int32_t *ctrB, int32_t k, const int32_t *batchA, const int32_t *batchB,
+                       int32_t nb, const fcc_options *opts, fcc_result **out);
+
+/*
  * Batched contraction: n independent products A[t] x B[t] of one mode
  * pattern (every A[t] of one order, every B[t] of one order, the same ctrA,
  * ctrB, k), run as ONE pipeline: one index build, one tile plan and one

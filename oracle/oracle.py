@@ -142,6 +142,37 @@ def bruteforce(a_coords, a_vals, a_max, b_coords, b_vals, b_max, ctr_a, ctr_b):
     return _take(res, True)
 
 
+def multiply_batch_modes(a_coords, a_vals, b_coords, b_vals, ctr_a, ctr_b, batch_a, batch_b):
+    """Tensor<DT>::multiply(other, left_contr, left_batch, right_contr,
+    right_batch) (contract.hpp:284-367), restated with Python dictionaries for
+    small cases: A entries are grouped by (batch coordinates in left_batch
+    order, contracted coordinates) and joined with B's groups; each pair adds
+    a * b into the output (batch, A external, B external), externals in
+    ascending mode order (OutputCoordinate(batch, left, right).merge()).
+    Returns (coords (n, order) int64 sorted, values, sums of |a*b|)."""
+    a_coords = np.asarray(a_coords)
+    b_coords = np.asarray(b_coords)
+    ext_a = [m for m in range(a_coords.shape[1]) if m not in list(ctr_a) + list(batch_a)]
+    ext_b = [m for m in range(b_coords.shape[1]) if m not in list(ctr_b) + list(batch_b)]
+    groups = {}
+    for i in range(b_coords.shape[0]):
+        key = tuple(int(b_coords[i, m]) for m in list(batch_b) + list(ctr_b))
+        groups.setdefault(key, []).append(i)
+    acc, mag = {}, {}
+    for i in range(a_coords.shape[0]):
+        key = tuple(int(a_coords[i, m]) for m in list(batch_a) + list(ctr_a))
+        for j in groups.get(key, ()):
+            out = key[:len(batch_a)] + tuple(int(a_coords[i, m]) for m in ext_a) + \
+                tuple(int(b_coords[j, m]) for m in ext_b)
+            p = float(a_vals[i]) * float(b_vals[j])
+            acc[out] = acc.get(out, 0.0) + p
+            mag[out] = mag.get(out, 0.0) + abs(p)
+    order = len(batch_a) + len(ext_a) + len(ext_b)
+    keys = sorted(acc)
+    coords = np.array(keys, np.int64).reshape(len(keys), order)
+    return coords, np.array([acc[k] for k in keys]), np.array([mag[k] for k in keys])
+
+
 def count_products(a_coords, a_vals, a_max, b_coords, b_vals, b_max, ctr_a, ctr_b):
     ka, kb = _Keep(a_coords, a_vals, a_max), _Keep(b_coords, b_vals, b_max)
     ca = np.ascontiguousarray(ctr_a, np.int32)

@@ -96,3 +96,35 @@ def test_oracle_rejects_bad_arguments():
         oracle.fastcc_multiply(c, v, m, c, v, m, [0, 0], [0, 1])  # repeated mode
     with pytest.raises(ValueError):
         oracle.fastcc_multiply(c, v, m, c, v, m, [2], [0])  # out of range
+
+
+def test_batch_mode_restatement_reduces_to_fastcc_and_to_batched_slices():
+    """oracle.multiply_batch_modes (Tensor::multiply, contract.hpp:284-367):
+    without batch modes it equals fastcc_multiply; with one it equals the
+    per-batch-index fastcc_multiply of the slices, batch index prepended."""
+    import oracle
+    rng = np.random.Generator(np.random.PCG64(55))
+    ea, eb = [5, 4, 6], [6, 4, 3]  # A(b, i, k), B(k, b, j)
+    la = rng.choice(np.prod(ea), 60, replace=False)
+    lb = rng.choice(np.prod(eb), 40, replace=False)
+    ac = np.stack(np.unravel_index(la, ea), 1).astype(np.int32)
+    bc = np.stack(np.unravel_index(lb, eb), 1).astype(np.int32)
+    av, bv = rng.uniform(-1, 1, 60), rng.uniform(-1, 1, 40)
+    c0, v0, _ = oracle.multiply_batch_modes(ac, av, bc, bv, [2], [0], [], [])
+    o = oracle.fastcc_multiply(ac, av, np.array(ea) - 1, bc, bv, np.array(eb) - 1, [2], [0])
+    idx = np.lexsort(o["coords"].T[::-1])
+    assert np.array_equal(c0, o["coords"][idx].astype(np.int64))
+    assert np.allclose(v0, o["values"][idx], rtol=1e-12, atol=1e-15)
+    c1, v1, _ = oracle.multiply_batch_modes(ac, av, bc, bv, [2], [0], [0], [1])
+    rows = []
+    for bidx in range(ea[0]):
+        sa, sb = ac[ac[:, 0] == bidx], bc[bc[:, 1] == bidx]
+        if len(sa) == 0 or len(sb) == 0:
+            continue
+        va, vb = av[ac[:, 0] == bidx], bv[bc[:, 1] == bidx]
+        c, v, _ = oracle.multiply_batch_modes(sa[:, 1:], va, sb[:, [0, 2]], vb, [1], [0], [], [])
+        for k in range(len(v)):
+            rows.append(((bidx,) + tuple(c[k]), v[k]))
+    rows.sort()
+    assert np.array_equal(c1, np.array([r[0] for r in rows], np.int64).reshape(len(rows), 3))
+    assert np.allclose(v1, [r[1] for r in rows], rtol=1e-12)
