@@ -25,6 +25,13 @@ namespace {
 
 thread_local std::string g_last_error;  // errors without a context
 
+// SoA result coordinates (mode m at in[m * cap + i]) -> row-major out[i * order + m].
+__global__ void k_interleave(const uint32_t *__restrict__ in, int64_t cap, int order, int64_t n,
+                             uint32_t *__restrict__ out) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    for (int m = 0; m < order; m++) out[i * order + m] = in[int64_t(m) * cap + i];
+}
+
 fcc::Runtime runtime_of(fcc_ctx *ctx) {
   fcc::Runtime rt(ctx->arena);
   rt.stream = ctx->stream;
@@ -382,6 +389,14 @@ int fcc_result_copy_to_host(const fcc_result *r, int32_t *coords, int64_t stride
           FCC_CUDA(cudaMemcpyAsync(coords + m * stride_mode, r->d_coords + m * r->cap, sizeof(uint32_t) * n,
                                    cudaMemcpyDeviceToHost, s));
         FCC_CUDA(cudaStreamSynchronize(s));
+      } else if (stride_mode == 1 && stride_nnz == r->order) {
+        // row-major (the drop-in's ListTensor): interleave on the device, one copy out
+        void *p = fcc::pool_alloc(ctx->pool, sizeof(uint32_t) * size_t(n) * r->order, s);
+        k_interleave<<<fcc::grid_for(n, 256), 256, 0, s>>>(r->d_coords, r->cap, r->order, n,
+                                                           static_cast<uint32_t *>(p));
+        FCC_LAUNCH_CHECK();
+        FCC_CUDA(cudaMemcpyAsync(coords, p, sizeof(uint32_t) * size_t(n) * r->order, cudaMemcpyDeviceToHost, s));
+        FCC_CUDA(cudaFreeAsync(p, s));
       } else {
         std::vector<uint32_t> tmp(size_t(n) * r->order);
         for (int m = 0; m < r->order; m++)

@@ -1603,8 +1603,10 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   {
     u64 pd = opt.products_per_item > 0 ? u64(opt.products_per_item) : (u64(1) << 20);
     hc[FCC_CLASS_DENSE].pmax = std::min<u64>(pd, u64(kListMax) * kCtaRun);
+    // an item's distinct outputs never exceed its multiply-adds, and the probe
+    // loop covers the whole table: 3/4 of the slots bounds the load at 0.75
     for (int c = FCC_CLASS_HASH_L; c < FCC_NUM_CLASSES; c++) {
-      const u64 cap = hc[c].slots / 2;
+      const u64 cap = hc[c].slots / 4 * 3;
       hc[c].pmax = opt.products_per_item > 0 ? std::min<u64>(u64(opt.products_per_item), cap) : cap;
     }
   }
