@@ -721,12 +721,195 @@ __device__ void build_item_plan(const u64 *__restrict__ P, u32 ea, u32 eb, u64 p
   __syncthreads();
 }
 
+// ---- phase 1 with bulk-copy staging ----
+//
+// Warp 0 (one lane) produces: it reads each long entry's metadata and copies
+// the entry's B segment, in chunks of kStageCh multiply-adds, from global
+// memory into a ring of kStageBufs shared-memory buffers with cp.async.bulk,
+// completion tracked by an mbarrier per buffer ("full"). The other warps
+// consume: wait for a chunk, apply its plain FMA read-modify-writes, and
+// release the buffer through a second mbarrier ("empty", one arrival per
+// consumer warp). Chunks of one entry touch distinct columns, so consumers
+// wait for each other only where a new entry starts. The producer runs up
+// to kStageBufs chunks ahead, so segment loads and entry metadata overlap the
+// accumulation. Every wait, including the consumers' wait between entries,
+// is an mbarrier poll with a bounded count; on timeout the kernel flags
+// ERRB_INTERNAL, stops issuing, waits (bounded) for its copies in flight and
+// skips its remaining work.
+constexpr u32 kStageCh = 2048;
+constexpr u32 kStageBufs = 2;
+constexpr u32 kStageValBytes = (kStageCh + 2) * 8;  // 16-byte multiple: room for a 1-element head
+constexpr u32 kStageColBytes = (kStageCh + 4) * 4;  // 16-byte multiple: room for a 3-element head
+constexpr u32 kStageBufBytes = kStageValBytes + kStageColBytes;
+constexpr u32 kStageBytes = kStageBufs * kStageBufBytes;
+constexpr long long kWaitPolls = 1ll << 24;
+
+struct StageHdr {  // one staged chunk (written by the producer before the copies)
+  double va;
+  u32 base, cnt, sc, sv;  // tile offset of the entry's row, multiply-adds, col / val head skip
+  u32 first, more;        // first chunk of an entry after the item's first; another chunk follows
+};
+
+struct StageCtl {
+  unsigned long long full[kStageBufs], empty[kStageBufs];
+  StageHdr hdr[kStageBufs];
+  u32 seq;    // chunks staged so far by this CTA (sets buffer and mbarrier parity)
+  u32 fail;   // a wait timed out: skip the remaining work
+};
+
+__device__ __forceinline__ u32 smem_addr(const void *p) { return u32(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, u32 parity) {
+  const u32 a = smem_addr(bar);
+  for (long long it = 0; it < kWaitPolls; it++) {
+    u32 done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done) : "r"(a), "r"(parity) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void stage_init(StageCtl &c, u32 consumers) {
+  if (threadIdx.x == 0) {
+    for (u32 b = 0; b < kStageBufs; b++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&c.full[b])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&c.empty[b])), "r"(consumers)
+                   : "memory");
+    }
+    c.seq = 0;
+    c.fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, u32 bytes, unsigned long long *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+// Phase 1 of a dense item with staging (all threads call; ends with a barrier).
+template <bool kSentinel>
+__device__ void dense_phase1_staged(const ProdSrc &s, const u32 *__restrict__ colB, u64 p0, u64 p1, u32 LB,
+                                    double *acc, u32 *mask, const ItemPlan &pl, unsigned char *stage,
+                                    StageCtl &ctl, u32 *err) {
+  const u32 nlong = min(pl.nlong, kListMax);
+  const u32 tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const u32 nconsumers = blockDim.x - 32;
+  u32 seq = ctl.seq;  // every role advances it by one per chunk
+  if (nlong == 0 || ctl.fail) {
+    __syncthreads();
+    return;
+  }
+  if (warp == 0) {
+    if (lane == 0) {  // producer
+      bool ok = true;
+      u32 issued_last[kStageBufs];
+      bool issued[kStageBufs] = {};
+      // entry metadata one entry ahead: its loads overlap this entry's copies
+      u32 e = pl.list[0];
+      u64 npb = __ldg(&s.P[e]), npe = __ldg(&s.P[e + 1]);
+      double nva = __ldg(&s.valA[e]);
+      u32 nslot = __ldg(&s.slotA[e]), nsb = __ldg(&s.sbA[e]);
+      for (u32 li = 0; li < nlong && ok; li++) {
+        const u64 pb = npb;
+        const u64 lo = max(pb, p0), hi = min(npe, p1);
+        const double va = nva;
+        const u32 base = nslot * LB;
+        const u32 b0 = nsb + u32(lo - pb);
+        const u32 n = u32(hi - lo);
+        if (li + 1 < nlong) {
+          e = pl.list[li + 1];
+          npb = __ldg(&s.P[e]);
+          npe = __ldg(&s.P[e + 1]);
+          nva = __ldg(&s.valA[e]);
+          nslot = __ldg(&s.slotA[e]);
+          nsb = __ldg(&s.sbA[e]);
+        }
+        for (u32 off = 0; off < n; off += kStageCh, seq++) {
+          const u32 b = seq % kStageBufs;
+          if (seq >= kStageBufs && !mbar_wait(&ctl.empty[b], ((seq / kStageBufs) - 1) & 1)) {
+            ok = false;
+            break;
+          }
+          const u32 cnt = min(kStageCh, n - off), g = b0 + off;
+          const u32 sc = g & 3u, sv = g & 1u;
+          const u32 cbytes = ((sc + cnt + 3u) & ~3u) * 4u, vbytes = ((sv + cnt + 1u) & ~1u) * 8u;
+          StageHdr &h = ctl.hdr[b];
+          h.va = va;
+          h.base = base;
+          h.cnt = cnt;
+          h.sc = sc;
+          h.sv = sv;
+          h.first = (off == 0 && li > 0) ? 1u : 0u;
+          h.more = (li + 1 < nlong || off + kStageCh < n) ? 1u : 0u;
+          unsigned char *buf = stage + b * kStageBufBytes;
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&ctl.full[b])),
+                       "r"(cbytes + vbytes)
+                       : "memory");
+          bulk_g2s(buf, s.valB + (g - sv), vbytes, &ctl.full[b]);
+          bulk_g2s(buf + kStageValBytes, colB + (g - sc), cbytes, &ctl.full[b]);
+          issued[b] = true;
+          issued_last[b] = seq;
+        }
+      }
+      if (!ok) {  // stop; let the copies in flight land before the buffers are reused
+        atomicOr(err, ERRB_INTERNAL);
+        ctl.fail = 1;
+        for (u32 b = 0; b < kStageBufs; b++)
+          if (issued[b]) mbar_wait(&ctl.full[b], (issued_last[b] / kStageBufs) & 1);
+      }
+      ctl.seq = seq;
+    }
+  } else {  // consumers
+    const u32 ctid = tid - 32;
+    for (;;) {
+      const u32 b = seq % kStageBufs;
+      if (!mbar_wait(&ctl.full[b], (seq / kStageBufs) & 1)) {
+        atomicOr(err, ERRB_INTERNAL);
+        ctl.fail = 1;
+        break;
+      }
+      const StageHdr h = ctl.hdr[b];
+      // a new entry may share columns with the previous one: wait until every
+      // consumer warp has released the previous chunk (a bounded wait, unlike
+      // a named barrier)
+      if (h.first) {
+        const u32 pseq = seq - 1, pb = pseq % kStageBufs;
+        if (!mbar_wait(&ctl.empty[pb], (pseq / kStageBufs) & 1)) {
+          atomicOr(err, ERRB_INTERNAL);
+          ctl.fail = 1;
+          break;
+        }
+      }
+      const double *val = reinterpret_cast<const double *>(stage + b * kStageBufBytes) + h.sv;
+      const u32 *col = reinterpret_cast<const u32 *>(stage + b * kStageBufBytes + kStageValBytes) + h.sc;
+      for (u32 i = ctid; i < h.cnt; i += nconsumers) {
+        const u32 q = h.base + col[i];
+        acc[q] = fma(h.va, val[i], acc[q]);
+        if (!kSentinel) atomicOr(&mask[q >> 5], 1u << (q & 31));
+      }
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&ctl.empty[b])) : "memory");
+      seq++;
+      if (!h.more) break;
+    }
+  }
+  __syncthreads();
+}
+
 template <bool kSentinel, class Add>
 __device__ void dense_item(const ProdSrc &s, const u32 *__restrict__ colB, u32 alo, u32 ahi, u64 p0, u64 p1,
-                           u32 ea, u32 eb, u32 LB, double *acc, u32 *mask, ItemPlan &pl, Add &add) {
+                           u32 ea, u32 eb, u32 LB, double *acc, u32 *mask, ItemPlan &pl, Add &add,
+                           unsigned char *stage, StageCtl &ctl, u32 *err) {
   build_item_plan(s.P, ea, eb, p0, p1, 256, pl);
   const u32 tid = threadIdx.x, lane = tid & 31;
-  const u32 nlong = min(pl.nlong, kListMax);
+  const u32 nlong = stage ? 0u : min(pl.nlong, kListMax);
+  if (stage) dense_phase1_staged<kSentinel>(s, colB, p0, p1, LB, acc, mask, pl, stage, ctl, err);
   for (u32 li = 0; li < nlong; li++) {
     const u32 e = pl.list[li];
     const u64 pb = __ldg(&s.P[e]);
@@ -791,6 +974,7 @@ struct DenseArgs {
   Decode dec;
   u32 *err;
   u64 *item_cyc;  // per item: SM cycles from fetch to drained (NULL: not recorded)
+  u32 stage_off;  // byte offset of phase 1's staging ring in dynamic shared memory; 0: no staging
 };
 
 // The touched mask of positions [32w, 32w+32) of a dense tile, in every lane.
@@ -989,7 +1173,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
   __shared__ u32 s_cnt[1024];
   __shared__ u64 s_base;
   __shared__ ItemPlan plan;
+  __shared__ StageCtl ctl;
   const int tid = threadIdx.x;
+  unsigned char *stage = a.stage_off ? smem + a.stage_off : nullptr;
+  if (stage) stage_init(ctl, nwarps - 1);
   const double init = kSentinel ? __longlong_as_double((long long)kNegZero) : 0.0;
   for (u32 i = tid; i < a.area; i += blockDim.x) acc[i] = init;
   if (!kSentinel)
@@ -1008,7 +1195,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
     const u32 t = item.tile;
     const u32 LB = a.tile_lb[t], used = a.tile_nrows[t] * LB;
     dense_item<kSentinel>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, item.ea, item.eb, LB,
-                          acc, mask, plan, add);
+                          acc, mask, plan, add, stage, ctl, a.err);
     __syncthreads();
     if (a.hot) {
       merge_hot_dense<kSentinel>(acc, mask, priv, pmask, a.hot);
@@ -1168,10 +1355,11 @@ struct HashAdd {
   }
 };
 
-// kThreads 256 and 128 run four and up to eight CTAs per SM (small tables):
-// independent items overlap their barriers and memory latency.
+// kThreads 256 and 128 run three and six CTAs per SM (the shared-memory
+// limits of the 4096- and 2048-slot tables): independent items overlap their
+// barriers and memory latency.
 template <class ColT, int kThreads>
-__global__ void __launch_bounds__(kThreads, kThreads == 128 ? 8 : kThreads == 256 ? 4 : 1)
+__global__ void __launch_bounds__(kThreads, kThreads == 128 ? 6 : kThreads == 256 ? 3 : 1)
     k_contract_hash(HashArgs<ColT> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   // layout: hk[slots] | hv[slots] | priv[nwarps*hot] | pmask[nwarps*hot/32]
@@ -1502,8 +1690,9 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   radix_sort_pairs(keyB, permB, nB, bits_for(sb.keyspace - 1), ar, st);
 
   const bool colb32 = sb.span <= 0xFFFFFFFFull;
-  double *valB = ar.get_n<double>(nB);
-  void *colB = colb32 ? static_cast<void *>(ar.get_n<u32>(nB)) : static_cast<void *>(ar.get_n<u64>(nB));
+  // padded: staged copies round their end up to 16 bytes
+  double *valB = ar.get_n<double>(nB + 2);
+  void *colB = colb32 ? static_cast<void *>(ar.get_n<u32>(nB + 4)) : static_cast<void *>(ar.get_n<u64>(nB));
   if (colb32)
     k_gather_b<u32><<<grid_for(nB, 256), 256, 0, st>>>(permB, extB, sb.vals, nB, static_cast<u32 *>(colB), valB,
                                                        sc32(S_TINY));
@@ -1621,6 +1810,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
                                  : "the forced hash class is disabled by hash_slots or tile_threads"};
   if (custom_hash && forced < 0 && opt.accumulator == FCC_ACC_HASH) forced = FCC_CLASS_HASH_L;
   if (opt.dense_fill_log2 < 0 || opt.dense_fill_log2 > 40) throw Error{FCC_ERR_ARG, "dense_fill_log2 out of range"};
+  if (opt.dense_staging < -1 || opt.dense_staging > 0) throw Error{FCC_ERR_ARG, "dense_staging must be -1 or 0"};
   const bool learned = forced < 0 && opt.schedule == FCC_SCHED_LEARNED && ctx->sched && ctx->sched->model;
   const bool want_record = opt.timing == 2 && ctx->sched;
   // Row groups (batched contractions): dense tiles hold rows of one group,
@@ -1859,10 +2049,16 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     DenseArgs da{items + cbeg[FCC_CLASS_DENSE], ccount[FCC_CLASS_DENSE], counters + FCC_CLASS_DENSE, tile_abeg,
                  tile_rank0, tile_lb, tile_nrows, urow, split_of_tile, split_tiles_d, nsplit_d, src,
                  static_cast<const u32 *>(colB), u32(area), u32(words), hot, gacc, gmask, o, dec, ctx->d_err,
-                 item_cyc ? item_cyc + cbeg[FCC_CLASS_DENSE] : nullptr};
+                 item_cyc ? item_cyc + cbeg[FCC_CLASS_DENSE] : nullptr, 0u};
     if (ccount[FCC_CLASS_DENSE]) {
       const int threads = hc[FCC_CLASS_DENSE].threads;
-      const size_t smem = class_smem(FCC_CLASS_DENSE, hot);
+      size_t smem = class_smem(FCC_CLASS_DENSE, hot);
+      // phase 1's staging ring, when it fits beside the tile
+      const size_t soff = (smem + 15) & ~size_t(15);
+      if (opt.dense_staging >= 0 && soff + kStageBytes <= dense_dyn_cap) {
+        da.stage_off = u32(soff);
+        smem = soff + kStageBytes;
+      }
       const void *kern;
       if (threads == 512) kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true, 512>)
                                           : reinterpret_cast<const void *>(k_contract_dense<false, 512>);

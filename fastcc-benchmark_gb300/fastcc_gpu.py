@@ -53,7 +53,8 @@ class Options(ctypes.Structure):
                 ("pad0", ctypes.c_int32), ("capacity_hint", ctypes.c_int64),
                 ("dense_mode", ctypes.c_int32), ("tile_threads", ctypes.c_int32),
                 ("hot_columns", ctypes.c_int32), ("schedule", ctypes.c_int32),
-                ("dense_fill_log2", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("dense_fill_log2", ctypes.c_int32), ("dense_staging", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
 
     def __init__(self, **kw):
         super().__init__()

@@ -104,7 +104,10 @@ typedef struct fcc_options {
   int32_t dense_fill_log2;    /* FCC_SCHED_RULE: a tile takes the dense class only when its
                                  multiply-adds >= its area / 2^dense_fill_log2; 0 = whenever
                                  the tile fits the dense accumulator */
-  int32_t reserved[3];
+  int32_t dense_staging;      /* 0: dense tiles stage the B segments of long A entries in shared
+                                 memory with bulk copies when the ring fits beside the tile;
+                                 -1: never */
+  int32_t reserved[2];
 } fcc_options;
 
 /* Tile classes: every output tile runs in one of them. The hash classes

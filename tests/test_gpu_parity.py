@@ -244,3 +244,18 @@ def test_launch_counter_counts_kernels(ctx):
     before = F.launch_count()
     ctx.fastcc_multiply(w["a"], w["b"], w["ctr_a"], w["ctr_b"])
     assert F.launch_count() - before >= 10
+
+
+@pytest.mark.parametrize("staging", [0, -1])
+def test_staged_phase1_matches_oracle(ctx, staging):
+    # B span 16,000: one-row dense tiles with room for the staging ring; Zipf hub
+    # segments of thousands of entries put most multiply-adds in phase 1
+    w = workloads.zipf3(seed=41, nnz=150_000, dims=(16_000, 16_000, 400))
+    a, b = w["a"], w["b"]
+    args = (a.coords, a.values, a.max_index, b.coords, b.values, b.max_index, w["ctr_a"], w["ctr_b"])
+    o = run_oracle(*args, tile=128)
+    for opts in ({"dense_staging": staging}, {"dense_staging": staging, "dense_mode": F.DENSE_BITMASK},
+                 {"dense_staging": staging, "products_per_item": 3000}):
+        c, v, prods = run_gpu(ctx, *args, **opts)
+        assert prods == o["products"]
+        check_parity(c, v, o["coords"], o["values"], o["abs_sum"])
