@@ -191,6 +191,35 @@ int fcc_contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const i
   });
 }
 
+int fcc_contract_into(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                      const int32_t *ctrB, int32_t k, const fcc_options *opts, uint32_t *out_coords,
+                      int64_t out_mode_stride, double *out_values, int64_t out_capacity, int64_t *out_nnz,
+                      int64_t *out_products) {
+  if (!ctx || !out_nnz) return FCC_ERR_ARG;
+  *out_nnz = 0;
+  if (out_products) *out_products = 0;
+  if (out_capacity < 0 || (out_capacity > 0 && (!out_values || out_mode_stride < out_capacity)))
+    return FCC_ERR_ARG;
+  fcc_options o;
+  if (opts) o = *opts; else fcc_options_default(&o);
+  o.capacity_hint = 0;
+  fcc_result res;
+  res.ctx = ctx;
+  const int st = guarded(ctx, [&] {
+    fcc::Runtime rt = runtime_of(ctx);
+    rt.out_coords = out_coords;
+    rt.out_stride = out_mode_stride;
+    rt.out_vals = out_values;
+    rt.out_cap = fcc::u64(out_capacity);
+    rt.caller_out = true;
+    fcc::i64 products = 0;
+    fcc::contract(&rt, A, B, ctrA, ctrB, k, o, &res, &products, false, nullptr, 0);
+    if (out_products) *out_products = products;
+  });
+  *out_nnz = res.nnz;  // on FCC_ERR_CAPACITY: the entries the output needs
+  return st;
+}
+
 int fcc_contract_modes(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
                        const int32_t *ctrB, int32_t k, const int32_t *batchA, const int32_t *batchB, int32_t nb,
                        const fcc_options *opts, fcc_result **out) {

@@ -1613,7 +1613,7 @@ struct Timing {
 // The whole contraction. count_only stops after the segment lookup and
 // returns the multiply-add count in *products. res (NULL when count_only)
 // receives the output; its buffers come from ctx->pool, or are the caller's
-// buffers of ctx when ctx->pool is NULL. group_lb (ngroups entries, may be
+// buffers (ctx->out_*) when ctx->caller_out is set or there is no pool. group_lb (ngroups entries, may be
 // NULL) makes A's leading external index a group index: rows of group g use
 // B columns [0, group_lb[g]) only, and dense tiles are sized per group.
 void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
@@ -1642,7 +1642,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
 
   if (!count_only) {
     res->order = out_order;
-    res->owned = ctx->pool != nullptr;
+    res->owned = !(ctx->caller_out || !ctx->pool);
   }
   struct Cleanup {
     fcc_result *r;
@@ -2022,10 +2022,15 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (opt.capacity_hint > 0) cap = std::min<u64>(cap, u64(opt.capacity_hint));
 
   int ctas_per_sm[FCC_NUM_CLASSES] = {};
-  if (!ctx->pool) cap = ctx->out_cap;  // caller buffers: their capacity, no retry
+  const bool caller_out = ctx->caller_out || !ctx->pool;
+  if (caller_out) {  // caller buffers: their capacity, no retry
+    cap = ctx->out_cap;
+    if (cap > 0 && (!ctx->out_vals || (out_order > 0 && (!ctx->out_coords || ctx->out_stride < i64(cap)))))
+      throw Error{FCC_ERR_ARG, "output buffers missing or mode stride below the capacity"};
+  }
   for (int attempt = 0;; attempt++) {
     i64 stride = i64(cap);
-    if (ctx->pool) {
+    if (!caller_out) {
       res->d_vals = static_cast<double *>(pool_alloc(ctx->pool, sizeof(double) * cap, st));
       if (out_order > 0) res->d_coords = static_cast<u32 *>(pool_alloc(ctx->pool, sizeof(u32) * cap * out_order, st));
     } else {
@@ -2122,7 +2127,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       res->nnz = i64(produced);
       break;
     }
-    if (!ctx->pool) {
+    if (caller_out) {
       res->nnz = i64(produced);  // tells the caller the capacity it needs
       throw Error{FCC_ERR_CAPACITY, "the output needs " + std::to_string(produced) + " entries, the buffers hold " +
                                         std::to_string(cap)};

@@ -120,6 +120,7 @@ struct Runtime {
   i64 out_stride = 0;
   double *out_vals = nullptr;
   u64 out_cap = 0;
+  bool caller_out = false;         // write the output into out_* (any device-accessible memory)
   SchedIo *sched = nullptr;        // NULL: no learned schedule and no per-tile record
 };
 

@@ -94,6 +94,7 @@ extern "C" int fcc_contract_noalloc(const fcc_tensor *A, const fcc_tensor *B, co
     rt.out_stride = out_mode_stride;
     rt.out_vals = out_values;
     rt.out_cap = fcc::u64(out_capacity);
+    rt.caller_out = true;
     fcc_options o;
     if (opts) {
       o = *opts;

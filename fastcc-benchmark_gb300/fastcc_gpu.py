@@ -86,6 +86,9 @@ def lib():
                                          i32, ctypes.POINTER(Options), ctypes.POINTER(i64)]
         L.fcc_contract_batch.argtypes = [vp, i32, ctypes.POINTER(_CTensor), ctypes.POINTER(_CTensor), vp, vp,
                                          i32, ctypes.POINTER(Options), ctypes.POINTER(vp), vp]
+        L.fcc_contract_into.argtypes = [vp, ctypes.POINTER(_CTensor), ctypes.POINTER(_CTensor), vp, vp, i32,
+                                        ctypes.POINTER(Options), vp, i64, vp, i64, ctypes.POINTER(i64),
+                                        ctypes.POINTER(i64)]
         L.fcc_contract_modes.argtypes = [vp, ctypes.POINTER(_CTensor), ctypes.POINTER(_CTensor), vp, vp, i32, vp,
                                          vp, i32, ctypes.POINTER(Options), ctypes.POINTER(vp)]
         L.fcc_autotune.argtypes = [vp, ctypes.POINTER(_CTensor), ctypes.POINTER(_CTensor), vp, vp, i32,
@@ -244,6 +247,34 @@ class Context:
                                 int(ca.size), ctypes.byref(o), ctypes.byref(out))
         self._check(rc)
         return Result(self, out.value)
+
+    def contract_into(self, a, b, ctr_a, ctr_b, out_coords, out_values, opts=None):
+        """fcc_contract_into: the output written into caller buffers, out_coords
+        (order, capacity) int32/uint32 and out_values (capacity,) float64, as
+        numpy arrays in pinned host memory (the kernels write them directly)
+        or CUDA torch tensors. Returns (entries, multiply-adds); raises
+        FccError(FCC_ERR_CAPACITY) with .needed when they do not fit."""
+        ca = np.ascontiguousarray(ctr_a, dtype=np.int32)
+        cb = np.ascontiguousarray(ctr_b, dtype=np.int32)
+        ta, tb = a._struct(), b._struct()
+        if isinstance(out_values, np.ndarray):
+            cptr, vptr = out_coords.ctypes.data, out_values.ctypes.data
+            stride = out_coords.strides[0] // 4 if out_coords.ndim == 2 else out_values.shape[0]
+        else:
+            cptr, vptr = out_coords.data_ptr(), out_values.data_ptr()
+            stride = out_coords.stride(0) if out_coords.dim() == 2 else out_values.shape[0]
+        cap = int(out_values.shape[0])
+        n, p = ctypes.c_int64(), ctypes.c_int64()
+        o = opts if opts is not None else Options()
+        rc = lib().fcc_contract_into(self._h, ctypes.byref(ta), ctypes.byref(tb),
+                                     ca.ctypes.data if ca.size else None, cb.ctypes.data if cb.size else None,
+                                     int(ca.size), ctypes.byref(o), cptr or None, stride, vptr or None, cap,
+                                     ctypes.byref(n), ctypes.byref(p))
+        if rc != 0:
+            err = FccError(rc, lib().fcc_last_error(self._h).decode())
+            err.needed = n.value
+            raise err
+        return n.value, p.value
 
     def contract_modes(self, a, b, ctr_a, ctr_b, batch_a, batch_b, opts=None):
         """Contraction with batch modes (fcc_contract_modes; the reference's

@@ -170,6 +170,22 @@ int fcc_options_default(fcc_options *opts);
 int fcc_contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
                  const int32_t *ctrB, int32_t k, const fcc_options *opts, fcc_result **out);
 
+/*
+ * The contraction written into the caller's buffers: coords (mode m at
+ * out_coords[m * out_mode_stride + i], uint32, out_mode_stride >=
+ * out_capacity) and out_values, out_capacity entries, in any memory the
+ * device can write: device memory, or pinned host memory, in which case the
+ * tile kernels stream the output to the host while they compute (no separate
+ * copy afterwards). Entry order is unspecified. Returns FCC_ERR_CAPACITY with
+ * *out_nnz = the entries needed when the output does not fit (the buffers'
+ * contents are then undefined). No counterpart in the reference, whose
+ * output goes to a host list.
+ */
+int fcc_contract_into(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const int32_t *ctrA,
+                      const int32_t *ctrB, int32_t k, const fcc_options *opts, uint32_t *out_coords,
+                      int64_t out_mode_stride, double *out_values, int64_t out_capacity, int64_t *out_nnz,
+                      int64_t *out_products);
+
 /* Result access. Replaces ListTensor's compute_nnz_count/run_through_nnz
  * (index_tensors.hpp:105-114), which are the reference's only accessors. */
 int fcc_result_info(const fcc_result *r, int32_t *order, int64_t *nnz, int64_t *products);
