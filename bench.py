@@ -286,11 +286,15 @@ def run_sched_eval(model_path, reps=3):
         ctx.sched_set_model(model)
         t_learn, fp_learn = timed(call, F.Options(timing=1, schedule=F.SCHED_LEARNED))
         cls = np.bincount(ctx.sched_last_tiles(features=False, cost=False)["cls"], minlength=F.NUM_CLASSES)
+        t_mix, fp_mix = timed(call, F.Options(timing=1, schedule=F.SCHED_LEARNED, sched_mix_margin=10))
+        cls_mix = np.bincount(ctx.sched_last_tiles(features=False, cost=False)["cls"], minlength=F.NUM_CLASSES)
         ctx.sched_set_model(None)
         line = {"case": name, "autotuned": F.Context.options_dict(best), "autotuned_ms": t_auto, "rule_ms": t_rule,
                 "learned_ms": t_learn, "learned_vs_autotuned": t_auto / t_learn,
                 "learned_tiles_per_class": [int(c) for c in cls],
-                "identical_output": same(fp_auto, fp_learn) and same(fp_auto, fp_rule), "outputs": fp_auto[0]}
+                "learned_margin10_ms": t_mix, "learned_margin10_tiles_per_class": [int(c) for c in cls_mix],
+                "identical_output": same(fp_auto, fp_learn) and same(fp_auto, fp_rule) and same(fp_auto, fp_mix),
+                "outputs": fp_auto[0]}
         print(json.dumps(line), flush=True)
         out.append(line)
     # batched + learned against 256 autotuned plain contractions

@@ -377,6 +377,30 @@ __global__ void k_tile_class(const u32 *__restrict__ ntiles_p, i64 nmax, const u
   }
 }
 
+// Sums over the tiles of 2^pred: per enabled class (every tile in that class)
+// and of the per-tile minimum (a mix). out: FCC_NUM_CLASSES + 1 doubles.
+__global__ void k_pred_sums(const u32 *__restrict__ ntiles_p, i64 nmax, const float *__restrict__ pred, ClassTable ct,
+                            double *__restrict__ out) {
+  const u32 ntiles = *ntiles_p;
+  double s[FCC_NUM_CLASSES + 1] = {};
+  for (i64 t = i64(blockIdx.x) * blockDim.x + threadIdx.x; t < min(nmax, i64(ntiles));
+       t += i64(gridDim.x) * blockDim.x) {
+    double mn = 1e300;
+    for (int c = 0; c < FCC_NUM_CLASSES; c++) {
+      if (!ct.enabled[c]) continue;
+      const double v = exp2(double(pred[t * FCC_NUM_CLASSES + c]));
+      s[c] += v;
+      mn = fmin(mn, v);
+    }
+    s[FCC_NUM_CLASSES] += mn;
+  }
+  for (int c = 0; c <= FCC_NUM_CLASSES; c++) {
+    double v = s[c];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(&out[c], v);
+  }
+}
+
 // Per tile in class order (position i, tile corder[i]): work items, split
 // flags (dense / hash), output bound and (split hash tiles) global region size.
 __global__ void k_tile_items(const u32 *__restrict__ ntiles_p, i64 nmax, const u32 *__restrict__ corder,
@@ -975,6 +999,7 @@ struct DenseArgs {
   u32 *err;
   u64 *item_cyc;  // per item: SM cycles from fetch to drained (NULL: not recorded)
   u32 stage_off;  // byte offset of phase 1's staging ring in dynamic shared memory; 0: no staging
+  u64 *merge_cyc; // per tile: SM cycles of its split-tile merge (NULL: not recorded)
 };
 
 // The touched mask of positions [32w, 32w+32) of a dense tile, in every lane.
@@ -1218,11 +1243,13 @@ __global__ void __launch_bounds__(kTileThreads) k_merge_dense(DenseArgs a) {
   __shared__ u64 s_base;
   __shared__ u64 s_rows[kRowCache];
   for (u32 s = blockIdx.x; s < a.nsplit; s += gridDim.x) {
+    const long long c0 = clock64();
     const u32 t = a.split_tiles[s];
     const u32 LB = a.tile_lb[t];
     drain_dense<false>(a.gacc + u64(s) * a.area, a.gmask + u64(s) * a.words, a.tile_nrows[t] * LB, LB,
                        magic_for(LB), a.urow, a.tile_rank0[t], a.out, a.dec, a.err, s_cnt, s_warp, &s_base, s_rows);
     __syncthreads();
+    if (a.merge_cyc && threadIdx.x == 0) a.merge_cyc[t] = u64(clock64() - c0);
   }
 }
 
@@ -1254,6 +1281,7 @@ struct HashArgs {
   Decode dec;
   u32 *err;
   u64 *item_cyc;  // per item: SM cycles from fetch to drained (NULL: not recorded)
+  u64 *merge_cyc; // per tile: SM cycles of its split-tile merge (NULL: not recorded)
 };
 
 // Emits occupied slots of an open-addressing table, coalesced per warp, and
@@ -1441,11 +1469,13 @@ __global__ void __launch_bounds__(kTileThreads) k_merge_hash(HashArgs<ColT> a) {
   __shared__ u64 s_base;
   __shared__ u64 s_rows[kRowCache];
   for (u32 s = blockIdx.x; s < a.nsplit; s += gridDim.x) {
+    const long long c0 = clock64();
     const u32 t = a.split_tiles[s];
     const u64 off = a.hoff[t];
     drain_hash(a.gkeys + off, a.gvals + off, a.hsz[t], a.LB, a.TL, a.tile_rank0[t], a.tile_nrows[t], a.urow,
                a.out, a.dec, a.err, s_wcnt, &s_base, s_rows, kRowCache);
     __syncthreads();
+    if (a.merge_cyc && threadIdx.x == 0) a.merge_cyc[t] = u64(clock64() - c0);
   }
 }
 
@@ -1551,7 +1581,8 @@ const double *upload_values(Runtime *ctx, const fcc_tensor *t) {
 
 // Device scalar block: slot numbers in a u64 array.
 enum Scalar { S_NSEG = 0, S_NA2, S_NTILES, S_NITEMS, S_NSPLIT, S_CAP, S_HASH, S_CURSOR, S_COUNTER, S_NROWS,
-              S_PTOTAL, S_ERR, S_TINY, S_HOT, S_NSPLIT_H, S_CLS0, S_CLS_END = S_CLS0 + FCC_NUM_CLASSES, S_COUNT };
+              S_PTOTAL, S_ERR, S_TINY, S_HOT, S_NSPLIT_H, S_CLS0, S_CLS_END = S_CLS0 + FCC_NUM_CLASSES,
+              S_PSUM0, S_PSUM_END = S_PSUM0 + FCC_NUM_CLASSES + 1, S_COUNT };
 static_assert(S_COUNT <= 32, "the pinned scalar block holds 32 entries");
 
 // Copies the scalar block and the error word to pinned host memory, waits,
@@ -1768,7 +1799,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   const bool custom_hash = opt.hash_slots > 0 || (opt.tile_threads > 0 && opt.accumulator == FCC_ACC_HASH);
   HostClass hc[FCC_NUM_CLASSES];
   hc[FCC_CLASS_DENSE] = {false, opt.tile_threads > 0 ? opt.tile_threads : kTileThreads, 0u, 0, dense};
-  hc[FCC_CLASS_HASH_L] = {true, opt.tile_threads > 0 ? opt.tile_threads : 512,
+  hc[FCC_CLASS_HASH_L] = {true, opt.tile_threads > 0 ? opt.tile_threads : 1024,
                           opt.hash_slots > 0 ? u32(opt.hash_slots) : 8192u, 0, opt.accumulator != FCC_ACC_DENSE};
   hc[FCC_CLASS_HASH_M] = {true, 256, 4096u, 0, opt.accumulator != FCC_ACC_DENSE && !custom_hash};
   hc[FCC_CLASS_HASH_S] = {true, 128, 2048u, 0, opt.accumulator != FCC_ACC_DENSE && !custom_hash};
@@ -1811,6 +1842,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (custom_hash && forced < 0 && opt.accumulator == FCC_ACC_HASH) forced = FCC_CLASS_HASH_L;
   if (opt.dense_fill_log2 < 0 || opt.dense_fill_log2 > 40) throw Error{FCC_ERR_ARG, "dense_fill_log2 out of range"};
   if (opt.dense_staging < -1 || opt.dense_staging > 0) throw Error{FCC_ERR_ARG, "dense_staging must be -1 or 0"};
+  if (opt.sched_mix_margin < 0 || opt.sched_mix_margin > 1000) throw Error{FCC_ERR_ARG, "bad sched_mix_margin"};
   const bool learned = forced < 0 && opt.schedule == FCC_SCHED_LEARNED && ctx->sched && ctx->sched->model;
   const bool want_record = opt.timing == 2 && ctx->sched;
   // Row groups (batched contractions): dense tiles hold rows of one group,
@@ -1902,6 +1934,30 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (learned) {
     pred = ar.get_n<float>(size_t(nA2) * FCC_NUM_CLASSES);
     predict_costs(st, sc32(S_NTILES), u32(nA2), feat, ctx->sched->model, pred);
+    // With sched_mix_margin > 0, a launch-level decision: predicted totals of
+    // every class run on all tiles, and of the per-tile best; classes are mixed
+    // only when the mix is predicted to win by that margin, otherwise every
+    // tile takes the class of the lowest predicted total.
+    if (opt.sched_mix_margin > 0) {
+    FCC_CUDA(cudaMemsetAsync(d_sc + S_PSUM0, 0, sizeof(u64) * (FCC_NUM_CLASSES + 1), st));
+    k_pred_sums<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), nA2, pred, ctab,
+                                                    reinterpret_cast<double *>(d_sc + S_PSUM0));
+    FCC_LAUNCH_CHECK();
+    read_scalars(ctx, d_sc);
+    double best = 1e300, mix = 0;
+    int best_c = -1;
+    for (int c = 0; c < FCC_NUM_CLASSES; c++) {
+      if (!hc[c].enabled) continue;
+      double v;
+      std::memcpy(&v, &ctx->h_scalars[S_PSUM0 + c], sizeof(v));
+      if (v < best) { best = v; best_c = c; }
+    }
+    std::memcpy(&mix, &ctx->h_scalars[S_PSUM0 + FCC_NUM_CLASSES], sizeof(mix));
+    if (best_c >= 0 && !(mix * (1.0 + opt.sched_mix_margin / 100.0) < best)) {
+      ctab.forced = best_c;
+      pred = nullptr;
+    }
+    }
   }
   u32 *cls = ar.get_n<u32>(nA2);
   u64 *ckey = ar.get_n<u64>(nA2);
@@ -1968,6 +2024,8 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     gvals = ar.get_n<double>(hash_total);
   }
   u64 *item_cyc = want_record ? ar.get_n<u64>(std::max<u32>(nitems, 1)) : nullptr;
+  u64 *merge_cyc = want_record ? ar.get_n<u64>(nA2) : nullptr;
+  if (merge_cyc) FCC_CUDA(cudaMemsetAsync(merge_cyc, 0, sizeof(u64) * nA2, st));
   u32 *counters = ar.get_n<u32>(FCC_NUM_CLASSES);
   tm.mark(3);
 
@@ -2054,7 +2112,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     DenseArgs da{items + cbeg[FCC_CLASS_DENSE], ccount[FCC_CLASS_DENSE], counters + FCC_CLASS_DENSE, tile_abeg,
                  tile_rank0, tile_lb, tile_nrows, urow, split_of_tile, split_tiles_d, nsplit_d, src,
                  static_cast<const u32 *>(colB), u32(area), u32(words), hot, gacc, gmask, o, dec, ctx->d_err,
-                 item_cyc ? item_cyc + cbeg[FCC_CLASS_DENSE] : nullptr, 0u};
+                 item_cyc ? item_cyc + cbeg[FCC_CLASS_DENSE] : nullptr, 0u, merge_cyc};
     if (ccount[FCC_CLASS_DENSE]) {
       const int threads = hc[FCC_CLASS_DENSE].threads;
       size_t smem = class_smem(FCC_CLASS_DENSE, hot);
@@ -2085,7 +2143,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       HashArgs<ColT> ha{nullptr, 0, nullptr, tile_rank0, urow, tile_nrows, tile_abeg, split_of_tile, split_tiles_h,
                         nsplit_h, src, colptr, LB, u32(grouped ? std::max<u64>(TL, 2) : TL), 0u, hot, hoff_t,
                         hsz_t, gkeys, gvals, o, dec,
-                        ctx->d_err, nullptr};
+                        ctx->d_err, nullptr, merge_cyc};
       for (int c = FCC_CLASS_HASH_L; c < FCC_NUM_CLASSES; c++) {
         if (!ccount[c]) continue;
         ha.items = items + cbeg[c];
@@ -2147,7 +2205,8 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       double *cost = ar.get_n<double>(ntiles);
       double occ[FCC_NUM_CLASSES];
       for (int c = 0; c < FCC_NUM_CLASSES; c++) occ[c] = ctas_per_sm[c] > 0 ? double(ctas_per_sm[c]) : 1.0;
-      tile_costs(st, ntiles, corder, cls, item_off, t_items, item_cyc, occ, cost);
+      // merges run up to two CTAs per SM (grid <= 2 x SMs)
+      tile_costs(st, ntiles, corder, cls, item_off, t_items, item_cyc, occ, merge_cyc, 2.0, cost);
       FCC_CUDA(cudaStreamSynchronize(st));
       io.cost = cost;
     }

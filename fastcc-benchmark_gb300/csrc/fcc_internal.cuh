@@ -103,7 +103,8 @@ void tile_features(cudaStream_t st, const u32 *ntiles_p, u32 nmax, const u32 *ab
 void predict_costs(cudaStream_t st, const u32 *ntiles_p, u32 nmax, const float *feat, const float *model,
                    float *pred);
 void tile_costs(cudaStream_t st, u32 ntiles, const u32 *corder, const u32 *cls, const u32 *item_off,
-                const u32 *t_items, const u64 *item_cyc, const double *occ, double *cost);
+                const u32 *t_items, const u64 *item_cyc, const double *occ, const u64 *merge_cyc,
+                double merge_occ, double *cost);
 
 struct Runtime {
   explicit Runtime(Arena &a) : arena(a) {}

@@ -224,18 +224,20 @@ __global__ void k_gather_rows(const u32 *__restrict__ idx, u32 n, const float *_
   }
 }
 
-// cost[t] = sum of tile t's item cycles / CTAs per SM of its class.
+// cost[t] = sum of tile t's item cycles / CTAs per SM of its class, plus its
+// split-tile merge cycles / merge CTAs per SM.
 struct Occ {
   double v[FCC_NUM_CLASSES];
 };
 __global__ void k_tile_costs(u32 ntiles, const u32 *__restrict__ corder, const u32 *__restrict__ cls,
                              const u32 *__restrict__ item_off, const u32 *__restrict__ t_items,
-                             const u64 *__restrict__ item_cyc, Occ occ, double *__restrict__ cost) {
+                             const u64 *__restrict__ item_cyc, Occ occ, const u64 *__restrict__ merge_cyc,
+                             double merge_occ, double *__restrict__ cost) {
   for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < ntiles; i += gridDim.x * blockDim.x) {
     const u32 t = corder[i];
     double s = 0;
     for (u32 k = 0; k < t_items[i]; k++) s += double(item_cyc[item_off[i] + k]);
-    cost[t] = s / occ.v[cls[t]];
+    cost[t] = s / occ.v[cls[t]] + (merge_cyc ? double(merge_cyc[t]) / merge_occ : 0.0);
   }
 }
 
@@ -301,10 +303,12 @@ void predict_costs(cudaStream_t st, const u32 *ntiles_p, u32 nmax, const float *
 }
 
 void tile_costs(cudaStream_t st, u32 ntiles, const u32 *corder, const u32 *cls, const u32 *item_off,
-                const u32 *t_items, const u64 *item_cyc, const double *occ, double *cost) {
+                const u32 *t_items, const u64 *item_cyc, const double *occ, const u64 *merge_cyc,
+                double merge_occ, double *cost) {
   Occ o;
   for (int c = 0; c < FCC_NUM_CLASSES; c++) o.v[c] = occ[c];
-  k_tile_costs<<<grid_rows(ntiles, 256), 256, 0, st>>>(ntiles, corder, cls, item_off, t_items, item_cyc, o, cost);
+  k_tile_costs<<<grid_rows(ntiles, 256), 256, 0, st>>>(ntiles, corder, cls, item_off, t_items, item_cyc, o,
+                                                       merge_cyc, merge_occ, cost);
   FCC_LAUNCH_CHECK();
 }
 

@@ -107,7 +107,10 @@ typedef struct fcc_options {
   int32_t dense_staging;      /* 0: dense tiles stage the B segments of long A entries in shared
                                  memory with bulk copies when the ring fits beside the tile;
                                  -1: never */
-  int32_t reserved[2];
+  int32_t sched_mix_margin;   /* FCC_SCHED_LEARNED: 0 (default): every tile takes its best predicted
+                                 class; > 0: one class for every tile unless the model predicts the
+                                 mix faster than the best single class by this many percent */
+  int32_t reserved[1];
 } fcc_options;
 
 /* Tile classes: every output tile runs in one of them. The hash classes
@@ -115,7 +118,7 @@ typedef struct fcc_options {
  * so that small tiles overlap their barriers and memory latency. */
 enum {
   FCC_CLASS_DENSE = 0,   /* shared-memory dense tile, 512 threads (tile_threads) */
-  FCC_CLASS_HASH_L = 1,  /* hash, 8192 slots, 512 threads, one CTA per SM */
+  FCC_CLASS_HASH_L = 1,  /* hash, 8192 slots, 1024 threads (tile_threads), one CTA per SM */
   FCC_CLASS_HASH_M = 2,  /* hash, 4096 slots, 256 threads */
   FCC_CLASS_HASH_S = 3,  /* hash, 2048 slots, 128 threads */
   FCC_NUM_CLASSES = 4

@@ -169,14 +169,16 @@ def test_learned_schedule_mixes_classes_and_records_tiles(ctx):
     # B span 20,000: one row per tile, hub rows with many multiply-adds, tail rows with few
     w = workloads.zipf3(seed=25, nnz=80_000, dims=(20_000, 20_000, 500_000))
     rng = np.random.Generator(np.random.PCG64(32))
-    # a model that prefers the dense class for tiles with many multiply-adds
+    # a model under which hash tiles cost their multiply-adds and dense tiles a
+    # constant 2^9: hub tiles go dense, small tiles to hash, and the mix beats
+    # every single class by far more than the planner's margin
     m = np.zeros(F.SCHED_MODEL_FLOATS, np.float32)
     mean, scale, W1, b1, W2, b2, W3, b3 = _split(m)
     scale[:] = 1.0
     W1[0, 0] = 1.0            # h1_0 = log2(1 + multiply-adds)
     W2[0, 0] = 1.0            # h2_0 = h1_0
-    W3[0, F.CLASS_DENSE] = -1.0
-    b3[:] = [0.0, -9.0, -9.0, -9.0]  # predicted log2 costs: hash -9, dense -log2(1 + multiply-adds)
+    W3[0, 1:] = 1.0           # predicted log2 cost of every hash class: log2(1 + multiply-adds)
+    b3[:] = [9.0, 0.0, 0.0, 0.0]  # dense: 9
     ctx.sched_set_model(m)
     try:
         r = ctx.contract(w["a"], w["b"], w["ctr_a"], w["ctr_b"], F.Options(schedule=F.SCHED_LEARNED, timing=2))
@@ -239,3 +241,20 @@ def test_autotune_batch(ctx):
                                    [1, 2], want_abs=True)
         sel = c[:, 0] == t
         check_parity(c[sel, 1:], v[sel], o["coords"], o["values"], o["abs_sum"])
+
+
+def test_learned_schedule_picks_one_class_when_mixing_does_not_pay(ctx):
+    w = workloads.zipf3(seed=25, nnz=80_000, dims=(20_000, 20_000, 500_000))
+    m = np.zeros(F.SCHED_MODEL_FLOATS, np.float32)
+    mean, scale, W1, b1, W2, b2, W3, b3 = _split(m)
+    scale[:] = 1.0
+    b3[:] = [3.0, 2.0, 1.0, 1.05]  # constant predictions: the medium hash class is cheapest everywhere
+    ctx.sched_set_model(m)
+    try:
+        r = ctx.contract(w["a"], w["b"], w["ctr_a"], w["ctr_b"],
+                         F.Options(schedule=F.SCHED_LEARNED, sched_mix_margin=10))
+        r.free()
+        cls = ctx.sched_last_tiles(features=False, cost=False)["cls"]
+    finally:
+        ctx.sched_set_model(None)
+    assert np.all(cls == F.CLASS_HASH_M)
