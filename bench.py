@@ -391,6 +391,53 @@ def run_sweep(name, variants, reps=3):
                               "contract_ms": statistics.median(con)}), flush=True)
 
 
+def run_twomode(steps, stream, local):
+    """The two-mode self-contraction (A 5000x5000x2000x50, 5M nnz, over {0,2}):
+    GPU time per contraction with the default schedule, device-resident, next
+    to the CPU oracle on all host cores over a row sample of the same
+    workload (rows j % 8 == 0 of the left operand)."""
+    import numpy as np
+    import torch
+
+    import fastcc_gpu as F
+    import workloads
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    w = workloads.twomode(seed=1)
+    a = w["a"]
+    A = F.Tensor(torch.from_numpy(a.coords).cuda(), torch.from_numpy(a.values).cuda(), a.max_index)
+    ctx = F.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    for _ in range(3):
+        ctx.contract(A, A, w["ctr_a"], w["ctr_b"]).free()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = max(steps, 5)
+    e0.record(stream)
+    for _ in range(n):
+        ctx.contract(A, A, w["ctr_a"], w["ctr_b"]).free()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / n
+    r = ctx.contract(A, A, w["ctr_a"], w["ctr_b"])
+    prods, outs = r.products, r.nnz
+    r.free()
+    ctx.close()
+    oracle.build()
+    sel = (a.coords[:, 1] % 8) == 0
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    o = oracle.fastcc_multiply(a.coords[sel], a.values[sel], a.max_index, a.coords, a.values, a.max_index,
+                               w["ctr_a"], w["ctr_b"], tile_size=128, nthreads=threads)
+    dt = time.perf_counter() - t0
+    cpu_rate = o["products"] / dt
+    return {"workload": w["name"], "multiply_adds": prods, "outputs": outs, "gpu_ms": ms,
+            "multiply_adds_per_s": prods / (ms / 1000.0),
+            "cpu_oracle": {"multiply_adds_per_s": cpu_rate, "threads": threads,
+                           "sample": f"left operand rows with j % 8 == 0 ({o['products']} multiply-adds, {dt:.2f} s)"},
+            "gpu_vs_cpu": prods / (ms / 1000.0) / cpu_rate}
+
+
 def run_readme(steps, stream, local):
     """The README contraction (256x64x256x64, 200k nnz, x 512x64x64, 100k
     nnz over {1,3} x {1,2}): GPU ms per contraction (device-resident and end to
@@ -749,6 +796,7 @@ def main():
     if not args.no_batched:
         line["batched"] = run_batched(min(args.steps, 5), 3, stream, local)
         line["readme"] = run_readme(args.steps, stream, local)
+        line["twomode"] = run_twomode(args.steps, stream, local)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         # bounded sample: grow it (halve `every`) until one run takes >= 8 s
         every = 256
