@@ -328,17 +328,19 @@ struct ClassTable {
   u64 pmax[FCC_NUM_CLASSES];
   int forced;     // >= 0: every tile takes this class
   int fill_log2;  // rule: dense only when multiply-adds >= area >> fill_log2 (0: whenever it fits)
+  float override_log2;  // learned: leave the rule's class only for a class predicted cheaper by this (log2)
 };
 
 __device__ __forceinline__ u64 tile_area(const u32 *nrows, const u32 *lb, u64 LB, u32 t) {
   return u64(nrows[t]) * (lb ? u64(lb[t]) : LB);
 }
 
-// cls[t]: the class of tile t. Forced, or from the predicted costs (pred,
-// FCC_NUM_CLASSES per tile, lowest among the enabled classes wins; a tile
-// larger than a class's work item is split, as under a forced class), or the
-// rule: dense when enabled and filled enough, else the smallest hash table
-// holding the tile, else the largest. ckey/corder: sort keys for the
+// cls[t]: the class of tile t. Forced, or the rule: dense when enabled and
+// filled enough, else the smallest hash table holding the tile, else the
+// largest. With predicted costs (pred, FCC_NUM_CLASSES log2 costs per tile)
+// the tile leaves the rule's class for the cheapest predicted class when that
+// is cheaper by more than override_log2 (a tile larger than a class's work
+// item is split, as under a forced class). ckey/corder: sort keys for the
 // class-order permutation (padding tiles sort last).
 __global__ void k_tile_class(const u32 *__restrict__ ntiles_p, i64 nmax, const u32 *__restrict__ abeg,
                              const u64 *__restrict__ P, const u32 *__restrict__ nrows, const u32 *__restrict__ lb,
@@ -353,15 +355,7 @@ __global__ void k_tile_class(const u32 *__restrict__ ntiles_p, i64 nmax, const u
     }
     const u64 prod = P[abeg[t + 1]] - P[abeg[t]];
     int c = ct.forced;
-    if (c < 0 && pred) {
-      float best = 3.4e38f;
-      for (int k = 0; k < FCC_NUM_CLASSES; k++) {
-        if (!ct.enabled[k]) continue;
-        const float v = pred[t * FCC_NUM_CLASSES + k];
-        if (v < best) { best = v; c = k; }
-      }
-    }
-    if (c < 0) {
+    if (c < 0) {  // the rule
       const u64 area = tile_area(nrows, lb, LB, u32(t));
       if (ct.enabled[FCC_CLASS_DENSE] && (ct.fill_log2 == 0 || prod >= (area >> ct.fill_log2))) {
         c = FCC_CLASS_DENSE;
@@ -370,6 +364,12 @@ __global__ void k_tile_class(const u32 *__restrict__ ntiles_p, i64 nmax, const u
         for (int k = FCC_NUM_CLASSES - 1; k > FCC_CLASS_HASH_L; k--)
           if (ct.enabled[k] && prod <= ct.pmax[k]) { c = k; break; }
         if (!ct.enabled[c]) c = FCC_CLASS_DENSE;  // only dense is enabled
+      }
+      if (pred) {  // the model overrides the rule where it predicts a clearly cheaper class
+        const float *pt = pred + t * FCC_NUM_CLASSES;
+        float best = pt[c] - ct.override_log2;
+        for (int k = 0; k < FCC_NUM_CLASSES; k++)
+          if (ct.enabled[k] && pt[k] < best) { best = pt[k]; c = k; }
       }
     }
     cls[t] = u32(c);
@@ -1925,6 +1925,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   }
   ctab.forced = forced;
   ctab.fill_log2 = opt.dense_fill_log2;
+  ctab.override_log2 = 0.32f;  // the model must predict at least 25% cheaper to leave the rule
   const u32 *lb_or_null = dense ? tile_lb : nullptr;
   float *feat = nullptr, *pred = nullptr;
   if (learned || want_record) {

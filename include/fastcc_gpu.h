@@ -107,9 +107,9 @@ typedef struct fcc_options {
   int32_t dense_staging;      /* 0: dense tiles stage the B segments of long A entries in shared
                                  memory with bulk copies when the ring fits beside the tile;
                                  -1: never */
-  int32_t sched_mix_margin;   /* FCC_SCHED_LEARNED: 0 (default): every tile takes its best predicted
-                                 class; > 0: one class for every tile unless the model predicts the
-                                 mix faster than the best single class by this many percent */
+  int32_t sched_mix_margin;   /* FCC_SCHED_LEARNED: 0 (default): per-tile choices; > 0: one class for
+                                 every tile unless the model predicts the per-tile mix faster than
+                                 the best single class by this many percent */
   int32_t reserved[1];
 } fcc_options;
 
@@ -127,8 +127,9 @@ enum {
 typedef enum fcc_schedule {
   FCC_SCHED_RULE = 0,     /* dense when the tile fits it (see dense_fill_log2), else the smallest
                              hash table that holds the tile without splitting it */
-  FCC_SCHED_LEARNED = 1,  /* per-tile class from the context's cost model (fcc_sched_set_model);
-                             FCC_SCHED_RULE when none is set */
+  FCC_SCHED_LEARNED = 1,  /* the rule's class, overridden per tile where the context's cost model
+                             (fcc_sched_set_model) predicts another class at least 25% cheaper;
+                             FCC_SCHED_RULE when no model is set */
   FCC_SCHED_FORCE = 2     /* FCC_SCHED_FORCE + class: one class for every tile */
 } fcc_schedule;
 
