@@ -406,22 +406,27 @@ __global__ void k_pred_sums(const u32 *__restrict__ ntiles_p, i64 nmax, const fl
 __global__ void k_tile_items(const u32 *__restrict__ ntiles_p, i64 nmax, const u32 *__restrict__ corder,
                              const u32 *__restrict__ cls, const u32 *__restrict__ abeg, const u64 *__restrict__ P,
                              const u32 *__restrict__ nrows, const u32 *__restrict__ lb, u64 LB, ClassTable ct,
-                             u32 *__restrict__ nitems, u32 *__restrict__ split_d, u32 *__restrict__ split_h,
-                             u64 *__restrict__ cap, u64 *__restrict__ hsz) {
+                             int esc, u32 *__restrict__ nitems, u32 *__restrict__ split_d,
+                             u32 *__restrict__ split_h, u64 *__restrict__ cap, u64 *__restrict__ hsz,
+                             u32 *__restrict__ esc_flag, u64 *__restrict__ esc_cnt) {
   const u32 ntiles = *ntiles_p;
   for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < nmax; i += i64(gridDim.x) * blockDim.x) {
     if (i >= ntiles) {
-      nitems[i] = 0; split_d[i] = 0; split_h[i] = 0; cap[i] = 0; hsz[i] = 0;
+      nitems[i] = 0; split_d[i] = 0; split_h[i] = 0; cap[i] = 0; hsz[i] = 0; esc_flag[i] = 0; esc_cnt[i] = 0;
       continue;
     }
     const u32 t = corder[i], c = cls[t];
     const u64 prod = P[abeg[t + 1]] - P[abeg[t]];
-    const u64 items = (prod + ct.pmax[c] - 1) / ct.pmax[c];
+    u64 items = (prod + ct.pmax[c] - 1) / ct.pmax[c];
     const u64 area = tile_area(nrows, lb, LB, t);  // rows x LB fits 64 bits (host check)
     const u64 bound = prod < area ? prod : area;
+    const bool to_esc = esc && ct.hash[c] && items > 1;  // a hash tile too big for its table
+    if (to_esc) items = 0;
     nitems[i] = u32(items);
     split_d[i] = (!ct.hash[c] && items > 1) ? 1u : 0u;
     split_h[i] = (ct.hash[c] && items > 1) ? 1u : 0u;
+    esc_flag[i] = to_esc ? 1u : 0u;
+    esc_cnt[i] = to_esc ? prod : 0;
     cap[i] = bound;
     u64 h = 0;
     if (ct.hash[c] && items > 1) {
@@ -448,10 +453,21 @@ __global__ void k_item_write(const u32 *__restrict__ ntiles_p, const u32 *__rest
                              const u32 *__restrict__ split_d_idx, const u32 *__restrict__ split_h_idx,
                              int *__restrict__ split_of_tile, u32 *__restrict__ split_tiles_d,
                              u32 *__restrict__ split_tiles_h, const u64 *__restrict__ hoff_i,
-                             const u64 *__restrict__ hsz_i, u64 *__restrict__ hoff_t, u64 *__restrict__ hsz_t) {
+                             const u64 *__restrict__ hsz_i, u64 *__restrict__ hoff_t, u64 *__restrict__ hsz_t,
+                             const u32 *__restrict__ esc_flag, const u32 *__restrict__ esc_idx,
+                             const u64 *__restrict__ esc_off, u32 *__restrict__ esc_tiles,
+                             u64 *__restrict__ esc_base) {
   const u32 ntiles = *ntiles_p;
   for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < ntiles; i += i64(gridDim.x) * blockDim.x) {
     const u32 t = corder[i];
+    if (esc_flag[i]) {  // expanded, sorted and reduced instead of run as items
+      esc_tiles[esc_idx[i]] = t;
+      esc_base[esc_idx[i]] = esc_off[i];
+      split_of_tile[t] = -1;
+      hoff_t[t] = 0;
+      hsz_t[t] = 0;
+      continue;
+    }
     const u64 pmax = ct.pmax[cls[t]];
     const u32 alo = abeg[t], ahi = abeg[t + 1];
     const u64 b = P[alo], e = P[ahi];
@@ -1479,6 +1495,75 @@ __global__ void __launch_bounds__(kTileThreads) k_merge_hash(HashArgs<ColT> a) {
   }
 }
 
+// ---------------------------------------------- expand, sort, reduce ----
+//
+// Hash tiles with more multiply-adds than a table holds (hub rows) are not
+// split into table-sized items merged through a global hash; their products
+// are expanded into (key, value) pairs, key = esc index x span + slot x LB +
+// column, radix-sorted (stable, so equal keys keep the products' order) and
+// reduced run by run: every output written once, no atomics.
+
+struct EscArgs {
+  const u32 *tiles;     // esc index -> tile
+  const u64 *base;      // esc index -> first pair
+  u32 n;                // esc tiles
+  u64 span, LB;         // key = s * span + slot * LB + col
+  u64 *keys;
+  u64 *vals;            // the products' bits (double), sorted along with the keys
+  u64 total;            // pairs
+};
+
+// One CTA per esc tile (grid-stride), one warp per A entry of the tile.
+template <class ColT>
+__global__ void __launch_bounds__(256) k_esc_expand(EscArgs a, const ProdSrc src, const ColT *__restrict__ colB,
+                                                    const u32 *__restrict__ tile_abeg) {
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (u32 s = blockIdx.x; s < a.n; s += gridDim.x) {
+    const u32 t = a.tiles[s];
+    const u32 ea = tile_abeg[t], eb = tile_abeg[t + 1];
+    const u64 p0 = __ldg(&src.P[ea]), base = a.base[s];
+    for (u32 e = ea + warp; e < eb; e += nwarps) {
+      const u64 pe = __ldg(&src.P[e]), len = __ldg(&src.P[e + 1]) - pe;
+      const double va = __ldg(&src.valA[e]);
+      const u64 kb = u64(s) * a.span + u64(__ldg(&src.slotA[e])) * a.LB;
+      const u32 sb = __ldg(&src.sbA[e]);
+      const u64 off = base + (pe - p0);
+      for (u64 i = lane; i < len; i += 32) {
+        a.keys[off + i] = kb + u64(__ldg(&colB[sb + i]));
+        a.vals[off + i] = u64(__double_as_longlong(va * __ldg(&src.valB[sb + i])));
+      }
+    }
+  }
+}
+
+__global__ void k_esc_flags(const u64 *__restrict__ keys, u64 n, u32 *__restrict__ flag) {
+  for (u64 i = u64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += u64(gridDim.x) * blockDim.x)
+    flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+}
+
+__global__ void k_esc_reserve(const Out out, const u32 *__restrict__ nruns, u64 *__restrict__ base, u32 *err) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *base = reserve(out, *nruns, err);
+}
+
+// Each run of equal keys (starting where flag = 1) is summed in sorted order
+// by the thread whose position holds its start, and emitted at base + rank.
+__global__ void k_esc_reduce(EscArgs a, const u32 *__restrict__ flag, const u32 *__restrict__ rank,
+                             const u64 *__restrict__ base_p, const u32 *__restrict__ tile_rank0,
+                             const u64 *__restrict__ urow, const Out out, const Decode dec) {
+  const u64 base = *base_p;
+  if (base == ~0ull) return;  // over capacity: counted by the cursor, retried by the host
+  for (u64 i = u64(blockIdx.x) * blockDim.x + threadIdx.x; i < a.total; i += u64(gridDim.x) * blockDim.x) {
+    if (!flag[i]) continue;
+    const u64 key = a.keys[i];
+    double v = __longlong_as_double((long long)a.vals[i]);
+    for (u64 j = i + 1; j < a.total && !flag[j]; j++) v += __longlong_as_double((long long)a.vals[j]);
+    const u64 s = key / a.span, rem = key - s * a.span;
+    const u64 slot = rem / a.LB, col = rem - slot * a.LB;
+    const u32 t = a.tiles[s];
+    emit(out, dec, base + rank[i], __ldg(&urow[tile_rank0[t] + slot]), col, v);
+  }
+}
+
 // ------------------------------------------------------- host pipeline ----
 
 namespace {
@@ -1582,7 +1667,8 @@ const double *upload_values(Runtime *ctx, const fcc_tensor *t) {
 // Device scalar block: slot numbers in a u64 array.
 enum Scalar { S_NSEG = 0, S_NA2, S_NTILES, S_NITEMS, S_NSPLIT, S_CAP, S_HASH, S_CURSOR, S_COUNTER, S_NROWS,
               S_PTOTAL, S_ERR, S_TINY, S_HOT, S_NSPLIT_H, S_CLS0, S_CLS_END = S_CLS0 + FCC_NUM_CLASSES,
-              S_PSUM0, S_PSUM_END = S_PSUM0 + FCC_NUM_CLASSES + 1, S_COUNT };
+              S_PSUM0, S_PSUM_END = S_PSUM0 + FCC_NUM_CLASSES + 1, S_NESC, S_ESC_PAIRS, S_ESC_RUNS, S_ESC_BASE,
+              S_COUNT };
 static_assert(S_COUNT <= 32, "the pinned scalar block holds 32 entries");
 
 // Copies the scalar block and the error word to pinned host memory, waits,
@@ -1843,6 +1929,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (opt.dense_fill_log2 < 0 || opt.dense_fill_log2 > 40) throw Error{FCC_ERR_ARG, "dense_fill_log2 out of range"};
   if (opt.dense_staging < -1 || opt.dense_staging > 0) throw Error{FCC_ERR_ARG, "dense_staging must be -1 or 0"};
   if (opt.sched_mix_margin < 0 || opt.sched_mix_margin > 1000) throw Error{FCC_ERR_ARG, "bad sched_mix_margin"};
+  if (opt.hash_esc < 0 || opt.hash_esc > 1) throw Error{FCC_ERR_ARG, "hash_esc must be 0 or 1"};
   const bool learned = forced < 0 && opt.schedule == FCC_SCHED_LEARNED && ctx->sched && ctx->sched->model;
   const bool want_record = opt.timing == 2 && ctx->sched;
   // Row groups (batched contractions): dense tiles hold rows of one group,
@@ -1969,11 +2056,30 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   // tiles in class order (stable), so that each class's items are contiguous
   radix_sort_pairs(ckey, corder, nA2, 3, ar, st);
 
+  // Hash tiles too big for their table, on request (hash_esc = 1): expand,
+  // sort and reduce when the pairs fit (at most 56 bytes of temporaries per
+  // multiply-add, within half of the free device memory) and the key space
+  // fits 64 bits. Not the default: on the two-mode workload the radix sort of
+  // the pairs costs more than the global-hash merge it replaces.
+  const u64 esc_rows = grouped ? dense_cap : TL;
+  bool esc = false;
+  // (not while recording per-tile costs: expanded tiles have no work items to time)
+  if (opt.hash_esc > 0 && !want_record) {
+    size_t fb = 0, tb = 0;
+    FCC_CUDA(cudaMemGetInfo(&fb, &tb));
+    const unsigned __int128 keyspace = (unsigned __int128)nA2 * esc_rows * LB;
+    esc = ptotal <= 0xFFFFFFFFull && (unsigned __int128)ptotal * 56 <= fb / 2 && keyspace < ((unsigned __int128)1 << 64);
+  }
   u32 *t_items = ar.get_n<u32>(nA2), *t_split_d = ar.get_n<u32>(nA2), *t_split_h = ar.get_n<u32>(nA2);
   u64 *t_cap = ar.get_n<u64>(nA2), *t_hsz = ar.get_n<u64>(nA2);
+  u32 *esc_flag = ar.get_n<u32>(nA2), *esc_idx = ar.get_n<u32>(nA2);
+  u64 *esc_cnt = ar.get_n<u64>(nA2), *esc_off = ar.get_n<u64>(nA2);
   k_tile_items<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), nA2, corder, cls, tile_abeg, P, tile_nrows,
-                                                   lb_or_null, LB, ctab, t_items, t_split_d, t_split_h, t_cap, t_hsz);
+                                                   lb_or_null, LB, ctab, esc ? 1 : 0, t_items, t_split_d, t_split_h,
+                                                   t_cap, t_hsz, esc_flag, esc_cnt);
   FCC_LAUNCH_CHECK();
+  scan_exclusive(esc_flag, esc_idx, nA2, sc32(S_NESC), ar, st);
+  scan_exclusive(esc_cnt, esc_off, nA2, d_sc + S_ESC_PAIRS, ar, st);
   u32 *item_off = ar.get_n<u32>(nA2), *split_d_idx = ar.get_n<u32>(nA2), *split_h_idx = ar.get_n<u32>(nA2);
   u64 *t_hoff = ar.get_n<u64>(nA2);
   scan_exclusive(t_items, item_off, nA2, sc32(S_NITEMS), ar, st);
@@ -1990,6 +2096,8 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   const u32 nsplit_h = scalar32(ctx, S_NSPLIT_H);
   const u64 cap_total = ctx->h_scalars[S_CAP];
   const u64 hash_total = ctx->h_scalars[S_HASH];
+  const u32 nesc = scalar32(ctx, S_NESC);
+  const u64 esc_pairs = ctx->h_scalars[S_ESC_PAIRS];
   u32 cbeg[FCC_NUM_CLASSES + 1], ccount[FCC_NUM_CLASSES];
   {
     u32 next = nitems;
@@ -2007,10 +2115,21 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   u32 *split_tiles_d = ar.get_n<u32>(std::max<u32>(nsplit_d, 1));
   u32 *split_tiles_h = ar.get_n<u32>(std::max<u32>(nsplit_h, 1));
   u64 *hoff_t = ar.get_n<u64>(nA2), *hsz_t = ar.get_n<u64>(nA2);
+  u32 *esc_tiles = ar.get_n<u32>(std::max<u32>(nesc, 1));
+  u64 *esc_base = ar.get_n<u64>(std::max<u32>(nesc, 1));
   k_item_write<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), corder, cls, tile_abeg, P, item_off, ctab, items,
                                                    t_split_d, t_split_h, split_d_idx, split_h_idx, split_of_tile,
-                                                   split_tiles_d, split_tiles_h, t_hoff, t_hsz, hoff_t, hsz_t);
+                                                   split_tiles_d, split_tiles_h, t_hoff, t_hsz, hoff_t, hsz_t,
+                                                   esc_flag, esc_idx, esc_off, esc_tiles, esc_base);
   FCC_LAUNCH_CHECK();
+  EscArgs ea{esc_tiles, esc_base, nesc, esc_rows * LB, LB, nullptr, nullptr, esc_pairs};
+  u32 *esc_rflag = nullptr, *esc_rank = nullptr;
+  if (nesc > 0) {
+    ea.keys = ar.get_n<u64>(esc_pairs);
+    ea.vals = ar.get_n<u64>(esc_pairs);
+    esc_rflag = ar.get_n<u32>(esc_pairs);
+    esc_rank = ar.get_n<u32>(esc_pairs);
+  }
   const u64 words = dense ? (area + 31) / 32 : 0;
   double *gacc = nullptr;
   u32 *gmask = nullptr;
@@ -2173,6 +2292,21 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       }
       if (nsplit_h > 0) {
         k_merge_hash<ColT><<<std::min<u32>(nsplit_h, u32(ctx->num_sms) * 2), kTileThreads, 0, st>>>(ha);
+        FCC_LAUNCH_CHECK();
+      }
+      if (nesc > 0) {  // hub hash tiles: expand, sort, reduce
+        if (attempt == 0) {
+          k_esc_expand<ColT><<<std::min<u32>(nesc, u32(ctx->num_sms) * 8), 256, 0, st>>>(ea, src, colptr, tile_abeg);
+          FCC_LAUNCH_CHECK();
+          radix_sort_pairs64(ea.keys, ea.vals, i64(esc_pairs), bits_for(u64(nesc) * ea.span - 1), ar, st);
+          k_esc_flags<<<grid_for(i64(esc_pairs), 256), 256, 0, st>>>(ea.keys, esc_pairs, esc_rflag);
+          FCC_LAUNCH_CHECK();
+          scan_exclusive(esc_rflag, esc_rank, i64(esc_pairs), sc32(S_ESC_RUNS), ar, st);
+        }
+        k_esc_reserve<<<1, 32, 0, st>>>(o, sc32(S_ESC_RUNS), d_sc + S_ESC_BASE, ctx->d_err);
+        FCC_LAUNCH_CHECK();
+        k_esc_reduce<<<grid_for(i64(esc_pairs), 256), 256, 0, st>>>(ea, esc_rflag, esc_rank, d_sc + S_ESC_BASE,
+                                                                    tile_rank0, urow, o, dec);
         FCC_LAUNCH_CHECK();
       }
     };

@@ -172,6 +172,7 @@ void scan_exclusive_wide(const u32 *in, u64 *out, i64 n, u64 *total, Arena &ar, 
 // keys. keys/vals are sorted in place (ping-ponging through scratch buffers
 // taken from the arena).
 void radix_sort_pairs(u64 *keys, u32 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s);
+void radix_sort_pairs64(u64 *keys, u64 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s);  // 64-bit payload
 
 inline int grid_for(i64 n, int threads, int max_blocks = 1 << 20) {
   i64 b = (n + threads - 1) / threads;

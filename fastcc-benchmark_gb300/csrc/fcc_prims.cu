@@ -249,9 +249,10 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_hist(const u64 *__restrict__ 
   }
 }
 
+template <class V>
 __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const u64 *__restrict__ kin,
-                                                           const u32 *__restrict__ vin,
-                                                           u64 *__restrict__ kout, u32 *__restrict__ vout,
+                                                           const V *__restrict__ vin,
+                                                           u64 *__restrict__ kout, V *__restrict__ vout,
                                                            i64 n, int shift, const u32 *__restrict__ offs,
                                                            int nblk) {
   __shared__ u32 wcnt[kRsWarps][256];
@@ -261,7 +262,8 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const u64 *__restrict
   const u32 lt_mask = (1u << lane) - 1u;
   const i64 base = i64(blockIdx.x) * kRsTile + warp * (kRsItems * 32);
   u64 k[kRsItems];
-  u32 v[kRsItems], r[kRsItems], dg[kRsItems];
+  V v[kRsItems];
+  u32 r[kRsItems], dg[kRsItems];
 #pragma unroll
   for (int j = 0; j < kRsItems; j++) {
     i64 i = base + j * 32 + lane;
@@ -302,30 +304,41 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const u64 *__restrict
 
 }  // namespace
 
-void radix_sort_pairs(u64 *keys, u32 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s) {
+namespace {
+template <class V>
+void radix_sort_impl(u64 *keys, V *vals, i64 n, int nbits, Arena &ar, cudaStream_t s) {
   if (n <= 1 || nbits <= 0) return;
   if (n > i64(0xFFFFFFFFu)) throw Error{FCC_ERR_ARG, "radix sort: more than 2^32 keys"};
   const int nblk = int((n + kRsTile - 1) / kRsTile);
   u64 *k2 = ar.get_n<u64>(size_t(n));
-  u32 *v2 = ar.get_n<u32>(size_t(n));
+  V *v2 = ar.get_n<V>(size_t(n));
   u32 *hist = ar.get_n<u32>(size_t(nblk) * 256);
   u64 *ka = keys, *kb = k2;
-  u32 *va = vals, *vb = v2;
+  V *va = vals, *vb = v2;
   const int passes = (nbits + 7) / 8;
   for (int p = 0; p < passes; p++) {
     const int shift = 8 * p;
     k_rs_hist<<<nblk, kRsThreads, 0, s>>>(ka, n, shift, hist, nblk);
     FCC_LAUNCH_CHECK();
     scan_exclusive(hist, hist, i64(nblk) * 256, nullptr, ar, s);
-    k_rs_scatter<<<nblk, kRsThreads, 0, s>>>(ka, va, kb, vb, n, shift, hist, nblk);
+    k_rs_scatter<V><<<nblk, kRsThreads, 0, s>>>(ka, va, kb, vb, n, shift, hist, nblk);
     FCC_LAUNCH_CHECK();
     std::swap(ka, kb);
     std::swap(va, vb);
   }
   if (ka != keys) {
     FCC_CUDA(cudaMemcpyAsync(keys, ka, sizeof(u64) * size_t(n), cudaMemcpyDeviceToDevice, s));
-    FCC_CUDA(cudaMemcpyAsync(vals, va, sizeof(u32) * size_t(n), cudaMemcpyDeviceToDevice, s));
+    FCC_CUDA(cudaMemcpyAsync(vals, va, sizeof(V) * size_t(n), cudaMemcpyDeviceToDevice, s));
   }
+}
+}  // namespace
+
+void radix_sort_pairs(u64 *keys, u32 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s) {
+  radix_sort_impl<u32>(keys, vals, n, nbits, ar, s);
+}
+
+void radix_sort_pairs64(u64 *keys, u64 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s) {
+  radix_sort_impl<u64>(keys, vals, n, nbits, ar, s);
 }
 
 }  // namespace fcc
