@@ -429,9 +429,9 @@ __global__ void k_tile_items(const u32 *__restrict__ ntiles_p, i64 nmax, const u
     esc_cnt[i] = to_esc ? prod : 0;
     cap[i] = bound;
     u64 h = 0;
-    if (ct.hash[c] && items > 1) {
+    if (ct.hash[c] && items > 1) {  // the tile's global table: load <= 0.8 (outputs <= bound)
       h = 64;
-      while (h < 2 * bound) h <<= 1;
+      while (h < bound + bound / 4) h <<= 1;
     }
     hsz[i] = h;
   }
