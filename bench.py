@@ -379,16 +379,16 @@ def run_sweep(name, variants, reps=3):
     with F.Context(0) as ctx:
         for v in variants:
             opts = F.Options(timing=1, **v)
-            tot, con = [], []
+            ph = []
             for rep in range(reps + 1):
                 r = ctx.contract(A, B, w["ctr_a"], w["ctr_b"], opts)
                 t = ctx.timings()
                 r.free()
                 if rep:
-                    tot.append(t["total"])
-                    con.append(t["contract"])
-            print(json.dumps({"workload": name, "options": v, "total_ms": statistics.median(tot),
-                              "contract_ms": statistics.median(con)}), flush=True)
+                    ph.append(t)
+            med = {k: round(statistics.median(p[k] for p in ph), 4) for k in ph[0]}
+            print(json.dumps({"workload": name, "options": v, "total_ms": med["total"],
+                              "contract_ms": med["contract"], "phases_ms": med}), flush=True)
 
 
 def run_twomode(steps, stream, local):

@@ -782,7 +782,6 @@ constexpr u32 kStageValBytes = (kStageCh + 2) * 8;  // 16-byte multiple: room fo
 constexpr u32 kStageColBytes = (kStageCh + 4) * 4;  // 16-byte multiple: room for a 3-element head
 constexpr u32 kStageBufBytes = kStageValBytes + kStageColBytes;
 constexpr u32 kStageBytes = kStageBufs * kStageBufBytes;
-constexpr long long kWaitPolls = 1ll << 24;
 
 struct StageHdr {  // one staged chunk (written by the producer before the copies)
   double va;
@@ -797,19 +796,6 @@ struct StageCtl {
   u32 fail;   // a wait timed out: skip the remaining work
 };
 
-__device__ __forceinline__ u32 smem_addr(const void *p) { return u32(__cvta_generic_to_shared(p)); }
-
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, u32 parity) {
-  const u32 a = smem_addr(bar);
-  for (long long it = 0; it < kWaitPolls; it++) {
-    u32 done;
-    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-                 : "=r"(done) : "r"(a), "r"(parity) : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
 __device__ __forceinline__ void stage_init(StageCtl &c, u32 consumers) {
   if (threadIdx.x == 0) {
     for (u32 b = 0; b < kStageBufs; b++) {
@@ -823,13 +809,6 @@ __device__ __forceinline__ void stage_init(StageCtl &c, u32 consumers) {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
-}
-
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, u32 bytes, unsigned long long *bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_addr(dst)),
-               "l"(src), "r"(bytes), "r"(smem_addr(bar))
-               : "memory");
 }
 
 // Phase 1 of a dense item with staging (all threads call; ends with a barrier).
@@ -1804,7 +1783,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   FCC_LAUNCH_CHECK();
   k_linearize<<<grid_for(nB, 256), 256, 0, st>>>(sb.coords, sb.sn, sb.sm, nB, sb.lin, extB, keyB, permB, ctx->d_err);
   FCC_LAUNCH_CHECK();
-  radix_sort_pairs(keyB, permB, nB, bits_for(sb.keyspace - 1), ar, st);
+  radix_sort_pairs(keyB, permB, nB, bits_for(sb.keyspace - 1), ar, st, ctx->d_err);
 
   const bool colb32 = sb.span <= 0xFFFFFFFFull;
   // padded: staged copies round their end up to 16 bytes
@@ -1827,7 +1806,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   FCC_LAUNCH_CHECK();
 
   // ---- A: sort by row, look up segments, drop unmatched ----
-  radix_sort_pairs(extA, permA, nA, bits_for(sa.span - 1), ar, st);
+  radix_sort_pairs(extA, permA, nA, bits_for(sa.span - 1), ar, st, ctx->d_err);
   u32 *segTmp = ar.get_n<u32>(nA), *flagA = ar.get_n<u32>(nA), *idxA = ar.get_n<u32>(nA);
   k_lookup<<<grid_for(nA, 256), 256, 0, st>>>(keyA, permA, nA, ukey, sc32(S_NSEG), segTmp, flagA);
   FCC_LAUNCH_CHECK();
@@ -1965,7 +1944,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     FCC_LAUNCH_CHECK();
     k_col_sortkeys<<<grid_for(i64(LB), 256), 256, 0, st>>>(count, LB, lbits, ckey, cidx);
     FCC_LAUNCH_CHECK();
-    radix_sort_pairs(ckey, cidx, i64(LB), 32 + lbits, ar, st);
+    radix_sort_pairs(ckey, cidx, i64(LB), 32 + lbits, ar, st, ctx->d_err);
     k_col_tables<<<grid_for(i64(LB), 256), 256, 0, st>>>(ckey, LB, lbits, hot_want, colmap, inv_col,
                                                         reinterpret_cast<unsigned long long *>(d_sc + S_HOT));
     FCC_LAUNCH_CHECK();
@@ -2054,7 +2033,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
                                                    ctab, pred, cls, ckey, corder);
   FCC_LAUNCH_CHECK();
   // tiles in class order (stable), so that each class's items are contiguous
-  radix_sort_pairs(ckey, corder, nA2, 3, ar, st);
+  radix_sort_pairs(ckey, corder, nA2, 3, ar, st, ctx->d_err);
 
   // Hash tiles too big for their table, on request (hash_esc = 1): expand,
   // sort and reduce when the pairs fit (at most 56 bytes of temporaries per
@@ -2298,7 +2277,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
         if (attempt == 0) {
           k_esc_expand<ColT><<<std::min<u32>(nesc, u32(ctx->num_sms) * 8), 256, 0, st>>>(ea, src, colptr, tile_abeg);
           FCC_LAUNCH_CHECK();
-          radix_sort_pairs64(ea.keys, ea.vals, i64(esc_pairs), bits_for(u64(nesc) * ea.span - 1), ar, st);
+          radix_sort_pairs64(ea.keys, ea.vals, i64(esc_pairs), bits_for(u64(nesc) * ea.span - 1), ar, st, ctx->d_err);
           k_esc_flags<<<grid_for(i64(esc_pairs), 256), 256, 0, st>>>(ea.keys, esc_pairs, esc_rflag);
           FCC_LAUNCH_CHECK();
           scan_exclusive(esc_rflag, esc_rank, i64(esc_pairs), sc32(S_ESC_RUNS), ar, st);

@@ -134,3 +134,72 @@ extern "C" int fcc_diag_fp64_fma_rate(int32_t device, double *fma_per_second) {
   *fma_per_second = double(2 * sms) * 1024.0 * 8.0 * iters / (double(ms) * 1e-3);
   return FCC_OK;
 }
+
+// The library's stable LSD radix sort on caller data: keys (and their 32- or
+// 64-bit payloads) are copied to the device, sorted `reps` times from the
+// same unsorted copy, and the sorted pairs come back; *ms_per_sort is the
+// mean device time of one sort (CUDA events around the sort alone).
+extern "C" int fcc_diag_radix_sort(const uint64_t *keys, const void *vals, int64_t n, int32_t nbits,
+                                   int32_t value_bytes, int32_t reps, uint64_t *keys_out, void *vals_out,
+                                   double *ms_per_sort) {
+  using namespace fcc;
+  if (n < 0 || nbits < 0 || nbits > 64 || reps < 1 || (value_bytes != 4 && value_bytes != 8) ||
+      (n > 0 && (!keys || !vals || !keys_out || !vals_out)) || !ms_per_sort || n > i64(0xFFFFFFFFu))
+    return FCC_ERR_ARG;
+  *ms_per_sort = 0;
+  if (n == 0) return FCC_OK;
+  const size_t kb = (sizeof(u64) * size_t(n) + 255) & ~size_t(255);
+  const size_t vb = (size_t(value_bytes) * size_t(n) + 255) & ~size_t(255);
+  const size_t kn = sizeof(u64) * size_t(n), vn = size_t(value_bytes) * size_t(n);
+  const size_t nblk = (size_t(n) + 4095) / 4096;
+  const size_t scratch = kb + vb + nblk * 256 * 8 + (size_t(16) << 20);
+  char *d = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = FCC_OK;
+  if (cudaMalloc(&d, 2 * (kb + vb) + scratch + 256) != cudaSuccess) {
+    cudaGetLastError();
+    return FCC_ERR_OOM;
+  }
+  try {
+    FCC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    FCC_CUDA(cudaEventCreate(&e0));
+    FCC_CUDA(cudaEventCreate(&e1));
+    u64 *k0 = reinterpret_cast<u64 *>(d), *k1 = reinterpret_cast<u64 *>(d + kb);
+    char *v0 = d + 2 * kb, *v1 = v0 + vb;
+    u32 *err = reinterpret_cast<u32 *>(v1 + vb);
+    Arena ar;
+    ar.init_fixed(v1 + vb + 256, scratch);
+    FCC_CUDA(cudaMemsetAsync(err, 0, sizeof(u32), st));
+    FCC_CUDA(cudaMemcpyAsync(k0, keys, kn, cudaMemcpyHostToDevice, st));
+    FCC_CUDA(cudaMemcpyAsync(v0, vals, vn, cudaMemcpyHostToDevice, st));
+    double total = 0;
+    for (int r = 0; r < reps; r++) {
+      FCC_CUDA(cudaMemcpyAsync(k1, k0, kn, cudaMemcpyDeviceToDevice, st));
+      FCC_CUDA(cudaMemcpyAsync(v1, v0, vn, cudaMemcpyDeviceToDevice, st));
+      ar.begin(st);
+      FCC_CUDA(cudaEventRecord(e0, st));
+      if (value_bytes == 4) radix_sort_pairs(k1, reinterpret_cast<u32 *>(v1), n, nbits, ar, st, err);
+      else radix_sort_pairs64(k1, reinterpret_cast<u64 *>(v1), n, nbits, ar, st, err);
+      FCC_CUDA(cudaEventRecord(e1, st));
+      FCC_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      FCC_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      total += ms;
+    }
+    FCC_CUDA(cudaMemcpyAsync(keys_out, k1, kn, cudaMemcpyDeviceToHost, st));
+    FCC_CUDA(cudaMemcpyAsync(vals_out, v1, vn, cudaMemcpyDeviceToHost, st));
+    u32 h_err = 0;
+    FCC_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(u32), cudaMemcpyDeviceToHost, st));
+    FCC_CUDA(cudaStreamSynchronize(st));
+    if (h_err) throw Error{FCC_ERR_CUDA, "radix sort: a bulk-copy wait gave up"};
+    *ms_per_sort = total / reps;
+  } catch (const fcc::Error &e) {
+    rc = e.status;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  cudaFree(d);
+  return rc;
+}

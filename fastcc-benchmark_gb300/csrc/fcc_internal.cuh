@@ -30,6 +30,47 @@ enum ErrBits : u32 {
   ERRB_INTERNAL = 8u,  // an invariant of the plan did not hold
 };
 
+#ifdef __CUDACC__
+// Bulk asynchronous copies (cp.async.bulk) completed on shared-memory
+// mbarriers. Every wait polls at most kWaitPolls times; a caller whose wait
+// fails flags ERRB_INTERNAL and stops.
+constexpr long long kWaitPolls = 1ll << 24;
+
+__device__ __forceinline__ u32 smem_addr(const void *p) { return u32(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, u32 parity) {
+  const u32 a = smem_addr(bar);
+  for (long long it = 0; it < kWaitPolls; it++) {
+    u32 done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done) : "r"(a), "r"(parity) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, u32 count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_tx(unsigned long long *bar, u32 bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+// Global to shared memory; dst, src and bytes multiples of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, u32 bytes, unsigned long long *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+#endif
+
 // Thrown inside the library and turned into a status at the C ABI.
 struct Error {
   int status;
@@ -171,8 +212,11 @@ void scan_exclusive_wide(const u32 *in, u64 *out, i64 n, u64 *total, Arena &ar, 
 // Stable LSD radix sort of (key, value) pairs on the low `nbits` bits of the
 // keys. keys/vals are sorted in place (ping-ponging through scratch buffers
 // taken from the arena).
-void radix_sort_pairs(u64 *keys, u32 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s);
-void radix_sort_pairs64(u64 *keys, u64 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s);  // 64-bit payload
+// Stable LSD radix sort on the low nbits of the keys; err: device error word
+// (ERRB_INTERNAL when a copy wait of the scatter gives up).
+void radix_sort_pairs(u64 *keys, u32 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s, u32 *err);
+void radix_sort_pairs64(u64 *keys, u64 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s,
+                        u32 *err);  // 64-bit payload
 
 inline int grid_for(i64 n, int threads, int max_blocks = 1 << 20) {
   i64 b = (n + threads - 1) / threads;

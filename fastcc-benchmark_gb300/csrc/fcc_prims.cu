@@ -219,7 +219,10 @@ void scan_exclusive_wide(const u32 *in, u64 *out, i64 n, u64 *total, Arena &ar, 
 // (digit-major, so one exclusive scan yields every tile's output offsets), the
 // scan, and a stable scatter. Within a tile each warp ranks its keys with
 // __match_any_sync; ranks follow key order (warp, step, lane), which keeps the
-// sort stable.
+// sort stable. The scatter keeps each tile in shared memory, ranks it
+// block-wide and writes it out in sorted order, so a warp's stores cover runs
+// of consecutive positions (a tile holds 16 keys per digit on average)
+// instead of one or two keys per digit.
 
 namespace {
 
@@ -227,6 +230,7 @@ constexpr int kRsThreads = 256;
 constexpr int kRsWarps = kRsThreads / 32;
 constexpr int kRsItems = 16;
 constexpr int kRsTile = kRsThreads * kRsItems;  // 4096 keys per tile
+static_assert(kRsThreads == 256, "the scatter scans one digit per thread");
 
 __global__ void __launch_bounds__(kRsThreads) k_rs_hist(const u64 *__restrict__ keys, i64 n, int shift,
                                                         u32 *__restrict__ hist, int nblk) {
@@ -235,11 +239,15 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_hist(const u64 *__restrict__ 
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const i64 base = i64(blockIdx.x) * kRsTile + warp * (kRsItems * 32);
-#pragma unroll 4
+  u64 k[kRsItems];  // every load in flight before the first count
+#pragma unroll
   for (int j = 0; j < kRsItems; j++) {
     i64 i = base + j * 32 + lane;
-    if (i < n) atomicAdd(&h[warp][u32(keys[i] >> shift) & 255u], 1u);
+    k[j] = i < n ? keys[i] : 0;
   }
+#pragma unroll
+  for (int j = 0; j < kRsItems; j++)
+    if (base + j * 32 + lane < n) atomicAdd(&h[warp][u32(k[j] >> shift) & 255u], 1u);
   __syncthreads();
   for (int d = threadIdx.x; d < 256; d += kRsThreads) {
     u32 s = 0;
@@ -249,56 +257,152 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_hist(const u64 *__restrict__ 
   }
 }
 
+// Shared memory of the scatter: two tile buffers (the next tile is copied in
+// while the current one is ranked), per-warp digit counters, which the tile's
+// source order reuses once the ranks are final, and the tile's output bases.
+template <class V>
+struct RsSmem {
+  u64 keys[2][kRsTile];
+  V vals[2][kRsTile];
+  union {
+    u32 wcnt[kRsWarps][256];
+    unsigned short sidx[kRsTile];  // sorted position -> position in the tile
+  } u;
+  u32 gbase[256];  // output position of the tile's sorted position 0 of each digit
+  u32 wsum[kRsWarps];
+  unsigned long long full[2];
+  u32 fail;
+};
+static_assert(kRsTile <= 65536, "tile positions are 16-bit");
+
+// Persistent: CTA c takes tiles c, c + gridDim.x, ... Thread 0 starts the
+// bulk copy of the next tile's keys and values before the current tile is
+// ranked, so the load latency stays off the critical path. Partial tiles (or
+// bases that are not 16-byte aligned, bulk == 0) are loaded by all threads.
 template <class V>
 __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const u64 *__restrict__ kin,
                                                            const V *__restrict__ vin,
                                                            u64 *__restrict__ kout, V *__restrict__ vout,
                                                            i64 n, int shift, const u32 *__restrict__ offs,
-                                                           int nblk) {
-  __shared__ u32 wcnt[kRsWarps][256];
-  for (int i = threadIdx.x; i < kRsWarps * 256; i += kRsThreads) (&wcnt[0][0])[i] = 0;
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+                                                           int nblk, int bulk, u32 *err) {
+  extern __shared__ __align__(128) unsigned char rs_raw[];
+  RsSmem<V> &S = *reinterpret_cast<RsSmem<V> *>(rs_raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const u32 lt_mask = (1u << lane) - 1u;
-  const i64 base = i64(blockIdx.x) * kRsTile + warp * (kRsItems * 32);
-  u64 k[kRsItems];
-  V v[kRsItems];
-  u32 r[kRsItems], dg[kRsItems];
-#pragma unroll
-  for (int j = 0; j < kRsItems; j++) {
-    i64 i = base + j * 32 + lane;
-    bool valid = i < n;
-    k[j] = valid ? kin[i] : 0;
-    v[j] = valid ? vin[i] : 0;
-    u32 d = valid ? (u32(k[j] >> shift) & 255u) : (256u + lane);
-    u32 peers = __match_any_sync(kFull, d);
-    u32 before = 0;
-    if (valid) before = wcnt[warp][d];
-    __syncwarp();
-    if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] = before + __popc(peers);
-    __syncwarp();
-    r[j] = before + __popc(peers & lt_mask);
-    dg[j] = d;
+  const int G = gridDim.x;
+  auto tile_cnt = [&](int t) { return int(min(i64(kRsTile), n - i64(t) * kRsTile)); };
+  auto staged = [&](int t) { return bulk && tile_cnt(t) == kRsTile; };
+  auto issue = [&](int t, int b) {  // thread 0
+    if (staged(t)) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // after the buffer's last generic reads
+      mbar_arrive_tx(&S.full[b], u32(kRsTile * (sizeof(u64) + sizeof(V))));
+      bulk_g2s(S.keys[b], kin + i64(t) * kRsTile, u32(kRsTile * sizeof(u64)), &S.full[b]);
+      bulk_g2s(S.vals[b], vin + i64(t) * kRsTile, u32(kRsTile * sizeof(V)), &S.full[b]);
+    } else {
+      mbar_arrive(&S.full[b]);  // completes the phase; the threads load the tile themselves
+    }
+  };
+  if (tid == 0) {
+    mbar_init(&S.full[0], 1);
+    mbar_init(&S.full[1], 1);
+    S.fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < 256; d += kRsThreads) {
-    u32 run = offs[i64(d) * nblk + blockIdx.x];
-#pragma unroll
-    for (int w = 0; w < kRsWarps; w++) {
-      u32 c = wcnt[w][d];
-      wcnt[w][d] = run;
-      run += c;
+  if (tid == 0 && int(blockIdx.x) < nblk) issue(blockIdx.x, 0);
+  int it = 0;
+  for (int t = blockIdx.x; t < nblk; t += G, it++) {
+    const int b = it & 1;
+    const int cnt = tile_cnt(t);
+    if (tid == 0 && t + G < nblk) issue(t + G, b ^ 1);  // its buffer was last read before the loop's end barrier
+    const u32 my_off = offs[i64(tid) * nblk + t];          // thread tid: digit tid
+    for (int i = tid; i < kRsWarps * 256; i += kRsThreads) (&S.u.wcnt[0][0])[i] = 0;
+    if (!staged(t)) {
+      for (int i = tid; i < cnt; i += kRsThreads) {
+        S.keys[b][i] = kin[i64(t) * kRsTile + i];
+        S.vals[b][i] = vin[i64(t) * kRsTile + i];
+      }
     }
+    if (!mbar_wait(&S.full[b], u32(it >> 1) & 1u)) S.fail = 1;
+    __syncthreads();
+    if (S.fail) break;
+    // Rank within the warp: warp w holds tile positions [512 w, 512 w + 512)
+    // in (step, lane) order, so ranks follow input order.
+    const int wbase = warp * (kRsItems * 32);
+    u32 r[kRsItems], dg[kRsItems];
+#pragma unroll
+    for (int j = 0; j < kRsItems; j++) {
+      const int idx = wbase + j * 32 + lane;
+      const bool valid = idx < cnt;
+      const u32 d = valid ? (u32(S.keys[b][idx] >> shift) & 255u) : (256u + lane);
+      const u32 peers = __match_any_sync(kFull, d);
+      u32 before = 0;
+      if (valid) before = S.u.wcnt[warp][d];
+      __syncwarp();
+      if (valid && lane == __ffs(peers) - 1) S.u.wcnt[warp][d] = before + __popc(peers);
+      __syncwarp();
+      r[j] = before + __popc(peers & lt_mask);
+      dg[j] = d;
+    }
+    __syncthreads();
+    // Thread d: the tile's count of digit d, its start in the tile's sorted
+    // order (block exclusive scan over digits) and each warp's start within it.
+    {
+      u32 c[kRsWarps], tot = 0;
+#pragma unroll
+      for (int w = 0; w < kRsWarps; w++) {
+        c[w] = S.u.wcnt[w][tid];
+        tot += c[w];
+      }
+      u32 inc = tot;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const u32 v = __shfl_up_sync(kFull, inc, o);
+        if (lane >= o) inc += v;
+      }
+      if (lane == 31) S.wsum[warp] = inc;
+      __syncthreads();
+      u32 start = inc - tot;
+      for (int w = 0; w < warp; w++) start += S.wsum[w];
+      S.gbase[tid] = my_off - start;
+#pragma unroll
+      for (int w = 0; w < kRsWarps; w++) {
+        S.u.wcnt[w][tid] = start;
+        start += c[w];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kRsItems; j++)
+      if (wbase + j * 32 + lane < cnt) r[j] += S.u.wcnt[warp][dg[j]];
+    __syncthreads();  // the counters are dead: their space takes the source order
+#pragma unroll
+    for (int j = 0; j < kRsItems; j++)
+      if (wbase + j * 32 + lane < cnt) S.u.sidx[r[j]] = (unsigned short)(wbase + j * 32 + lane);
+    __syncthreads();
+    // Out in sorted order: consecutive threads write consecutive positions of
+    // one digit's run.
+#pragma unroll 4
+    for (int q = 0; q < kRsItems; q++) {
+      const int i = q * kRsThreads + tid;
+      if (i < cnt) {
+        const int src = S.u.sidx[i];
+        const u64 key = S.keys[b][src];
+        const u32 pos = S.gbase[u32(key >> shift) & 255u] + u32(i);
+        kout[pos] = key;
+        vout[pos] = S.vals[b][src];
+      }
+    }
+    __syncthreads();
   }
-  __syncthreads();
-#pragma unroll
-  for (int j = 0; j < kRsItems; j++) {
-    i64 i = base + j * 32 + lane;
-    if (i < n) {
-      u32 pos = wcnt[warp][dg[j]] + r[j];
-      kout[pos] = k[j];
-      vout[pos] = v[j];
-    }
+  if (S.fail && tid == 0) {
+    atomicOr(err, ERRB_INTERNAL);
+    // The current and the next tile's copies may be in flight: wait for them
+    // (bounded) before the CTA's shared memory is released.
+    const int t = int(blockIdx.x) + it * G;
+    mbar_wait(&S.full[it & 1], u32(it >> 1) & 1u);
+    if (t + G < nblk) mbar_wait(&S.full[(it + 1) & 1], u32((it + 1) >> 1) & 1u);
   }
 }
 
@@ -306,7 +410,25 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const u64 *__restrict
 
 namespace {
 template <class V>
-void radix_sort_impl(u64 *keys, V *vals, i64 n, int nbits, Arena &ar, cudaStream_t s) {
+int rs_grid(int nblk) {
+  static int per_sm[64] = {0}, sms[64] = {0};
+  int dev = 0;
+  FCC_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) throw Error{FCC_ERR_CUDA, "device ordinal out of range"};
+  if (per_sm[dev] == 0) {
+    const int smem = int(sizeof(RsSmem<V>));
+    FCC_CUDA(cudaFuncSetAttribute(k_rs_scatter<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int p = 0;
+    FCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, k_rs_scatter<V>, kRsThreads, smem));
+    FCC_CUDA(cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev));
+    if (p < 1) throw Error{FCC_ERR_CUDA, "radix scatter does not fit on an SM"};
+    per_sm[dev] = p;
+  }
+  return std::min(nblk, per_sm[dev] * sms[dev]);
+}
+
+template <class V>
+void radix_sort_impl(u64 *keys, V *vals, i64 n, int nbits, Arena &ar, cudaStream_t s, u32 *err) {
   if (n <= 1 || nbits <= 0) return;
   if (n > i64(0xFFFFFFFFu)) throw Error{FCC_ERR_ARG, "radix sort: more than 2^32 keys"};
   const int nblk = int((n + kRsTile - 1) / kRsTile);
@@ -315,13 +437,17 @@ void radix_sort_impl(u64 *keys, V *vals, i64 n, int nbits, Arena &ar, cudaStream
   u32 *hist = ar.get_n<u32>(size_t(nblk) * 256);
   u64 *ka = keys, *kb = k2;
   V *va = vals, *vb = v2;
+  const int grid = rs_grid<V>(nblk);
+  const bool aligned = ((reinterpret_cast<uintptr_t>(keys) | reinterpret_cast<uintptr_t>(vals) |
+                         reinterpret_cast<uintptr_t>(k2) | reinterpret_cast<uintptr_t>(v2)) & 15) == 0;
   const int passes = (nbits + 7) / 8;
   for (int p = 0; p < passes; p++) {
     const int shift = 8 * p;
     k_rs_hist<<<nblk, kRsThreads, 0, s>>>(ka, n, shift, hist, nblk);
     FCC_LAUNCH_CHECK();
     scan_exclusive(hist, hist, i64(nblk) * 256, nullptr, ar, s);
-    k_rs_scatter<V><<<nblk, kRsThreads, 0, s>>>(ka, va, kb, vb, n, shift, hist, nblk);
+    k_rs_scatter<V><<<grid, kRsThreads, sizeof(RsSmem<V>), s>>>(ka, va, kb, vb, n, shift, hist, nblk,
+                                                                 aligned ? 1 : 0, err);
     FCC_LAUNCH_CHECK();
     std::swap(ka, kb);
     std::swap(va, vb);
@@ -333,12 +459,12 @@ void radix_sort_impl(u64 *keys, V *vals, i64 n, int nbits, Arena &ar, cudaStream
 }
 }  // namespace
 
-void radix_sort_pairs(u64 *keys, u32 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s) {
-  radix_sort_impl<u32>(keys, vals, n, nbits, ar, s);
+void radix_sort_pairs(u64 *keys, u32 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s, u32 *err) {
+  radix_sort_impl<u32>(keys, vals, n, nbits, ar, s, err);
 }
 
-void radix_sort_pairs64(u64 *keys, u64 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s) {
-  radix_sort_impl<u64>(keys, vals, n, nbits, ar, s);
+void radix_sort_pairs64(u64 *keys, u64 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s, u32 *err) {
+  radix_sort_impl<u64>(keys, vals, n, nbits, ar, s, err);
 }
 
 }  // namespace fcc
