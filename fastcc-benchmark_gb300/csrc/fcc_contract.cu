@@ -1515,31 +1515,183 @@ __global__ void __launch_bounds__(256) k_esc_expand(EscArgs a, const ProdSrc src
   }
 }
 
-__global__ void k_esc_flags(const u64 *__restrict__ keys, u64 n, u32 *__restrict__ flag) {
-  for (u64 i = u64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += u64(gridDim.x) * blockDim.x)
-    flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+// The sorted pairs are read in chunks of 256 positions, one warp per chunk,
+// eight consecutive positions per lane. A run of equal keys starts at a
+// "head" (position 0 or a key change); runs are numbered in key order by the
+// heads before them.
+constexpr u32 kEscPer = 8;
+constexpr u64 kEscChunk = 32 * kEscPer;
+
+struct EscLane {  // one lane's eight positions
+  u64 k[kEscPer];
+  u32 heads;  // bit q: position q starts a run
+};
+
+__device__ __forceinline__ EscLane esc_load_keys(const EscArgs &a, u64 c, u32 lane) {
+  EscLane L;
+  const u64 p0 = c * kEscChunk + lane * kEscPer;
+  if (p0 + kEscPer <= a.total) {  // 64 aligned bytes
+    const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(a.keys + p0);
+#pragma unroll
+    for (u32 q = 0; q < kEscPer / 2; q++) {
+      const ulonglong2 w = src[q];
+      L.k[2 * q] = w.x;
+      L.k[2 * q + 1] = w.y;
+    }
+  } else {
+#pragma unroll
+    for (u32 q = 0; q < kEscPer; q++) L.k[q] = p0 + q < a.total ? a.keys[p0 + q] : ~0ull;
+  }
+  u64 prev = __shfl_up_sync(kFull, L.k[kEscPer - 1], 1);
+  if (lane == 0 && c > 0) prev = a.keys[c * kEscChunk - 1];
+  L.heads = 0;
+#pragma unroll
+  for (u32 q = 0; q < kEscPer; q++) {
+    const u64 pk = q ? L.k[q - 1] : prev;
+    if (p0 + q < a.total && (p0 + q == 0 || L.k[q] != pk)) L.heads |= 1u << q;
+  }
+  return L;
+}
+
+// Heads per chunk (the runs' numbering, after an exclusive scan).
+__global__ void __launch_bounds__(256) k_esc_count(EscArgs a, u32 *__restrict__ chunk_heads) {
+  const u32 lane = threadIdx.x & 31;
+  const u64 nchunks = (a.total + kEscChunk - 1) / kEscChunk;
+  const u64 nw = (u64(gridDim.x) * blockDim.x) >> 5;
+  for (u64 c = (u64(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += nw) {
+    const EscLane L = esc_load_keys(a, c, lane);
+    u32 n = __popc(L.heads);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(kFull, n, o);
+    if (lane == 0) chunk_heads[c] = n;
+  }
 }
 
 __global__ void k_esc_reserve(const Out out, const u32 *__restrict__ nruns, u64 *__restrict__ base, u32 *err) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *base = reserve(out, *nruns, err);
 }
 
-// Each run of equal keys (starting where flag = 1) is summed in sorted order
-// by the thread whose position holds its start, and emitted at base + rank.
-__global__ void k_esc_reduce(EscArgs a, const u32 *__restrict__ flag, const u32 *__restrict__ rank,
-                             const u64 *__restrict__ base_p, const u32 *__restrict__ tile_rank0,
-                             const u64 *__restrict__ urow, const Out out, const Decode dec) {
+__device__ __forceinline__ void esc_emit(const EscArgs &a, const u32 *__restrict__ tile_rank0,
+                                         const u64 *__restrict__ urow, const Out &out, const Decode &dec,
+                                         u64 idx, u64 key, double v) {
+  const u64 s = key / a.span, rem = key - s * a.span;
+  const u64 slot = rem / a.LB, col = rem - slot * a.LB;
+  emit(out, dec, idx, __ldg(&urow[tile_rank0[a.tiles[s]] + slot]), col, v);
+}
+
+// Each run is summed and emitted (at base + its number) by the lane holding
+// its head: its values in that lane in order, then the following lanes'
+// values up to the next head (a segmented suffix sum over the lanes), then,
+// for the chunk's last run, the positions after the chunk up to the next key
+// change, found by a galloping search over the sorted keys and summed by the
+// warp. A chunk's positions before its first head belong to an earlier run.
+__global__ void __launch_bounds__(256) k_esc_reduce(EscArgs a, const u32 *__restrict__ chunk_off,
+                                                    const u64 *__restrict__ base_p,
+                                                    const u32 *__restrict__ tile_rank0,
+                                                    const u64 *__restrict__ urow, const Out out, const Decode dec) {
   const u64 base = *base_p;
   if (base == ~0ull) return;  // over capacity: counted by the cursor, retried by the host
-  for (u64 i = u64(blockIdx.x) * blockDim.x + threadIdx.x; i < a.total; i += u64(gridDim.x) * blockDim.x) {
-    if (!flag[i]) continue;
-    const u64 key = a.keys[i];
-    double v = __longlong_as_double((long long)a.vals[i]);
-    for (u64 j = i + 1; j < a.total && !flag[j]; j++) v += __longlong_as_double((long long)a.vals[j]);
-    const u64 s = key / a.span, rem = key - s * a.span;
-    const u64 slot = rem / a.LB, col = rem - slot * a.LB;
-    const u32 t = a.tiles[s];
-    emit(out, dec, base + rank[i], __ldg(&urow[tile_rank0[t] + slot]), col, v);
+  const u32 lane = threadIdx.x & 31;
+  const u64 nchunks = (a.total + kEscChunk - 1) / kEscChunk;
+  const u64 nw = (u64(gridDim.x) * blockDim.x) >> 5;
+  for (u64 c = (u64(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += nw) {
+    const EscLane L = esc_load_keys(a, c, lane);
+    const u64 p0 = c * kEscChunk + lane * kEscPer;
+    double v[kEscPer];
+    if (p0 + kEscPer <= a.total) {
+      const double2 *src = reinterpret_cast<const double2 *>(a.vals + p0);
+#pragma unroll
+      for (u32 q = 0; q < kEscPer / 2; q++) {
+        const double2 w = src[q];
+        v[2 * q] = w.x;
+        v[2 * q + 1] = w.y;
+      }
+    } else {
+#pragma unroll
+      for (u32 q = 0; q < kEscPer; q++)
+        v[q] = p0 + q < a.total ? __longlong_as_double((long long)a.vals[p0 + q]) : 0.0;
+    }
+    const u32 nh = __popc(L.heads);
+    u32 incl = nh;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const u32 t = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += t;
+    }
+    u64 run = u64(chunk_off[c]) + (incl - nh);  // number of the lane's first run
+    // In-lane runs; the lane's last run stays open.
+    double lead = 0.0, acc = 0.0;
+    u64 key = 0;
+    bool open = false;
+#pragma unroll
+    for (u32 q = 0; q < kEscPer; q++) {
+      if ((L.heads >> q) & 1u) {
+        if (open) esc_emit(a, tile_rank0, urow, out, dec, base + run++, key, acc);
+        open = true;
+        key = L.k[q];
+        acc = v[q];
+      } else if (open) {
+        acc += v[q];
+      } else {
+        lead += v[q];
+      }
+    }
+    // Suffix over lanes: t = this lane's lead plus, while no head stops it,
+    // the leads of the lanes after it.
+    double t = lead;
+    bool f = nh > 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double to = __shfl_down_sync(kFull, t, o);
+      const bool fo = __shfl_down_sync(kFull, f ? 1u : 0u, o) != 0;
+      if (lane + o < 32) {
+        if (!f) t += to;
+        f = f || fo;
+      }
+    }
+    double cont = __shfl_down_sync(kFull, t, 1);
+    bool stops = __shfl_down_sync(kFull, f ? 1u : 0u, 1) != 0;
+    if (lane == 31) {
+      cont = 0.0;
+      stops = false;
+    }
+    if (open) acc += cont;
+    // The chunk's last run may continue past the chunk.
+    const bool walk = open && !stops;
+    const u32 wm = __ballot_sync(kFull, walk);
+    if (wm) {
+      const u32 wl = __ffs(wm) - 1;
+      const u64 k0 = __shfl_sync(kFull, key, wl);
+      const u64 q0 = (c + 1) * kEscChunk;
+      u64 end = q0;  // first position after the run
+      if (lane == wl) {
+        u64 step = 1, lo = q0;  // keys[lo - 1] == k0 (or lo == q0)
+        while (lo < a.total && a.keys[lo] == k0) {
+          const u64 hi = min(a.total, lo + step);
+          if (a.keys[hi - 1] == k0) {
+            lo = hi;
+            step <<= 1;
+          } else {
+            u64 l = lo, h = hi - 1;  // keys[l] == k0, keys[h] != k0
+            while (h - l > 1) {
+              const u64 m = l + (h - l) / 2;
+              if (a.keys[m] == k0) l = m;
+              else h = m;
+            }
+            lo = h;
+            break;
+          }
+        }
+        end = lo;
+      }
+      end = __shfl_sync(kFull, end, wl);
+      double sum = 0.0;
+      for (u64 i = q0 + lane; i < end; i += 32) sum += __longlong_as_double((long long)a.vals[i]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+      if (lane == wl) acc += sum;
+    }
+    if (open) esc_emit(a, tile_rank0, urow, out, dec, base + run, key, acc);
   }
 }
 
@@ -1908,7 +2060,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (opt.dense_fill_log2 < 0 || opt.dense_fill_log2 > 40) throw Error{FCC_ERR_ARG, "dense_fill_log2 out of range"};
   if (opt.dense_staging < -1 || opt.dense_staging > 0) throw Error{FCC_ERR_ARG, "dense_staging must be -1 or 0"};
   if (opt.sched_mix_margin < 0 || opt.sched_mix_margin > 1000) throw Error{FCC_ERR_ARG, "bad sched_mix_margin"};
-  if (opt.hash_esc < 0 || opt.hash_esc > 1) throw Error{FCC_ERR_ARG, "hash_esc must be 0 or 1"};
+  if (opt.hash_esc < -1 || opt.hash_esc > 1) throw Error{FCC_ERR_ARG, "hash_esc must be -1, 0 or 1"};
   const bool learned = forced < 0 && opt.schedule == FCC_SCHED_LEARNED && ctx->sched && ctx->sched->model;
   const bool want_record = opt.timing == 2 && ctx->sched;
   // Row groups (batched contractions): dense tiles hold rows of one group,
@@ -2035,15 +2187,17 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   // tiles in class order (stable), so that each class's items are contiguous
   radix_sort_pairs(ckey, corder, nA2, 3, ar, st, ctx->d_err);
 
-  // Hash tiles too big for their table, on request (hash_esc = 1): expand,
-  // sort and reduce when the pairs fit (at most 56 bytes of temporaries per
-  // multiply-add, within half of the free device memory) and the key space
-  // fits 64 bits. Not the default: on the two-mode workload the radix sort of
-  // the pairs costs more than the global-hash merge it replaces.
+  // Hash tiles too big for their table: expand, sort and reduce when the
+  // pairs fit (at most 56 bytes of temporaries per multiply-add, within half
+  // of the free device memory) and the key space fits 64 bits; else (and with
+  // hash_esc = -1) split into items merged through a global hash table. A
+  // fixed workspace (the allocation-free call) expands only on request
+  // (hash_esc = 1), since the pairs may not fit where the hash tables do.
   const u64 esc_rows = grouped ? dense_cap : TL;
   bool esc = false;
+  const bool esc_wanted = opt.hash_esc > 0 || (opt.hash_esc == 0 && !ar.is_fixed());
   // (not while recording per-tile costs: expanded tiles have no work items to time)
-  if (opt.hash_esc > 0 && !want_record) {
+  if (esc_wanted && !want_record) {
     size_t fb = 0, tb = 0;
     FCC_CUDA(cudaMemGetInfo(&fb, &tb));
     const unsigned __int128 keyspace = (unsigned __int128)nA2 * esc_rows * LB;
@@ -2102,12 +2256,14 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
                                                    esc_flag, esc_idx, esc_off, esc_tiles, esc_base);
   FCC_LAUNCH_CHECK();
   EscArgs ea{esc_tiles, esc_base, nesc, esc_rows * LB, LB, nullptr, nullptr, esc_pairs};
-  u32 *esc_rflag = nullptr, *esc_rank = nullptr;
+  u32 *esc_heads = nullptr, *esc_off_c = nullptr;
+  const u64 esc_chunks = (esc_pairs + kEscChunk - 1) / kEscChunk;
+  const int esc_grid = int(std::max<u64>(1, std::min<u64>((esc_chunks + 7) / 8, u64(ctx->num_sms) * 8)));
   if (nesc > 0) {
     ea.keys = ar.get_n<u64>(esc_pairs);
     ea.vals = ar.get_n<u64>(esc_pairs);
-    esc_rflag = ar.get_n<u32>(esc_pairs);
-    esc_rank = ar.get_n<u32>(esc_pairs);
+    esc_heads = ar.get_n<u32>(esc_chunks);
+    esc_off_c = ar.get_n<u32>(esc_chunks);
   }
   const u64 words = dense ? (area + 31) / 32 : 0;
   double *gacc = nullptr;
@@ -2278,14 +2434,13 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
           k_esc_expand<ColT><<<std::min<u32>(nesc, u32(ctx->num_sms) * 8), 256, 0, st>>>(ea, src, colptr, tile_abeg);
           FCC_LAUNCH_CHECK();
           radix_sort_pairs64(ea.keys, ea.vals, i64(esc_pairs), bits_for(u64(nesc) * ea.span - 1), ar, st, ctx->d_err);
-          k_esc_flags<<<grid_for(i64(esc_pairs), 256), 256, 0, st>>>(ea.keys, esc_pairs, esc_rflag);
+          k_esc_count<<<esc_grid, 256, 0, st>>>(ea, esc_heads);
           FCC_LAUNCH_CHECK();
-          scan_exclusive(esc_rflag, esc_rank, i64(esc_pairs), sc32(S_ESC_RUNS), ar, st);
+          scan_exclusive(esc_heads, esc_off_c, i64(esc_chunks), sc32(S_ESC_RUNS), ar, st);
         }
         k_esc_reserve<<<1, 32, 0, st>>>(o, sc32(S_ESC_RUNS), d_sc + S_ESC_BASE, ctx->d_err);
         FCC_LAUNCH_CHECK();
-        k_esc_reduce<<<grid_for(i64(esc_pairs), 256), 256, 0, st>>>(ea, esc_rflag, esc_rank, d_sc + S_ESC_BASE,
-                                                                    tile_rank0, urow, o, dec);
+        k_esc_reduce<<<esc_grid, 256, 0, st>>>(ea, esc_off_c, d_sc + S_ESC_BASE, tile_rank0, urow, o, dec);
         FCC_LAUNCH_CHECK();
       }
     };

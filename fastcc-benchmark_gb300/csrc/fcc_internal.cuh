@@ -113,6 +113,7 @@ class Arena {
   template <class T> T *get_n(size_t n) { return static_cast<T *>(get(sizeof(T) * (n ? n : 1))); }
   void release_all(cudaStream_t s);
   size_t high_water() const { return high_; }
+  bool is_fixed() const { return fixed_; }
 
  private:
   struct Chunk { char *p; size_t size; };

@@ -257,6 +257,19 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_hist(const u64 *__restrict__ 
   }
 }
 
+// Lanes of the warp whose 9-bit label equals this lane's: one ballot per
+// label bit, a lane keeps the lanes that agree with it on every bit.
+__device__ __forceinline__ u32 lanes_equal9(u32 label) {
+  u32 m = kFull;
+#pragma unroll
+  for (int bit = 0; bit < 9; bit++) {
+    const bool set = (label >> bit) & 1u;
+    const u32 v = __ballot_sync(kFull, set);
+    m &= set ? v : ~v;
+  }
+  return m;
+}
+
 // Shared memory of the scatter: two tile buffers (the next tile is copied in
 // while the current one is ranked), per-warp digit counters, which the tile's
 // source order reuses once the ranks are final, and the tile's output bases.
@@ -332,18 +345,24 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const u64 *__restrict
     const int wbase = warp * (kRsItems * 32);
     u32 r[kRsItems], dg[kRsItems];
 #pragma unroll
-    for (int j = 0; j < kRsItems; j++) {
+    for (int j = 0; j < kRsItems; j++) {  // digits first (256: no key), then the lanes sharing each
       const int idx = wbase + j * 32 + lane;
-      const bool valid = idx < cnt;
-      const u32 d = valid ? (u32(S.keys[b][idx] >> shift) & 255u) : (256u + lane);
-      const u32 peers = __match_any_sync(kFull, d);
+      dg[j] = idx < cnt ? (u32(S.keys[b][idx] >> shift) & 255u) : 256u;
+    }
+#pragma unroll
+    for (int j = 0; j < kRsItems; j++) r[j] = lanes_equal9(dg[j]);
+    // The per-warp counters are the only chain: one shared read and one
+    // write per step.
+#pragma unroll
+    for (int j = 0; j < kRsItems; j++) {
+      const u32 d = dg[j], peers = r[j];
+      const bool valid = d < 256u;
       u32 before = 0;
       if (valid) before = S.u.wcnt[warp][d];
       __syncwarp();
       if (valid && lane == __ffs(peers) - 1) S.u.wcnt[warp][d] = before + __popc(peers);
       __syncwarp();
       r[j] = before + __popc(peers & lt_mask);
-      dg[j] = d;
     }
     __syncthreads();
     // Thread d: the tile's count of digit d, its start in the tile's sorted
@@ -375,15 +394,15 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const u64 *__restrict
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < kRsItems; j++)
-      if (wbase + j * 32 + lane < cnt) r[j] += S.u.wcnt[warp][dg[j]];
+      if (dg[j] < 256u) r[j] += S.u.wcnt[warp][dg[j]];
     __syncthreads();  // the counters are dead: their space takes the source order
 #pragma unroll
     for (int j = 0; j < kRsItems; j++)
-      if (wbase + j * 32 + lane < cnt) S.u.sidx[r[j]] = (unsigned short)(wbase + j * 32 + lane);
+      if (dg[j] < 256u) S.u.sidx[r[j]] = (unsigned short)(wbase + j * 32 + lane);
     __syncthreads();
     // Out in sorted order: consecutive threads write consecutive positions of
     // one digit's run.
-#pragma unroll 4
+#pragma unroll
     for (int q = 0; q < kRsItems; q++) {
       const int i = q * kRsThreads + tid;
       if (i < cnt) {

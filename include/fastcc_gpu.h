@@ -110,9 +110,11 @@ typedef struct fcc_options {
   int32_t sched_mix_margin;   /* FCC_SCHED_LEARNED: 0 (default): per-tile choices; > 0: one class for
                                  every tile unless the model predicts the per-tile mix faster than
                                  the best single class by this many percent */
-  int32_t hash_esc;           /* 0 (default): hash tiles larger than their table are split into
-                                 items merged through a global hash table; 1: expanded to (key,
-                                 value) pairs, radix-sorted and reduced when the pairs fit */
+  int32_t hash_esc;           /* hash tiles larger than their table. 0 (default): expanded to (key,
+                                 value) pairs, radix-sorted and reduced when the pairs fit in
+                                 device memory (allocation-free calls: as -1); 1: the same, also in
+                                 allocation-free calls; -1: split into items merged through a
+                                 global hash table */
 } fcc_options;
 
 /* Tile classes: every output tile runs in one of them. The hash classes

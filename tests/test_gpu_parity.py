@@ -31,7 +31,10 @@ VARIANTS = [
     {},
     {"accumulator": F.ACC_HASH},
     {"products_per_item": 7},                               # forces split tiles
-    {"accumulator": F.ACC_HASH, "products_per_item": 5},    # global hash merge
+    {"accumulator": F.ACC_HASH, "products_per_item": 5},    # expand-sort-reduce (default)
+    {"accumulator": F.ACC_HASH, "products_per_item": 5, "hash_esc": -1},   # global hash merge
+    {"accumulator": F.ACC_HASH, "hash_slots": 64, "hash_esc": -1},
+    {"schedule": F.SCHED_FORCE + F.CLASS_HASH_S, "products_per_item": 40, "hash_esc": -1},
     {"rows_per_tile": 1},
     {"dense_cap": 2048, "products_per_item": 300},
     {"capacity_hint": 3},                                   # overflow -> exact-count retry
@@ -261,4 +264,27 @@ def test_staged_phase1_matches_oracle(ctx, staging):
                  {"dense_staging": staging, "products_per_item": 3000}):
         c, v, prods = run_gpu(ctx, *args, **opts)
         assert prods == o["products"]
+        check_parity(c, v, o["coords"], o["values"], o["abs_sum"])
+
+
+@pytest.mark.parametrize("rows,cols,k", [(3, 2, 4000), (1, 1, 70_000), (40, 37, 300)])
+def test_long_runs_of_equal_outputs(ctx, rows, cols, k):
+    # C(i, j) = sum_k A(i, k) B(k, j) with every k present: each output gets k
+    # products, so the sorted pairs of a split hash tile hold runs of k equal
+    # keys that cross many 256-position chunks of the reduction
+    rng = np.random.Generator(np.random.PCG64(rows * 1000 + k))
+    ii, kk = np.meshgrid(np.arange(rows), np.arange(k), indexing="ij")
+    a_c = np.stack([ii.ravel(), kk.ravel()], axis=1).astype(np.int32)
+    kk2, jj = np.meshgrid(np.arange(k), np.arange(cols), indexing="ij")
+    b_c = np.stack([kk2.ravel(), jj.ravel()], axis=1).astype(np.int32)
+    a_v = rng.uniform(-1, 1, a_c.shape[0])
+    b_v = rng.uniform(-1, 1, b_c.shape[0])
+    am, bm = np.array([rows - 1, k - 1], np.int32), np.array([k - 1, cols - 1], np.int32)
+    args = (a_c, a_v, am, b_c, b_v, bm, [1], [0])
+    o = run_oracle(*args)
+    for opts in ({"accumulator": F.ACC_HASH, "hash_slots": 64},
+                 {"accumulator": F.ACC_HASH, "hash_slots": 64, "hash_esc": -1},
+                 {"accumulator": F.ACC_HASH, "products_per_item": 100}):
+        c, v, prods = run_gpu(ctx, *args, **opts)
+        assert prods == o["products"] == rows * cols * k
         check_parity(c, v, o["coords"], o["values"], o["abs_sum"])
