@@ -1487,15 +1487,16 @@ struct EscArgs {
   const u64 *base;      // esc index -> first pair
   u32 n;                // esc tiles
   u64 span, LB;         // key = s * span + slot * LB + col
-  u64 *keys;
+  void *keys;           // u32 when every key fits 32 bits, else u64
   u64 *vals;            // the products' bits (double), sorted along with the keys
   u64 total;            // pairs
 };
 
 // One CTA per esc tile (grid-stride), one warp per A entry of the tile.
-template <class ColT>
+template <class ColT, class KeyT>
 __global__ void __launch_bounds__(256) k_esc_expand(EscArgs a, const ProdSrc src, const ColT *__restrict__ colB,
                                                     const u32 *__restrict__ tile_abeg) {
+  KeyT *keys = static_cast<KeyT *>(a.keys);
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (u32 s = blockIdx.x; s < a.n; s += gridDim.x) {
     const u32 t = a.tiles[s];
@@ -1508,7 +1509,7 @@ __global__ void __launch_bounds__(256) k_esc_expand(EscArgs a, const ProdSrc src
       const u32 sb = __ldg(&src.sbA[e]);
       const u64 off = base + (pe - p0);
       for (u64 i = lane; i < len; i += 32) {
-        a.keys[off + i] = kb + u64(__ldg(&colB[sb + i]));
+        keys[off + i] = KeyT(kb + u64(__ldg(&colB[sb + i])));
         a.vals[off + i] = u64(__double_as_longlong(va * __ldg(&src.valB[sb + i])));
       }
     }
@@ -1527,23 +1528,38 @@ struct EscLane {  // one lane's eight positions
   u32 heads;  // bit q: position q starts a run
 };
 
+template <class KeyT>
 __device__ __forceinline__ EscLane esc_load_keys(const EscArgs &a, u64 c, u32 lane) {
+  static_assert(sizeof(KeyT) == 4 || sizeof(KeyT) == 8, "32- or 64-bit keys");
+  const KeyT *keys = static_cast<const KeyT *>(a.keys);
   EscLane L;
   const u64 p0 = c * kEscChunk + lane * kEscPer;
-  if (p0 + kEscPer <= a.total) {  // 64 aligned bytes
-    const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(a.keys + p0);
+  if (p0 + kEscPer <= a.total) {  // 32 or 64 aligned bytes
+    if (sizeof(KeyT) == 8) {
+      const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(keys + p0);
 #pragma unroll
-    for (u32 q = 0; q < kEscPer / 2; q++) {
-      const ulonglong2 w = src[q];
-      L.k[2 * q] = w.x;
-      L.k[2 * q + 1] = w.y;
+      for (u32 q = 0; q < kEscPer / 2; q++) {
+        const ulonglong2 w = src[q];
+        L.k[2 * q] = w.x;
+        L.k[2 * q + 1] = w.y;
+      }
+    } else {
+      const uint4 *src = reinterpret_cast<const uint4 *>(keys + p0);
+#pragma unroll
+      for (u32 q = 0; q < kEscPer / 4; q++) {
+        const uint4 w = src[q];
+        L.k[4 * q] = w.x;
+        L.k[4 * q + 1] = w.y;
+        L.k[4 * q + 2] = w.z;
+        L.k[4 * q + 3] = w.w;
+      }
     }
   } else {
 #pragma unroll
-    for (u32 q = 0; q < kEscPer; q++) L.k[q] = p0 + q < a.total ? a.keys[p0 + q] : ~0ull;
+    for (u32 q = 0; q < kEscPer; q++) L.k[q] = p0 + q < a.total ? u64(keys[p0 + q]) : ~0ull;
   }
   u64 prev = __shfl_up_sync(kFull, L.k[kEscPer - 1], 1);
-  if (lane == 0 && c > 0) prev = a.keys[c * kEscChunk - 1];
+  if (lane == 0 && c > 0) prev = keys[c * kEscChunk - 1];
   L.heads = 0;
 #pragma unroll
   for (u32 q = 0; q < kEscPer; q++) {
@@ -1554,12 +1570,13 @@ __device__ __forceinline__ EscLane esc_load_keys(const EscArgs &a, u64 c, u32 la
 }
 
 // Heads per chunk (the runs' numbering, after an exclusive scan).
+template <class KeyT>
 __global__ void __launch_bounds__(256) k_esc_count(EscArgs a, u32 *__restrict__ chunk_heads) {
   const u32 lane = threadIdx.x & 31;
   const u64 nchunks = (a.total + kEscChunk - 1) / kEscChunk;
   const u64 nw = (u64(gridDim.x) * blockDim.x) >> 5;
   for (u64 c = (u64(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += nw) {
-    const EscLane L = esc_load_keys(a, c, lane);
+    const EscLane L = esc_load_keys<KeyT>(a, c, lane);
     u32 n = __popc(L.heads);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(kFull, n, o);
@@ -1585,6 +1602,7 @@ __device__ __forceinline__ void esc_emit(const EscArgs &a, const u32 *__restrict
 // for the chunk's last run, the positions after the chunk up to the next key
 // change, found by a galloping search over the sorted keys and summed by the
 // warp. A chunk's positions before its first head belong to an earlier run.
+template <class KeyT>
 __global__ void __launch_bounds__(256) k_esc_reduce(EscArgs a, const u32 *__restrict__ chunk_off,
                                                     const u64 *__restrict__ base_p,
                                                     const u32 *__restrict__ tile_rank0,
@@ -1595,7 +1613,7 @@ __global__ void __launch_bounds__(256) k_esc_reduce(EscArgs a, const u32 *__rest
   const u64 nchunks = (a.total + kEscChunk - 1) / kEscChunk;
   const u64 nw = (u64(gridDim.x) * blockDim.x) >> 5;
   for (u64 c = (u64(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += nw) {
-    const EscLane L = esc_load_keys(a, c, lane);
+    const EscLane L = esc_load_keys<KeyT>(a, c, lane);
     const u64 p0 = c * kEscChunk + lane * kEscPer;
     double v[kEscPer];
     if (p0 + kEscPer <= a.total) {
@@ -1665,17 +1683,18 @@ __global__ void __launch_bounds__(256) k_esc_reduce(EscArgs a, const u32 *__rest
       const u64 q0 = (c + 1) * kEscChunk;
       u64 end = q0;  // first position after the run
       if (lane == wl) {
+        const KeyT *keys = static_cast<const KeyT *>(a.keys);
         u64 step = 1, lo = q0;  // keys[lo - 1] == k0 (or lo == q0)
-        while (lo < a.total && a.keys[lo] == k0) {
+        while (lo < a.total && keys[lo] == k0) {
           const u64 hi = min(a.total, lo + step);
-          if (a.keys[hi - 1] == k0) {
+          if (keys[hi - 1] == k0) {
             lo = hi;
             step <<= 1;
           } else {
             u64 l = lo, h = hi - 1;  // keys[l] == k0, keys[h] != k0
             while (h - l > 1) {
               const u64 m = l + (h - l) / 2;
-              if (a.keys[m] == k0) l = m;
+              if (keys[m] == k0) l = m;
               else h = m;
             }
             lo = h;
@@ -2259,8 +2278,10 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   u32 *esc_heads = nullptr, *esc_off_c = nullptr;
   const u64 esc_chunks = (esc_pairs + kEscChunk - 1) / kEscChunk;
   const int esc_grid = int(std::max<u64>(1, std::min<u64>((esc_chunks + 7) / 8, u64(ctx->num_sms) * 8)));
+  const int esc_bits = nesc > 0 ? bits_for(u64(nesc) * ea.span - 1) : 0;
+  const bool esc_k32 = esc_bits <= 32;  // 32-bit keys: a quarter less traffic per sort pass
   if (nesc > 0) {
-    ea.keys = ar.get_n<u64>(esc_pairs);
+    ea.keys = esc_k32 ? static_cast<void *>(ar.get_n<u32>(esc_pairs)) : static_cast<void *>(ar.get_n<u64>(esc_pairs));
     ea.vals = ar.get_n<u64>(esc_pairs);
     esc_heads = ar.get_n<u32>(esc_chunks);
     esc_off_c = ar.get_n<u32>(esc_chunks);
@@ -2431,16 +2452,25 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       }
       if (nesc > 0) {  // hub hash tiles: expand, sort, reduce
         if (attempt == 0) {
-          k_esc_expand<ColT><<<std::min<u32>(nesc, u32(ctx->num_sms) * 8), 256, 0, st>>>(ea, src, colptr, tile_abeg);
-          FCC_LAUNCH_CHECK();
-          radix_sort_pairs64(ea.keys, ea.vals, i64(esc_pairs), bits_for(u64(nesc) * ea.span - 1), ar, st, ctx->d_err);
-          k_esc_count<<<esc_grid, 256, 0, st>>>(ea, esc_heads);
+          const u32 xgrid = std::min<u32>(nesc, u32(ctx->num_sms) * 8);
+          if (esc_k32) {
+            k_esc_expand<ColT, u32><<<xgrid, 256, 0, st>>>(ea, src, colptr, tile_abeg);
+            FCC_LAUNCH_CHECK();
+            radix_sort_pairs64(static_cast<u32 *>(ea.keys), ea.vals, i64(esc_pairs), esc_bits, ar, st, ctx->d_err);
+            k_esc_count<u32><<<esc_grid, 256, 0, st>>>(ea, esc_heads);
+          } else {
+            k_esc_expand<ColT, u64><<<xgrid, 256, 0, st>>>(ea, src, colptr, tile_abeg);
+            FCC_LAUNCH_CHECK();
+            radix_sort_pairs64(static_cast<u64 *>(ea.keys), ea.vals, i64(esc_pairs), esc_bits, ar, st, ctx->d_err);
+            k_esc_count<u64><<<esc_grid, 256, 0, st>>>(ea, esc_heads);
+          }
           FCC_LAUNCH_CHECK();
           scan_exclusive(esc_heads, esc_off_c, i64(esc_chunks), sc32(S_ESC_RUNS), ar, st);
         }
         k_esc_reserve<<<1, 32, 0, st>>>(o, sc32(S_ESC_RUNS), d_sc + S_ESC_BASE, ctx->d_err);
         FCC_LAUNCH_CHECK();
-        k_esc_reduce<<<esc_grid, 256, 0, st>>>(ea, esc_off_c, d_sc + S_ESC_BASE, tile_rank0, urow, o, dec);
+        if (esc_k32) k_esc_reduce<u32><<<esc_grid, 256, 0, st>>>(ea, esc_off_c, d_sc + S_ESC_BASE, tile_rank0, urow, o, dec);
+        else k_esc_reduce<u64><<<esc_grid, 256, 0, st>>>(ea, esc_off_c, d_sc + S_ESC_BASE, tile_rank0, urow, o, dec);
         FCC_LAUNCH_CHECK();
       }
     };

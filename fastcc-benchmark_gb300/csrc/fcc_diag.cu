@@ -139,18 +139,19 @@ extern "C" int fcc_diag_fp64_fma_rate(int32_t device, double *fma_per_second) {
 // 64-bit payloads) are copied to the device, sorted `reps` times from the
 // same unsorted copy, and the sorted pairs come back; *ms_per_sort is the
 // mean device time of one sort (CUDA events around the sort alone).
-extern "C" int fcc_diag_radix_sort(const uint64_t *keys, const void *vals, int64_t n, int32_t nbits,
-                                   int32_t value_bytes, int32_t reps, uint64_t *keys_out, void *vals_out,
+extern "C" int fcc_diag_radix_sort(const void *keys, int32_t key_bytes, const void *vals, int32_t value_bytes,
+                                   int64_t n, int32_t nbits, int32_t reps, void *keys_out, void *vals_out,
                                    double *ms_per_sort) {
   using namespace fcc;
-  if (n < 0 || nbits < 0 || nbits > 64 || reps < 1 || (value_bytes != 4 && value_bytes != 8) ||
+  const bool combo = (key_bytes == 8 && (value_bytes == 4 || value_bytes == 8)) || (key_bytes == 4 && value_bytes == 8);
+  if (n < 0 || nbits < 0 || nbits > 8 * key_bytes || reps < 1 || !combo ||
       (n > 0 && (!keys || !vals || !keys_out || !vals_out)) || !ms_per_sort || n > i64(0xFFFFFFFFu))
     return FCC_ERR_ARG;
   *ms_per_sort = 0;
   if (n == 0) return FCC_OK;
-  const size_t kb = (sizeof(u64) * size_t(n) + 255) & ~size_t(255);
+  const size_t kb = (size_t(key_bytes) * size_t(n) + 255) & ~size_t(255);
   const size_t vb = (size_t(value_bytes) * size_t(n) + 255) & ~size_t(255);
-  const size_t kn = sizeof(u64) * size_t(n), vn = size_t(value_bytes) * size_t(n);
+  const size_t kn = size_t(key_bytes) * size_t(n), vn = size_t(value_bytes) * size_t(n);
   const size_t nblk = (size_t(n) + 4095) / 4096;
   const size_t scratch = kb + vb + nblk * 256 * 8 + (size_t(16) << 20);
   char *d = nullptr;
@@ -165,7 +166,7 @@ extern "C" int fcc_diag_radix_sort(const uint64_t *keys, const void *vals, int64
     FCC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     FCC_CUDA(cudaEventCreate(&e0));
     FCC_CUDA(cudaEventCreate(&e1));
-    u64 *k0 = reinterpret_cast<u64 *>(d), *k1 = reinterpret_cast<u64 *>(d + kb);
+    char *k0 = d, *k1 = d + kb;
     char *v0 = d + 2 * kb, *v1 = v0 + vb;
     u32 *err = reinterpret_cast<u32 *>(v1 + vb);
     Arena ar;
@@ -179,8 +180,12 @@ extern "C" int fcc_diag_radix_sort(const uint64_t *keys, const void *vals, int64
       FCC_CUDA(cudaMemcpyAsync(v1, v0, vn, cudaMemcpyDeviceToDevice, st));
       ar.begin(st);
       FCC_CUDA(cudaEventRecord(e0, st));
-      if (value_bytes == 4) radix_sort_pairs(k1, reinterpret_cast<u32 *>(v1), n, nbits, ar, st, err);
-      else radix_sort_pairs64(k1, reinterpret_cast<u64 *>(v1), n, nbits, ar, st, err);
+      if (key_bytes == 4)
+        radix_sort_pairs64(reinterpret_cast<u32 *>(k1), reinterpret_cast<u64 *>(v1), n, nbits, ar, st, err);
+      else if (value_bytes == 4)
+        radix_sort_pairs(reinterpret_cast<u64 *>(k1), reinterpret_cast<u32 *>(v1), n, nbits, ar, st, err);
+      else
+        radix_sort_pairs64(reinterpret_cast<u64 *>(k1), reinterpret_cast<u64 *>(v1), n, nbits, ar, st, err);
       FCC_CUDA(cudaEventRecord(e1, st));
       FCC_CUDA(cudaEventSynchronize(e1));
       float ms = 0;

@@ -218,6 +218,8 @@ void scan_exclusive_wide(const u32 *in, u64 *out, i64 n, u64 *total, Arena &ar, 
 void radix_sort_pairs(u64 *keys, u32 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s, u32 *err);
 void radix_sort_pairs64(u64 *keys, u64 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s,
                         u32 *err);  // 64-bit payload
+void radix_sort_pairs64(u32 *keys, u64 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s,
+                        u32 *err);  // 32-bit keys (nbits <= 32), 64-bit payload
 
 inline int grid_for(i64 n, int threads, int max_blocks = 1 << 20) {
   i64 b = (n + threads - 1) / threads;

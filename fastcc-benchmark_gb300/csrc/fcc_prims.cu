@@ -232,14 +232,15 @@ constexpr int kRsItems = 16;
 constexpr int kRsTile = kRsThreads * kRsItems;  // 4096 keys per tile
 static_assert(kRsThreads == 256, "the scatter scans one digit per thread");
 
-__global__ void __launch_bounds__(kRsThreads) k_rs_hist(const u64 *__restrict__ keys, i64 n, int shift,
+template <class K>
+__global__ void __launch_bounds__(kRsThreads) k_rs_hist(const K *__restrict__ keys, i64 n, int shift,
                                                         u32 *__restrict__ hist, int nblk) {
   __shared__ u32 h[kRsWarps][256];
   for (int i = threadIdx.x; i < kRsWarps * 256; i += kRsThreads) (&h[0][0])[i] = 0;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const i64 base = i64(blockIdx.x) * kRsTile + warp * (kRsItems * 32);
-  u64 k[kRsItems];  // every load in flight before the first count
+  K k[kRsItems];  // every load in flight before the first count
 #pragma unroll
   for (int j = 0; j < kRsItems; j++) {
     i64 i = base + j * 32 + lane;
@@ -273,9 +274,9 @@ __device__ __forceinline__ u32 lanes_equal9(u32 label) {
 // Shared memory of the scatter: two tile buffers (the next tile is copied in
 // while the current one is ranked), per-warp digit counters, which the tile's
 // source order reuses once the ranks are final, and the tile's output bases.
-template <class V>
+template <class K, class V>
 struct RsSmem {
-  u64 keys[2][kRsTile];
+  K keys[2][kRsTile];
   V vals[2][kRsTile];
   union {
     u32 wcnt[kRsWarps][256];
@@ -292,14 +293,14 @@ static_assert(kRsTile <= 65536, "tile positions are 16-bit");
 // bulk copy of the next tile's keys and values before the current tile is
 // ranked, so the load latency stays off the critical path. Partial tiles (or
 // bases that are not 16-byte aligned, bulk == 0) are loaded by all threads.
-template <class V>
-__global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const u64 *__restrict__ kin,
+template <class K, class V>
+__global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const K *__restrict__ kin,
                                                            const V *__restrict__ vin,
-                                                           u64 *__restrict__ kout, V *__restrict__ vout,
+                                                           K *__restrict__ kout, V *__restrict__ vout,
                                                            i64 n, int shift, const u32 *__restrict__ offs,
                                                            int nblk, int bulk, u32 *err) {
   extern __shared__ __align__(128) unsigned char rs_raw[];
-  RsSmem<V> &S = *reinterpret_cast<RsSmem<V> *>(rs_raw);
+  RsSmem<K, V> &S = *reinterpret_cast<RsSmem<K, V> *>(rs_raw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const u32 lt_mask = (1u << lane) - 1u;
   const int G = gridDim.x;
@@ -308,8 +309,8 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const u64 *__restrict
   auto issue = [&](int t, int b) {  // thread 0
     if (staged(t)) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // after the buffer's last generic reads
-      mbar_arrive_tx(&S.full[b], u32(kRsTile * (sizeof(u64) + sizeof(V))));
-      bulk_g2s(S.keys[b], kin + i64(t) * kRsTile, u32(kRsTile * sizeof(u64)), &S.full[b]);
+      mbar_arrive_tx(&S.full[b], u32(kRsTile * (sizeof(K) + sizeof(V))));
+      bulk_g2s(S.keys[b], kin + i64(t) * kRsTile, u32(kRsTile * sizeof(K)), &S.full[b]);
       bulk_g2s(S.vals[b], vin + i64(t) * kRsTile, u32(kRsTile * sizeof(V)), &S.full[b]);
     } else {
       mbar_arrive(&S.full[b]);  // completes the phase; the threads load the tile themselves
@@ -407,7 +408,7 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const u64 *__restrict
       const int i = q * kRsThreads + tid;
       if (i < cnt) {
         const int src = S.u.sidx[i];
-        const u64 key = S.keys[b][src];
+        const K key = S.keys[b][src];
         const u32 pos = S.gbase[u32(key >> shift) & 255u] + u32(i);
         kout[pos] = key;
         vout[pos] = S.vals[b][src];
@@ -428,17 +429,17 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const u64 *__restrict
 }  // namespace
 
 namespace {
-template <class V>
+template <class K, class V>
 int rs_grid(int nblk) {
   static int per_sm[64] = {0}, sms[64] = {0};
   int dev = 0;
   FCC_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) throw Error{FCC_ERR_CUDA, "device ordinal out of range"};
   if (per_sm[dev] == 0) {
-    const int smem = int(sizeof(RsSmem<V>));
-    FCC_CUDA(cudaFuncSetAttribute(k_rs_scatter<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    const int smem = int(sizeof(RsSmem<K, V>));
+    FCC_CUDA(cudaFuncSetAttribute(k_rs_scatter<K, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int p = 0;
-    FCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, k_rs_scatter<V>, kRsThreads, smem));
+    FCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, k_rs_scatter<K, V>, kRsThreads, smem));
     FCC_CUDA(cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev));
     if (p < 1) throw Error{FCC_ERR_CUDA, "radix scatter does not fit on an SM"};
     per_sm[dev] = p;
@@ -446,44 +447,49 @@ int rs_grid(int nblk) {
   return std::min(nblk, per_sm[dev] * sms[dev]);
 }
 
-template <class V>
-void radix_sort_impl(u64 *keys, V *vals, i64 n, int nbits, Arena &ar, cudaStream_t s, u32 *err) {
+template <class K, class V>
+void radix_sort_impl(K *keys, V *vals, i64 n, int nbits, Arena &ar, cudaStream_t s, u32 *err) {
   if (n <= 1 || nbits <= 0) return;
   if (n > i64(0xFFFFFFFFu)) throw Error{FCC_ERR_ARG, "radix sort: more than 2^32 keys"};
   const int nblk = int((n + kRsTile - 1) / kRsTile);
-  u64 *k2 = ar.get_n<u64>(size_t(n));
+  K *k2 = ar.get_n<K>(size_t(n));
   V *v2 = ar.get_n<V>(size_t(n));
   u32 *hist = ar.get_n<u32>(size_t(nblk) * 256);
-  u64 *ka = keys, *kb = k2;
+  K *ka = keys, *kb = k2;
   V *va = vals, *vb = v2;
-  const int grid = rs_grid<V>(nblk);
+  const int grid = rs_grid<K, V>(nblk);
   const bool aligned = ((reinterpret_cast<uintptr_t>(keys) | reinterpret_cast<uintptr_t>(vals) |
                          reinterpret_cast<uintptr_t>(k2) | reinterpret_cast<uintptr_t>(v2)) & 15) == 0;
   const int passes = (nbits + 7) / 8;
   for (int p = 0; p < passes; p++) {
     const int shift = 8 * p;
-    k_rs_hist<<<nblk, kRsThreads, 0, s>>>(ka, n, shift, hist, nblk);
+    k_rs_hist<K><<<nblk, kRsThreads, 0, s>>>(ka, n, shift, hist, nblk);
     FCC_LAUNCH_CHECK();
     scan_exclusive(hist, hist, i64(nblk) * 256, nullptr, ar, s);
-    k_rs_scatter<V><<<grid, kRsThreads, sizeof(RsSmem<V>), s>>>(ka, va, kb, vb, n, shift, hist, nblk,
-                                                                 aligned ? 1 : 0, err);
+    k_rs_scatter<K, V><<<grid, kRsThreads, sizeof(RsSmem<K, V>), s>>>(ka, va, kb, vb, n, shift, hist, nblk,
+                                                                       aligned ? 1 : 0, err);
     FCC_LAUNCH_CHECK();
     std::swap(ka, kb);
     std::swap(va, vb);
   }
   if (ka != keys) {
-    FCC_CUDA(cudaMemcpyAsync(keys, ka, sizeof(u64) * size_t(n), cudaMemcpyDeviceToDevice, s));
+    FCC_CUDA(cudaMemcpyAsync(keys, ka, sizeof(K) * size_t(n), cudaMemcpyDeviceToDevice, s));
     FCC_CUDA(cudaMemcpyAsync(vals, va, sizeof(V) * size_t(n), cudaMemcpyDeviceToDevice, s));
   }
 }
 }  // namespace
 
 void radix_sort_pairs(u64 *keys, u32 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s, u32 *err) {
-  radix_sort_impl<u32>(keys, vals, n, nbits, ar, s, err);
+  radix_sort_impl<u64, u32>(keys, vals, n, nbits, ar, s, err);
 }
 
 void radix_sort_pairs64(u64 *keys, u64 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s, u32 *err) {
-  radix_sort_impl<u64>(keys, vals, n, nbits, ar, s, err);
+  radix_sort_impl<u64, u64>(keys, vals, n, nbits, ar, s, err);
+}
+
+void radix_sort_pairs64(u32 *keys, u64 *vals, i64 n, int nbits, Arena &ar, cudaStream_t s, u32 *err) {
+  if (nbits > 32) throw Error{FCC_ERR_ARG, "radix sort: more bits than a 32-bit key holds"};
+  radix_sort_impl<u32, u64>(keys, vals, n, nbits, ar, s, err);
 }
 
 }  // namespace fcc

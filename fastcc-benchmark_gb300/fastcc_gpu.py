@@ -461,15 +461,15 @@ def shared_update_rate(mode):
 def radix_sort(keys, vals, nbits, reps=1):
     """The library's stable radix sort of (keys, vals) on the low nbits of
     each key: returns (sorted keys, permuted vals, mean ms per sort)."""
-    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    keys = np.ascontiguousarray(keys)
     vals = np.ascontiguousarray(vals)
-    if vals.dtype.itemsize not in (4, 8) or vals.shape != keys.shape:
-        raise ValueError("vals: one 32- or 64-bit payload per key")
+    if keys.dtype not in (np.uint32, np.uint64) or vals.dtype.itemsize not in (4, 8) or vals.shape != keys.shape:
+        raise ValueError("keys: uint32 or uint64; vals: one 32- or 64-bit payload per key")
     ko, vo = np.empty_like(keys), np.empty_like(vals)
     ms = ctypes.c_double()
-    rc = lib().fcc_diag_radix_sort(keys.ctypes.data_as(ctypes.c_void_p), vals.ctypes.data_as(ctypes.c_void_p),
-                                   ctypes.c_int64(keys.size), ctypes.c_int32(nbits),
-                                   ctypes.c_int32(vals.dtype.itemsize), ctypes.c_int32(reps),
+    rc = lib().fcc_diag_radix_sort(keys.ctypes.data_as(ctypes.c_void_p), ctypes.c_int32(keys.dtype.itemsize),
+                                   vals.ctypes.data_as(ctypes.c_void_p), ctypes.c_int32(vals.dtype.itemsize),
+                                   ctypes.c_int64(keys.size), ctypes.c_int32(nbits), ctypes.c_int32(reps),
                                    ko.ctypes.data_as(ctypes.c_void_p), vo.ctypes.data_as(ctypes.c_void_p),
                                    ctypes.byref(ms))
     if rc != 0:

@@ -366,12 +366,12 @@ int fcc_diag_fp64_fma_rate(int32_t device, double *fma_per_second);
 int fcc_diag_shared_update_rate(int32_t mode, double *updates_per_second);
 
 /* Diagnostics: the library's stable LSD radix sort (8-bit digits over the
- * low nbits of each key) on caller data. keys[n] with payloads vals[n] of
- * value_bytes (4 or 8) each, host memory; the sorted pairs are written to
- * keys_out / vals_out, and *ms_per_sort receives the mean device time of one
- * sort over `reps` sorts of the same input. */
-int fcc_diag_radix_sort(const uint64_t *keys, const void *vals, int64_t n, int32_t nbits, int32_t value_bytes,
-                        int32_t reps, uint64_t *keys_out, void *vals_out, double *ms_per_sort);
+ * low nbits of each key) on caller data. keys[n] of key_bytes each with
+ * payloads vals[n] of value_bytes each (8/4, 8/8 or 4/8), host memory; the
+ * sorted pairs are written to keys_out / vals_out, and *ms_per_sort receives
+ * the mean device time of one sort over `reps` sorts of the same input. */
+int fcc_diag_radix_sort(const void *keys, int32_t key_bytes, const void *vals, int32_t value_bytes, int64_t n,
+                        int32_t nbits, int32_t reps, void *keys_out, void *vals_out, double *ms_per_sort);
 
 #ifdef __cplusplus
 }

@@ -54,6 +54,16 @@ def test_duplicates_and_presorted(dist, vdt):
     _check(keys, vals, 40)
 
 
+@pytest.mark.parametrize("n", [1, TILE - 1, TILE, 7 * TILE + 5, 300_001])
+@pytest.mark.parametrize("nbits", [5, 24, 31, 32])
+def test_32bit_keys_64bit_payloads(n, nbits):
+    rng = np.random.Generator(np.random.PCG64(n + 17 * nbits))
+    keys = rng.integers(0, 1 << nbits, n, dtype=np.uint64).astype(np.uint32)
+    keys[::5] = keys[0]
+    vals = rng.integers(0, np.iinfo(np.uint64).max, n, dtype=np.uint64, endpoint=True)
+    _check(keys, vals, nbits)
+
+
 def test_large_64bit_payloads():
     rng = np.random.Generator(np.random.PCG64(5))
     n = 2_000_000
