@@ -1486,31 +1486,108 @@ struct EscArgs {
   const u32 *tiles;     // esc index -> tile
   const u64 *base;      // esc index -> first pair
   u32 n;                // esc tiles
-  u64 span, LB;         // key = s * span + slot * LB + col
+  u64 span, LB;         // key = s * span + slot * LB + col, span = rows * LB
+  u64 rows;
+  u64 lbm;              // magic_for(LB) (used with 32-bit keys)
   void *keys;           // u32 when every key fits 32 bits, else u64
   u64 *vals;            // the products' bits (double), sorted along with the keys
   u64 total;            // pairs
 };
 
-// One CTA per esc tile (grid-stride), one warp per A entry of the tile.
+// Flat over all expanded pairs: each lane writes eight consecutive pairs.
+// The lane finds the esc tile and the A entry of its first pair by binary
+// search (over the tiles' first pairs, then over the tile's product prefix)
+// and advances both linearly from there. Hub rows have many A entries with
+// short B segments, so a warp per entry would leave most lanes idle.
+constexpr u32 kEscExpandPer = 8;
+
 template <class ColT, class KeyT>
 __global__ void __launch_bounds__(256) k_esc_expand(EscArgs a, const ProdSrc src, const ColT *__restrict__ colB,
                                                     const u32 *__restrict__ tile_abeg) {
   KeyT *keys = static_cast<KeyT *>(a.keys);
-  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  for (u32 s = blockIdx.x; s < a.n; s += gridDim.x) {
-    const u32 t = a.tiles[s];
-    const u32 ea = tile_abeg[t], eb = tile_abeg[t + 1];
-    const u64 p0 = __ldg(&src.P[ea]), base = a.base[s];
-    for (u32 e = ea + warp; e < eb; e += nwarps) {
-      const u64 pe = __ldg(&src.P[e]), len = __ldg(&src.P[e + 1]) - pe;
-      const double va = __ldg(&src.valA[e]);
-      const u64 kb = u64(s) * a.span + u64(__ldg(&src.slotA[e])) * a.LB;
-      const u32 sb = __ldg(&src.sbA[e]);
-      const u64 off = base + (pe - p0);
-      for (u64 i = lane; i < len; i += 32) {
-        keys[off + i] = KeyT(kb + u64(__ldg(&colB[sb + i])));
-        a.vals[off + i] = u64(__double_as_longlong(va * __ldg(&src.valB[sb + i])));
+  const u64 nth = u64(gridDim.x) * blockDim.x;
+  for (u64 q0 = (u64(blockIdx.x) * blockDim.x + threadIdx.x) * kEscExpandPer; q0 < a.total;
+       q0 += nth * kEscExpandPer) {
+    // esc tile: the last s with base[s] <= q0
+    u32 lo = 0, hi = a.n;  // base[lo] <= q0 < base[hi] (base[n] = total)
+    while (hi - lo > 1) {
+      const u32 m = (lo + hi) >> 1;
+      if (__ldg(&a.base[m]) <= q0) lo = m;
+      else hi = m;
+    }
+    u32 s = lo;
+    u64 tb = __ldg(&a.base[s]), tnext = s + 1 < a.n ? __ldg(&a.base[s + 1]) : a.total;
+    u32 t = a.tiles[s];
+    u32 ea = tile_abeg[t], eb = tile_abeg[t + 1];
+    u64 p0 = __ldg(&src.P[ea]);
+    // A entry: the last e with P[e] <= p
+    auto find_entry = [&](u64 p) {
+      u32 l = ea, h = eb;  // P[l] <= p < P[h]
+      while (h - l > 1) {
+        const u32 m = (l + h) >> 1;
+        if (__ldg(&src.P[m]) <= p) l = m;
+        else h = m;
+      }
+      return l;
+    };
+    u32 e = find_entry(p0 + (q0 - tb));
+    u64 pe = __ldg(&src.P[e]), pn = __ldg(&src.P[e + 1]);
+    u32 sb = __ldg(&src.sbA[e]);
+    double va = __ldg(&src.valA[e]);
+    u64 kb = u64(s) * a.span + u64(__ldg(&src.slotA[e])) * a.LB;
+    KeyT kk[kEscExpandPer];
+    double vv[kEscExpandPer];
+    const u32 cnt = u32(min(u64(kEscExpandPer), a.total - q0));
+#pragma unroll
+    for (u32 i = 0; i < kEscExpandPer; i++) {
+      if (i < cnt) {
+        const u64 q = q0 + i;
+        if (q == tnext) {  // the next esc tile (every esc tile has pairs)
+          s++;
+          tb = tnext;
+          tnext = s + 1 < a.n ? __ldg(&a.base[s + 1]) : a.total;
+          t = a.tiles[s];
+          ea = tile_abeg[t];
+          eb = tile_abeg[t + 1];
+          p0 = __ldg(&src.P[ea]);
+          e = ea;
+          pe = p0;
+          pn = __ldg(&src.P[e + 1]);
+          sb = __ldg(&src.sbA[e]);
+          va = __ldg(&src.valA[e]);
+          kb = u64(s) * a.span + u64(__ldg(&src.slotA[e])) * a.LB;
+        }
+        const u64 p = p0 + (q - tb);
+        while (p >= pn) {  // next A entry of the tile
+          e++;
+          pe = pn;
+          pn = __ldg(&src.P[e + 1]);
+          sb = __ldg(&src.sbA[e]);
+          va = __ldg(&src.valA[e]);
+          kb = u64(s) * a.span + u64(__ldg(&src.slotA[e])) * a.LB;
+        }
+        const u32 j = sb + u32(p - pe);
+        kk[i] = KeyT(kb + u64(__ldg(&colB[j])));
+        vv[i] = va * __ldg(&src.valB[j]);
+      }
+    }
+    if (cnt == kEscExpandPer) {  // 32 or 64 aligned bytes of keys, 64 of values
+      if (sizeof(KeyT) == 4) {
+        uint4 *dk = reinterpret_cast<uint4 *>(keys + q0);
+        dk[0] = make_uint4(u32(kk[0]), u32(kk[1]), u32(kk[2]), u32(kk[3]));
+        dk[1] = make_uint4(u32(kk[4]), u32(kk[5]), u32(kk[6]), u32(kk[7]));
+      } else {
+        ulonglong2 *dk = reinterpret_cast<ulonglong2 *>(keys + q0);
+#pragma unroll
+        for (u32 i = 0; i < kEscExpandPer / 2; i++) dk[i] = make_ulonglong2(u64(kk[2 * i]), u64(kk[2 * i + 1]));
+      }
+      double2 *dv = reinterpret_cast<double2 *>(a.vals + q0);
+#pragma unroll
+      for (u32 i = 0; i < kEscExpandPer / 2; i++) dv[i] = make_double2(vv[2 * i], vv[2 * i + 1]);
+    } else {
+      for (u32 i = 0; i < cnt; i++) {
+        keys[q0 + i] = kk[i];
+        a.vals[q0 + i] = u64(__double_as_longlong(vv[i]));
       }
     }
   }
@@ -1588,12 +1665,26 @@ __global__ void k_esc_reserve(const Out out, const u32 *__restrict__ nruns, u64 
   if (threadIdx.x == 0 && blockIdx.x == 0) *base = reserve(out, *nruns, err);
 }
 
+// Output row and column of a key. key / LB = s * rows + slot names the row;
+// consecutive runs mostly share it, so the lane keeps the last one.
+struct EscRowCache {
+  u64 q = ~0ull, row = 0;
+};
+
+template <class KeyT>
 __device__ __forceinline__ void esc_emit(const EscArgs &a, const u32 *__restrict__ tile_rank0,
                                          const u64 *__restrict__ urow, const Out &out, const Decode &dec,
-                                         u64 idx, u64 key, double v) {
-  const u64 s = key / a.span, rem = key - s * a.span;
-  const u64 slot = rem / a.LB, col = rem - slot * a.LB;
-  emit(out, dec, idx, __ldg(&urow[tile_rank0[a.tiles[s]] + slot]), col, v);
+                                         EscRowCache &rc, u64 idx, u64 key, double v) {
+  u64 q;
+  if (sizeof(KeyT) == 4) q = div_magic(u32(key), a.lbm);  // exact: key, LB < 2^32
+  else q = key / a.LB;
+  const u64 col = key - q * a.LB;
+  if (q != rc.q) {
+    const u64 s = q / a.rows, slot = q - s * a.rows;
+    rc.q = q;
+    rc.row = __ldg(&urow[tile_rank0[a.tiles[s]] + slot]);
+  }
+  emit(out, dec, idx, rc.row, col, v);
 }
 
 // Each run is summed and emitted (at base + its number) by the lane holding
@@ -1607,9 +1698,15 @@ __global__ void __launch_bounds__(256) k_esc_reduce(EscArgs a, const u32 *__rest
                                                     const u64 *__restrict__ base_p,
                                                     const u32 *__restrict__ tile_rank0,
                                                     const u64 *__restrict__ urow, const Out out, const Decode dec) {
+  // the chunk's finished runs, staged so that the warp emits them together
+  __shared__ u64 s_key[8][kEscChunk];
+  __shared__ double s_val[8][kEscChunk];
   const u64 base = *base_p;
   if (base == ~0ull) return;  // over capacity: counted by the cursor, retried by the host
-  const u32 lane = threadIdx.x & 31;
+  const u32 lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  u64 *sk = s_key[wib];
+  double *sv = s_val[wib];
+  EscRowCache rc;
   const u64 nchunks = (a.total + kEscChunk - 1) / kEscChunk;
   const u64 nw = (u64(gridDim.x) * blockDim.x) >> 5;
   for (u64 c = (u64(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += nw) {
@@ -1636,7 +1733,8 @@ __global__ void __launch_bounds__(256) k_esc_reduce(EscArgs a, const u32 *__rest
       const u32 t = __shfl_up_sync(kFull, incl, o);
       if (lane >= o) incl += t;
     }
-    u64 run = u64(chunk_off[c]) + (incl - nh);  // number of the lane's first run
+    const u32 nruns = __shfl_sync(kFull, incl, 31);  // runs starting in the chunk
+    u32 run = incl - nh;                             // the lane's first run, within the chunk
     // In-lane runs; the lane's last run stays open.
     double lead = 0.0, acc = 0.0;
     u64 key = 0;
@@ -1644,7 +1742,11 @@ __global__ void __launch_bounds__(256) k_esc_reduce(EscArgs a, const u32 *__rest
 #pragma unroll
     for (u32 q = 0; q < kEscPer; q++) {
       if ((L.heads >> q) & 1u) {
-        if (open) esc_emit(a, tile_rank0, urow, out, dec, base + run++, key, acc);
+        if (open) {
+          sk[run] = key;
+          sv[run] = acc;
+          run++;
+        }
         open = true;
         key = L.k[q];
         acc = v[q];
@@ -1710,7 +1812,14 @@ __global__ void __launch_bounds__(256) k_esc_reduce(EscArgs a, const u32 *__rest
       for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
       if (lane == wl) acc += sum;
     }
-    if (open) esc_emit(a, tile_rank0, urow, out, dec, base + run, key, acc);
+    if (open) {
+      sk[run] = key;
+      sv[run] = acc;
+    }
+    __syncwarp();
+    const u64 first = base + chunk_off[c];
+    for (u32 r = lane; r < nruns; r += 32) esc_emit<KeyT>(a, tile_rank0, urow, out, dec, rc, first + r, sk[r], sv[r]);
+    __syncwarp();
   }
 }
 
@@ -2274,7 +2383,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
                                                    split_tiles_d, split_tiles_h, t_hoff, t_hsz, hoff_t, hsz_t,
                                                    esc_flag, esc_idx, esc_off, esc_tiles, esc_base);
   FCC_LAUNCH_CHECK();
-  EscArgs ea{esc_tiles, esc_base, nesc, esc_rows * LB, LB, nullptr, nullptr, esc_pairs};
+  EscArgs ea{esc_tiles, esc_base, nesc, esc_rows * LB, LB, esc_rows, magic_for(LB), nullptr, nullptr, esc_pairs};
   u32 *esc_heads = nullptr, *esc_off_c = nullptr;
   const u64 esc_chunks = (esc_pairs + kEscChunk - 1) / kEscChunk;
   const int esc_grid = int(std::max<u64>(1, std::min<u64>((esc_chunks + 7) / 8, u64(ctx->num_sms) * 8)));
@@ -2452,7 +2561,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       }
       if (nesc > 0) {  // hub hash tiles: expand, sort, reduce
         if (attempt == 0) {
-          const u32 xgrid = std::min<u32>(nesc, u32(ctx->num_sms) * 8);
+          const u32 xgrid = u32(std::max<u64>(1, std::min<u64>((esc_pairs + 2047) / 2048, u64(ctx->num_sms) * 8)));
           if (esc_k32) {
             k_esc_expand<ColT, u32><<<xgrid, 256, 0, st>>>(ea, src, colptr, tile_abeg);
             FCC_LAUNCH_CHECK();
