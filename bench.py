@@ -736,7 +736,7 @@ def main():
     H = F.Tensor(pin_c.numpy(), pin_v.numpy(), a.max_index)
     out_c = torch.empty((out_order, out_nnz), dtype=torch.int32).pin_memory()
     out_v = torch.empty(out_nnz, dtype=torch.float64).pin_memory()
-    e2e_opts = F.Options()
+    e2e_opts = F.Options(timing=1)
     oc, ov = out_c.numpy(), out_v.numpy()
 
     def e2e_into():  # the tile kernels write the output straight into the pinned host buffers
@@ -761,6 +761,7 @@ def main():
         return dist_max(e0.elapsed_time(e1) / args.e2e_steps, ws)
 
     e2e_ms = e2e_time(e2e_into)
+    e2e_phases = ctx.timings()
     e2e_copy_ms = e2e_time(e2e_copy)
     h2d = 2 * (pin_c.numel() * 4 + pin_v.numel() * 8)
     d2h = out_nnz * (4 * out_order + 8)
@@ -788,7 +789,8 @@ def main():
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
                 "path": "fcc_contract_into: pinned host operands in, the tile kernels write the output "
                         "into pinned host buffers",
-                "copy_after_ms_per_step": e2e_copy_ms},
+                "copy_after_ms_per_step": e2e_copy_ms,
+                "phases_ms": {k: round(v, 4) for k, v in e2e_phases.items()}},
         "gpu_launches": launches,
         "clocks": clk,
         "phases_ms": {k: round(v, 4) for k, v in phases.items()},

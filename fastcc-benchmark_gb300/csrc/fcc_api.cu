@@ -43,6 +43,9 @@ fcc::Runtime runtime_of(fcc_ctx *ctx) {
   rt.phase_ms = ctx->phase_ms;
   rt.pool = ctx->pool;
   rt.sched = &ctx->sched;
+  rt.copy_stream = ctx->copy_stream;
+  rt.wave_ev = ctx->wave_ev;
+  rt.h_cursors = ctx->h_cursors;
   return rt;
 }
 
@@ -72,7 +75,7 @@ void set_thread_error(const std::string &msg) { g_last_error = msg; }
 
 extern "C" {
 
-static_assert(sizeof(fcc_options) == 80, "fcc_options layout is part of the ABI");
+static_assert(sizeof(fcc_options) == 88, "fcc_options layout is part of the ABI");
 
 int fcc_abi_version(void) { return FCC_ABI_VERSION; }
 
@@ -141,6 +144,9 @@ int fcc_ctx_create(int32_t device, fcc_ctx **out) {
     FCC_CUDA(cudaMalloc(reinterpret_cast<void **>(&ctx->d_err), sizeof(fcc::u32)));
     FCC_CUDA(cudaMallocHost(reinterpret_cast<void **>(&ctx->h_scalars), sizeof(fcc::u64) * 32));
     for (auto &e : ctx->ev) FCC_CUDA(cudaEventCreate(&e));
+    FCC_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    for (auto &e : ctx->wave_ev) FCC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    FCC_CUDA(cudaMallocHost(reinterpret_cast<void **>(&ctx->h_cursors), sizeof(fcc::u64) * (fcc::kMaxWaves + 1)));
   });
   if (st != FCC_OK) {
     if (ctx) fcc_ctx_destroy(ctx);
@@ -158,6 +164,11 @@ int fcc_ctx_destroy(fcc_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (auto &e : ctx->ev)
     if (e) cudaEventDestroy(e);
+  if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+  for (auto &e : ctx->wave_ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->h_cursors) cudaFreeHost(ctx->h_cursors);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->sched.model) cudaFree(ctx->sched.model);
   if (ctx->h_scalars) cudaFreeHost(ctx->h_scalars);

@@ -2189,6 +2189,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (opt.dense_staging < -1 || opt.dense_staging > 0) throw Error{FCC_ERR_ARG, "dense_staging must be -1 or 0"};
   if (opt.sched_mix_margin < 0 || opt.sched_mix_margin > 1000) throw Error{FCC_ERR_ARG, "bad sched_mix_margin"};
   if (opt.hash_esc < -1 || opt.hash_esc > 1) throw Error{FCC_ERR_ARG, "hash_esc must be -1, 0 or 1"};
+  if (opt.out_waves < 0 || opt.out_waves > kMaxWaves) throw Error{FCC_ERR_ARG, "out_waves must be in 0..16"};
   const bool learned = forced < 0 && opt.schedule == FCC_SCHED_LEARNED && ctx->sched && ctx->sched->model;
   const bool want_record = opt.timing == 2 && ctx->sched;
   // Row groups (batched contractions): dense tiles hold rows of one group,
@@ -2411,7 +2412,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   u64 *item_cyc = want_record ? ar.get_n<u64>(std::max<u32>(nitems, 1)) : nullptr;
   u64 *merge_cyc = want_record ? ar.get_n<u64>(nA2) : nullptr;
   if (merge_cyc) FCC_CUDA(cudaMemsetAsync(merge_cyc, 0, sizeof(u64) * nA2, st));
-  u32 *counters = ar.get_n<u32>(FCC_NUM_CLASSES);
+  u32 *counters = ar.get_n<u32>(FCC_NUM_CLASSES * kMaxWaves);  // item counters per wave and class
   tm.mark(3);
 
   // ---- contract + drain ----
@@ -2471,11 +2472,46 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     if (cap > 0 && (!ctx->out_vals || (out_order > 0 && (!ctx->out_coords || ctx->out_stride < i64(cap)))))
       throw Error{FCC_ERR_ARG, "output buffers missing or mode stride below the capacity"};
   }
+  // A caller output in pinned host memory is produced in device memory and
+  // copied out in waves of tiles: the outputs of a wave (a range of the output
+  // cursor) cross the host link while the next wave computes, instead of the
+  // tile kernels storing across the link themselves (about 0.5 GB per wave).
+  bool stream_out = false;
+  if (caller_out && ctx->pool && ctx->copy_stream && ctx->wave_ev && ctx->h_cursors && cap > 0) {
+    auto pinned_host = [](const void *p) {
+      cudaPointerAttributes pa{};
+      const bool h = cudaPointerGetAttributes(&pa, p) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+      cudaGetLastError();
+      return h;
+    };
+    stream_out = pinned_host(ctx->out_vals) && (out_order == 0 || pinned_host(ctx->out_coords));
+  }
+  const int waves = !stream_out          ? 1
+                    : opt.out_waves > 0 ? opt.out_waves
+                                        : int(std::min<u64>(kMaxWaves, std::max<u64>(1, (cap * per_out) >> 29)));
+  struct StageBufs {  // device copy of a streamed output, freed after its copies
+    cudaStream_t st = nullptr, cs = nullptr;
+    void *p[2] = {nullptr, nullptr};
+    ~StageBufs() {
+      if (cs) cudaStreamSynchronize(cs);
+      for (void *q : p)
+        if (q) cudaFreeAsync(q, st);
+    }
+  } stage_bufs;
+  stage_bufs.st = st;
+  stage_bufs.cs = stream_out ? ctx->copy_stream : nullptr;
   for (int attempt = 0;; attempt++) {
     i64 stride = i64(cap);
     if (!caller_out) {
       res->d_vals = static_cast<double *>(pool_alloc(ctx->pool, sizeof(double) * cap, st));
       if (out_order > 0) res->d_coords = static_cast<u32 *>(pool_alloc(ctx->pool, sizeof(u32) * cap * out_order, st));
+    } else if (stream_out) {
+      res->d_vals = static_cast<double *>(pool_alloc(ctx->pool, sizeof(double) * cap, st));
+      stage_bufs.p[0] = res->d_vals;
+      if (out_order > 0) {
+        res->d_coords = static_cast<u32 *>(pool_alloc(ctx->pool, sizeof(u32) * cap * out_order, st));
+        stage_bufs.p[1] = res->d_coords;
+      }
     } else {
       res->d_vals = ctx->out_vals;
       res->d_coords = ctx->out_coords;
@@ -2484,7 +2520,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     res->cap = stride;
     Out o{res->d_coords, stride, res->d_vals, cap, d_sc + S_CURSOR};
     FCC_CUDA(cudaMemsetAsync(d_sc + S_CURSOR, 0, sizeof(u64), st));
-    FCC_CUDA(cudaMemsetAsync(counters, 0, sizeof(u32) * FCC_NUM_CLASSES, st));
+    FCC_CUDA(cudaMemsetAsync(counters, 0, sizeof(u32) * FCC_NUM_CLASSES * kMaxWaves, st));
     FCC_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(u32), st));
     if (nsplit_d > 0) {
       FCC_CUDA(cudaMemsetAsync(gacc, 0, sizeof(double) * nsplit_d * area, st));
@@ -2498,7 +2534,19 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
                  tile_rank0, tile_lb, tile_nrows, urow, split_of_tile, split_tiles_d, nsplit_d, src,
                  static_cast<const u32 *>(colB), u32(area), u32(words), hot, gacc, gmask, o, dec, ctx->d_err,
                  item_cyc ? item_cyc + cbeg[FCC_CLASS_DENSE] : nullptr, 0u, merge_cyc};
-    if (ccount[FCC_CLASS_DENSE]) {
+    // Items of class c in wave w: a contiguous slice of the class's items.
+    auto wave_items = [&](int c, int w, u32 &lo, u32 &n) {
+      lo = u32(u64(ccount[c]) * u64(w) / u64(waves));
+      n = u32(u64(ccount[c]) * u64(w + 1) / u64(waves)) - lo;
+    };
+    auto run_dense = [&](int w) {
+      u32 lo = 0, n = 0;
+      wave_items(FCC_CLASS_DENSE, w, lo, n);
+      if (!n) return;
+      da.items = items + cbeg[FCC_CLASS_DENSE] + lo;
+      da.nitems = n;
+      da.counter = counters + w * FCC_NUM_CLASSES + FCC_CLASS_DENSE;
+      da.item_cyc = item_cyc ? item_cyc + cbeg[FCC_CLASS_DENSE] + lo : nullptr;
       const int threads = hc[FCC_CLASS_DENSE].threads;
       size_t smem = class_smem(FCC_CLASS_DENSE, hot);
       // phase 1's staging ring, when it fits beside the tile
@@ -2522,20 +2570,24 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
         else k_contract_dense<false, 1024><<<grid, 1024, smem, st>>>(da);
       }
       FCC_LAUNCH_CHECK();
-    }
-    auto run_hash = [&](auto colptr) {
+    };
+    // w >= 0: the hash classes' items of wave w; w < 0: the merges of split
+    // tiles and the expanded tiles, after every wave.
+    auto run_hash = [&](auto colptr, int w) {
       using ColT = std::remove_const_t<std::remove_pointer_t<decltype(colptr)>>;
       HashArgs<ColT> ha{nullptr, 0, nullptr, tile_rank0, urow, tile_nrows, tile_abeg, split_of_tile, split_tiles_h,
                         nsplit_h, src, colptr, LB, u32(grouped ? std::max<u64>(TL, 2) : TL), 0u, hot, hoff_t,
                         hsz_t, gkeys, gvals, o, dec,
                         ctx->d_err, nullptr, merge_cyc};
-      for (int c = FCC_CLASS_HASH_L; c < FCC_NUM_CLASSES; c++) {
-        if (!ccount[c]) continue;
-        ha.items = items + cbeg[c];
-        ha.nitems = ccount[c];
-        ha.counter = counters + c;
+      for (int c = FCC_CLASS_HASH_L; c < FCC_NUM_CLASSES && w >= 0; c++) {
+        u32 lo = 0, n = 0;
+        wave_items(c, w, lo, n);
+        if (!n) continue;
+        ha.items = items + cbeg[c] + lo;
+        ha.nitems = n;
+        ha.counter = counters + w * FCC_NUM_CLASSES + c;
         ha.slots = hc[c].slots;
-        ha.item_cyc = item_cyc ? item_cyc + cbeg[c] : nullptr;
+        ha.item_cyc = item_cyc ? item_cyc + cbeg[c] + lo : nullptr;
         const int threads = hc[c].threads;
         const size_t smem = class_smem(c, hot);
         const void *kern = threads == 128   ? reinterpret_cast<const void *>(k_contract_hash<ColT, 128>)
@@ -2550,7 +2602,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
         else k_contract_hash<ColT, 1024><<<grid, 1024, smem, st>>>(ha);
         FCC_LAUNCH_CHECK();
       }
-      tm.mark(4);
+      if (w >= 0) return;
       if (nsplit_d > 0) {
         k_merge_dense<<<std::min<u32>(nsplit_d, u32(ctx->num_sms) * 2), kTileThreads, 0, st>>>(da);
         FCC_LAUNCH_CHECK();
@@ -2583,9 +2635,40 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
         FCC_LAUNCH_CHECK();
       }
     };
-    if (colb32) run_hash(static_cast<const u32 *>(colB));
-    else run_hash(static_cast<const u64 *>(colB));
+    auto snapshot = [&](int w) {  // the output cursor after wave w, for the host's copies
+      FCC_CUDA(cudaMemcpyAsync(ctx->h_cursors + w, d_sc + S_CURSOR, sizeof(u64), cudaMemcpyDeviceToHost, st));
+      FCC_CUDA(cudaEventRecord(ctx->wave_ev[w], st));
+    };
+    for (int w = 0; w < waves; w++) {
+      run_dense(w);
+      if (colb32) run_hash(static_cast<const u32 *>(colB), w);
+      else run_hash(static_cast<const u64 *>(colB), w);
+      if (stream_out) snapshot(w);
+    }
+    tm.mark(4);
+    if (colb32) run_hash(static_cast<const u32 *>(colB), -1);
+    else run_hash(static_cast<const u64 *>(colB), -1);
+    if (stream_out) snapshot(waves);
     tm.mark(5);
+    if (stream_out) {  // copy each finished range while later waves run
+      u64 prev = 0;
+      for (int w = 0; w <= waves; w++) {
+        FCC_CUDA(cudaEventSynchronize(ctx->wave_ev[w]));
+        const u64 cur = std::min<u64>(ctx->h_cursors[w], cap);
+        if (cur <= prev) continue;
+        const size_t n = size_t(cur - prev);
+        for (int m = 0; m < out_order; m++)
+          FCC_CUDA(cudaMemcpyAsync(ctx->out_coords + i64(m) * ctx->out_stride + prev, res->d_coords + i64(m) * stride + prev,
+                                   sizeof(u32) * n, cudaMemcpyDeviceToHost, ctx->copy_stream));
+        FCC_CUDA(cudaMemcpyAsync(ctx->out_vals + prev, res->d_vals + prev, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                 ctx->copy_stream));
+        prev = cur;
+      }
+      FCC_CUDA(cudaStreamSynchronize(ctx->copy_stream));
+      res->d_vals = ctx->out_vals;
+      res->d_coords = ctx->out_coords;
+      res->cap = ctx->out_stride;
+    }
     read_scalars(ctx, d_sc);
     const u64 produced = ctx->h_scalars[S_CURSOR];
     const bool overflow = (u32(ctx->h_scalars[S_ERR]) & ERRB_OVERFLOW) != 0 || produced > cap;

@@ -165,7 +165,14 @@ struct Runtime {
   u64 out_cap = 0;
   bool caller_out = false;         // write the output into out_* (any device-accessible memory)
   SchedIo *sched = nullptr;        // NULL: no learned schedule and no per-tile record
+  // Streaming a caller output that lives in pinned host memory (NULL: not available):
+  cudaStream_t copy_stream = nullptr;  // device-to-host copies of finished output ranges
+  cudaEvent_t *wave_ev = nullptr;      // kMaxWaves + 1 events, one per wave and one after the merges
+  u64 *h_cursors = nullptr;            // pinned, kMaxWaves + 1 output cursor snapshots
 };
+
+// A pinned host output is produced in at most this many waves of tiles.
+constexpr int kMaxWaves = 16;
 
 void set_thread_error(const std::string &msg);
 void *pool_alloc(cudaMemPool_t pool, size_t bytes, cudaStream_t st);  // fcc_prims.cu
@@ -184,6 +191,9 @@ struct fcc_ctx {
   fcc::u64 *h_scalars = nullptr;   // pinned host scalars for read-backs
   cudaEvent_t ev[FCC_NUM_PHASES + 1] = {};
   double phase_ms[FCC_NUM_PHASES] = {};
+  cudaStream_t copy_stream = nullptr;          // output waves to pinned host buffers
+  cudaEvent_t wave_ev[fcc::kMaxWaves + 1] = {};
+  fcc::u64 *h_cursors = nullptr;               // pinned
   fcc::SchedIo sched;
   std::map<std::string, std::pair<fcc_options, double>> tuned;  // autotuner cache: signature -> best
   std::string last_error;

@@ -36,7 +36,7 @@ extern "C" {
 #endif
 
 #define FCC_MAX_ORDER 8
-#define FCC_ABI_VERSION 2
+#define FCC_ABI_VERSION 3
 
 typedef enum fcc_status {
   FCC_OK = 0,
@@ -115,6 +115,11 @@ typedef struct fcc_options {
                                  device memory (allocation-free calls: as -1); 1: the same, also in
                                  allocation-free calls; -1: split into items merged through a
                                  global hash table */
+  int32_t out_waves;          /* fcc_contract_into with pinned host output buffers: the output is
+                                 produced in device memory in this many waves of tiles (1..16),
+                                 each wave's outputs copied to the host while the next computes.
+                                 0 (default): one wave per 512 MB of output capacity */
+  int32_t pad1;
 } fcc_options;
 
 /* Tile classes: every output tile runs in one of them. The hash classes

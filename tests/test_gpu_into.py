@@ -38,6 +38,25 @@ def test_into_caller_buffers(ctx, where):
     check_parity(oc[:, :n].T, ov[:n], o["coords"], o["values"], o["abs_sum"])
 
 
+@pytest.mark.parametrize("opts", [{"out_waves": 2}, {"out_waves": 5, "products_per_item": 40},
+                                  {"out_waves": 16, "accumulator": F.ACC_HASH, "products_per_item": 30},
+                                  {"out_waves": 3, "accumulator": F.ACC_HASH, "hash_slots": 64, "hash_esc": -1}])
+def test_into_pinned_in_waves(ctx, opts):
+    # pinned host output: produced on the device in waves of tiles, each
+    # wave's range copied out while the next runs; split tiles and expanded
+    # tiles come after the last wave
+    import torch
+    w, o = _case()
+    n = len(o["values"])
+    order = o["coords"].shape[1]
+    oc = torch.full((order, n + 100), -1, dtype=torch.int32).pin_memory().numpy()
+    ov = torch.full((n + 100,), np.nan, dtype=torch.float64).pin_memory().numpy()
+    got, prods = ctx.contract_into(w["a"], w["b"], w["ctr_a"], w["ctr_b"], oc, ov, F.Options(**opts))
+    assert got == n and prods == o["products"]
+    check_parity(oc[:, :n].T, ov[:n], o["coords"], o["values"], o["abs_sum"])
+    assert (oc[:, n:] == -1).all() and np.isnan(ov[n:]).all()  # nothing written past the output
+
+
 def test_into_too_small_reports_the_size(ctx):
     import torch
     w, o = _case()
