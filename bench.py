@@ -9,7 +9,8 @@ sign-random lognormal values, contracted over modes {1,2}.
   value  = FP64 multiply-adds per second, inputs resident on the device
   e2e    = the same through the C ABI with host (pinned) operands and the full
            output delivered to pinned host buffers inside the timed region
-           (fcc_contract_into: the tile kernels write it there as they go;
+           (fcc_contract_into: the output is produced on the device in waves of
+           tiles, each wave's entries copied to the host while the next computes;
            copy_after_ms_per_step: device result, then one copy)
   roofline: the tile contraction kernel (k_contract_dense); algorithmic bytes
            = inputs read once + outputs written once
@@ -787,8 +788,8 @@ def main():
                               "note": "every multiply-add is one FP64 FMA; peak measured by fcc_diag_fp64_fma_rate"}},
         "e2e": {"value": products * ws / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
-                "path": "fcc_contract_into: pinned host operands in, the tile kernels write the output "
-                        "into pinned host buffers",
+                "path": "fcc_contract_into: pinned host operands in, output produced on the device in waves "
+                        "of tiles and copied to pinned host buffers while later waves compute",
                 "copy_after_ms_per_step": e2e_copy_ms,
                 "phases_ms": {k: round(v, 4) for k, v in e2e_phases.items()}},
         "gpu_launches": launches,

@@ -252,7 +252,8 @@ class Context:
     def contract_into(self, a, b, ctr_a, ctr_b, out_coords, out_values, opts=None):
         """fcc_contract_into: the output written into caller buffers, out_coords
         (order, capacity) int32/uint32 and out_values (capacity,) float64, as
-        numpy arrays in pinned host memory (the kernels write them directly)
+        numpy arrays in pinned host memory (filled wave by wave while the
+        contraction runs)
         or CUDA torch tensors. Returns (entries, multiply-adds); raises
         FccError(FCC_ERR_CAPACITY) with .needed when they do not fit."""
         ca = np.ascontiguousarray(ctr_a, dtype=np.int32)

@@ -188,8 +188,10 @@ int fcc_contract(fcc_ctx *ctx, const fcc_tensor *A, const fcc_tensor *B, const i
  * out_coords[m * out_mode_stride + i], uint32, out_mode_stride >=
  * out_capacity) and out_values, out_capacity entries, in any memory the
  * device can write: device memory, or pinned host memory, in which case the
- * tile kernels stream the output to the host while they compute (no separate
- * copy afterwards). Entry order is unspecified. Returns FCC_ERR_CAPACITY with
+ * output is produced in device memory in waves of tiles (opts->out_waves) and
+ * each wave's entries are copied to the host while the next wave computes;
+ * the allocation-free context has no copy stream and writes pinned host
+ * memory from the kernels. Entry order is unspecified. Returns FCC_ERR_CAPACITY with
  * *out_nnz = the entries needed when the output does not fit (the buffers'
  * contents are then undefined). No counterpart in the reference, whose
  * output goes to a host list.
