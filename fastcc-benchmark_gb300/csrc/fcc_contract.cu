@@ -420,7 +420,8 @@ __global__ void k_tile_items(const u32 *__restrict__ ntiles_p, i64 nmax, const u
     u64 items = (prod + ct.pmax[c] - 1) / ct.pmax[c];
     const u64 area = tile_area(nrows, lb, LB, t);  // rows x LB fits 64 bits (host check)
     const u64 bound = prod < area ? prod : area;
-    const bool to_esc = esc && ct.hash[c] && items > 1;  // a hash tile too big for its table
+    // esc 1: hash tiles too big for their table; 2: every hash tile
+    const bool to_esc = esc && ct.hash[c] && (items > 1 || esc == 2);
     if (to_esc) items = 0;
     nitems[i] = u32(items);
     split_d[i] = (!ct.hash[c] && items > 1) ? 1u : 0u;
@@ -776,7 +777,7 @@ __device__ void build_item_plan(const u64 *__restrict__ P, u32 ea, u32 eb, u64 p
 // is an mbarrier poll with a bounded count; on timeout the kernel flags
 // ERRB_INTERNAL, stops issuing, waits (bounded) for its copies in flight and
 // skips its remaining work.
-constexpr u32 kStageCh = 2048;
+constexpr u32 kStageCh = 1920;  // 4 x 480 consumer threads of a 512-thread tile: no partial round
 constexpr u32 kStageBufs = 2;
 constexpr u32 kStageValBytes = (kStageCh + 2) * 8;  // 16-byte multiple: room for a 1-element head
 constexpr u32 kStageColBytes = (kStageCh + 4) * 4;  // 16-byte multiple: room for a 3-element head
@@ -2188,7 +2189,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (opt.dense_fill_log2 < 0 || opt.dense_fill_log2 > 40) throw Error{FCC_ERR_ARG, "dense_fill_log2 out of range"};
   if (opt.dense_staging < -1 || opt.dense_staging > 0) throw Error{FCC_ERR_ARG, "dense_staging must be -1 or 0"};
   if (opt.sched_mix_margin < 0 || opt.sched_mix_margin > 1000) throw Error{FCC_ERR_ARG, "bad sched_mix_margin"};
-  if (opt.hash_esc < -1 || opt.hash_esc > 1) throw Error{FCC_ERR_ARG, "hash_esc must be -1, 0 or 1"};
+  if (opt.hash_esc < -1 || opt.hash_esc > 2) throw Error{FCC_ERR_ARG, "hash_esc must be -1, 0, 1 or 2"};
   if (opt.out_waves < 0 || opt.out_waves > kMaxWaves) throw Error{FCC_ERR_ARG, "out_waves must be in 0..16"};
   const bool learned = forced < 0 && opt.schedule == FCC_SCHED_LEARNED && ctx->sched && ctx->sched->model;
   const bool want_record = opt.timing == 2 && ctx->sched;
@@ -2337,7 +2338,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   u32 *esc_flag = ar.get_n<u32>(nA2), *esc_idx = ar.get_n<u32>(nA2);
   u64 *esc_cnt = ar.get_n<u64>(nA2), *esc_off = ar.get_n<u64>(nA2);
   k_tile_items<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), nA2, corder, cls, tile_abeg, P, tile_nrows,
-                                                   lb_or_null, LB, ctab, esc ? 1 : 0, t_items, t_split_d, t_split_h,
+                                                   lb_or_null, LB, ctab, esc ? (opt.hash_esc == 2 ? 2 : 1) : 0, t_items, t_split_d, t_split_h,
                                                    t_cap, t_hsz, esc_flag, esc_cnt);
   FCC_LAUNCH_CHECK();
   scan_exclusive(esc_flag, esc_idx, nA2, sc32(S_NESC), ar, st);

@@ -113,8 +113,9 @@ typedef struct fcc_options {
   int32_t hash_esc;           /* hash tiles larger than their table. 0 (default): expanded to (key,
                                  value) pairs, radix-sorted and reduced when the pairs fit in
                                  device memory (allocation-free calls: as -1); 1: the same, also in
-                                 allocation-free calls; -1: split into items merged through a
-                                 global hash table */
+                                 allocation-free calls; 2: every hash tile expanded, not only the
+                                 large ones; -1: split into items merged through a global hash
+                                 table */
   int32_t out_waves;          /* fcc_contract_into with pinned host output buffers: the output is
                                  produced in device memory in this many waves of tiles (1..16),
                                  each wave's outputs copied to the host while the next computes.

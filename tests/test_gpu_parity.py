@@ -50,6 +50,7 @@ VARIANTS = [
     {"accumulator": F.ACC_HASH, "products_per_item": 5, "hash_esc": 1},    # expand-sort-reduce of split tiles
     {"accumulator": F.ACC_HASH, "hash_slots": 64, "hash_esc": 1},
     {"schedule": F.SCHED_FORCE + F.CLASS_HASH_S, "products_per_item": 40, "hash_esc": 1},
+    {"accumulator": F.ACC_HASH, "hash_esc": 2},                               # every hash tile expanded
 ]
 
 
