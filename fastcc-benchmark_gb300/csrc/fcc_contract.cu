@@ -1485,11 +1485,12 @@ __global__ void __launch_bounds__(kTileThreads) k_merge_hash(HashArgs<ColT> a) {
 
 struct EscArgs {
   const u32 *tiles;     // esc index -> tile
-  const u64 *base;      // esc index -> first pair
+  const u64 *base;      // esc index -> first pair (counted from the first pair of all groups)
   u32 n;                // esc tiles
   u64 span, LB;         // key = s * span + slot * LB + col, span = rows * LB
   u64 rows;
   u64 lbm;              // magic_for(LB) (used with 32-bit keys)
+  u64 pair0;            // base[0]: this group's first pair
   void *keys;           // u32 when every key fits 32 bits, else u64
   u64 *vals;            // the products' bits (double), sorted along with the keys
   u64 total;            // pairs
@@ -1510,14 +1511,14 @@ __global__ void __launch_bounds__(256) k_esc_expand(EscArgs a, const ProdSrc src
   for (u64 q0 = (u64(blockIdx.x) * blockDim.x + threadIdx.x) * kEscExpandPer; q0 < a.total;
        q0 += nth * kEscExpandPer) {
     // esc tile: the last s with base[s] <= q0
-    u32 lo = 0, hi = a.n;  // base[lo] <= q0 < base[hi] (base[n] = total)
+    u32 lo = 0, hi = a.n;  // base[lo] <= q0 < base[hi] (base[n] = total), relative to pair0
     while (hi - lo > 1) {
       const u32 m = (lo + hi) >> 1;
-      if (__ldg(&a.base[m]) <= q0) lo = m;
+      if (__ldg(&a.base[m]) - a.pair0 <= q0) lo = m;
       else hi = m;
     }
     u32 s = lo;
-    u64 tb = __ldg(&a.base[s]), tnext = s + 1 < a.n ? __ldg(&a.base[s + 1]) : a.total;
+    u64 tb = __ldg(&a.base[s]) - a.pair0, tnext = s + 1 < a.n ? __ldg(&a.base[s + 1]) - a.pair0 : a.total;
     u32 t = a.tiles[s];
     u32 ea = tile_abeg[t], eb = tile_abeg[t + 1];
     u64 p0 = __ldg(&src.P[ea]);
@@ -1546,7 +1547,7 @@ __global__ void __launch_bounds__(256) k_esc_expand(EscArgs a, const ProdSrc src
         if (q == tnext) {  // the next esc tile (every esc tile has pairs)
           s++;
           tb = tnext;
-          tnext = s + 1 < a.n ? __ldg(&a.base[s + 1]) : a.total;
+          tnext = s + 1 < a.n ? __ldg(&a.base[s + 1]) - a.pair0 : a.total;
           t = a.tiles[s];
           ea = tile_abeg[t];
           eb = tile_abeg[t + 1];
@@ -1660,6 +1661,12 @@ __global__ void __launch_bounds__(256) k_esc_count(EscArgs a, u32 *__restrict__ 
     for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(kFull, n, o);
     if (lane == 0) chunk_heads[c] = n;
   }
+}
+
+// First pair of each group of G expanded tiles.
+__global__ void k_esc_group_starts(const u64 *__restrict__ base, u32 G, u32 ngroups, u64 *__restrict__ start) {
+  for (u32 g = blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += gridDim.x * blockDim.x)
+    start[g] = base[u64(g) * G];
 }
 
 __global__ void k_esc_reserve(const Out out, const u32 *__restrict__ nruns, u64 *__restrict__ base, u32 *err) {
@@ -2191,6 +2198,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (opt.sched_mix_margin < 0 || opt.sched_mix_margin > 1000) throw Error{FCC_ERR_ARG, "bad sched_mix_margin"};
   if (opt.hash_esc < -1 || opt.hash_esc > 2) throw Error{FCC_ERR_ARG, "hash_esc must be -1, 0, 1 or 2"};
   if (opt.out_waves < 0 || opt.out_waves > kMaxWaves) throw Error{FCC_ERR_ARG, "out_waves must be in 0..16"};
+  if (opt.esc_group < 0) throw Error{FCC_ERR_ARG, "esc_group must be >= 0"};
   const bool learned = forced < 0 && opt.schedule == FCC_SCHED_LEARNED && ctx->sched && ctx->sched->model;
   const bool want_record = opt.timing == 2 && ctx->sched;
   // Row groups (batched contractions): dense tiles hold rows of one group,
@@ -2317,15 +2325,21 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   // tiles in class order (stable), so that each class's items are contiguous
   radix_sort_pairs(ckey, corder, nA2, 3, ar, st, ctx->d_err);
 
-  // Hash tiles too big for their table: expand, sort and reduce when the
+  // Hash tiles expanded, sorted and reduced instead of accumulated in tables
+  // (esc_mode 2: every hash tile; 1: tiles too big for their table, which
+  // otherwise split into items merged through a global hash table), when the
   // pairs fit (at most 56 bytes of temporaries per multiply-add, within half
-  // of the free device memory) and the key space fits 64 bits; else (and with
-  // hash_esc = -1) split into items merged through a global hash table. A
-  // fixed workspace (the allocation-free call) expands only on request
-  // (hash_esc = 1), since the pairs may not fit where the hash tables do.
+  // of the free device memory) and the key space fits 64 bits. By default
+  // every hash tile, unless the caller chose the classes (a forced hash class
+  // or the learned schedule: then the tables run and only the oversized tiles
+  // expand); a fixed workspace (the allocation-free call) expands only on
+  // request, since the pairs may not fit where the hash tables do.
   const u64 esc_rows = grouped ? dense_cap : TL;
   bool esc = false;
-  const bool esc_wanted = opt.hash_esc > 0 || (opt.hash_esc == 0 && !ar.is_fixed());
+  int esc_mode = opt.hash_esc;
+  if (esc_mode == 0)
+    esc_mode = ar.is_fixed() ? -1 : ((forced >= 0 && forced != FCC_CLASS_DENSE) || learned) ? 1 : 2;
+  const bool esc_wanted = esc_mode > 0;
   // (not while recording per-tile costs: expanded tiles have no work items to time)
   if (esc_wanted && !want_record) {
     size_t fb = 0, tb = 0;
@@ -2338,7 +2352,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   u32 *esc_flag = ar.get_n<u32>(nA2), *esc_idx = ar.get_n<u32>(nA2);
   u64 *esc_cnt = ar.get_n<u64>(nA2), *esc_off = ar.get_n<u64>(nA2);
   k_tile_items<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), nA2, corder, cls, tile_abeg, P, tile_nrows,
-                                                   lb_or_null, LB, ctab, esc ? (opt.hash_esc == 2 ? 2 : 1) : 0, t_items, t_split_d, t_split_h,
+                                                   lb_or_null, LB, ctab, esc ? esc_mode : 0, t_items, t_split_d, t_split_h,
                                                    t_cap, t_hsz, esc_flag, esc_cnt);
   FCC_LAUNCH_CHECK();
   scan_exclusive(esc_flag, esc_idx, nA2, sc32(S_NESC), ar, st);
@@ -2385,17 +2399,48 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
                                                    split_tiles_d, split_tiles_h, t_hoff, t_hsz, hoff_t, hsz_t,
                                                    esc_flag, esc_idx, esc_off, esc_tiles, esc_base);
   FCC_LAUNCH_CHECK();
-  EscArgs ea{esc_tiles, esc_base, nesc, esc_rows * LB, LB, esc_rows, magic_for(LB), nullptr, nullptr, esc_pairs};
-  u32 *esc_heads = nullptr, *esc_off_c = nullptr;
-  const u64 esc_chunks = (esc_pairs + kEscChunk - 1) / kEscChunk;
-  const int esc_grid = int(std::max<u64>(1, std::min<u64>((esc_chunks + 7) / 8, u64(ctx->num_sms) * 8)));
-  const int esc_bits = nesc > 0 ? bits_for(u64(nesc) * ea.span - 1) : 0;
-  const bool esc_k32 = esc_bits <= 32;  // 32-bit keys: a quarter less traffic per sort pass
+  // Expanded tiles run in groups of at most G tiles, so that the keys (local
+  // tile index x span + slot x LB + column) fit 32 bits, a quarter less
+  // traffic per sort pass than 64-bit keys; a span over 32 bits takes one
+  // group with 64-bit keys. Each group is expanded, sorted and reduced on
+  // its own buffers.
+  struct EscGroup {
+    EscArgs a;
+    u32 *heads, *offc;  // per chunk: run heads, runs before it
+    u64 chunks;
+    int grid, bits;
+  };
+  std::vector<EscGroup> escg;
+  const u64 esc_span = esc_rows * LB;
+  const bool esc_k32 = esc_span <= 0xFFFFFFFFull;
   if (nesc > 0) {
-    ea.keys = esc_k32 ? static_cast<void *>(ar.get_n<u32>(esc_pairs)) : static_cast<void *>(ar.get_n<u64>(esc_pairs));
-    ea.vals = ar.get_n<u64>(esc_pairs);
-    esc_heads = ar.get_n<u32>(esc_chunks);
-    esc_off_c = ar.get_n<u32>(esc_chunks);
+    u64 G = esc_k32 ? std::max<u64>(1, 0xFFFFFFFFull / esc_span) : u64(nesc);
+    if (opt.esc_group > 0) G = std::min<u64>(G, u64(opt.esc_group));
+    const u32 ng = u32((u64(nesc) + G - 1) / G);
+    std::vector<u64> start(ng + 1, 0);
+    if (ng > 1) {
+      u64 *d_start = ar.get_n<u64>(ng);
+      k_esc_group_starts<<<1, 256, 0, st>>>(esc_base, u32(G), ng, d_start);
+      FCC_LAUNCH_CHECK();
+      FCC_CUDA(cudaMemcpyAsync(start.data(), d_start, sizeof(u64) * ng, cudaMemcpyDeviceToHost, st));
+      FCC_CUDA(cudaStreamSynchronize(st));
+    }
+    start[ng] = esc_pairs;
+    for (u32 g = 0; g < ng; g++) {
+      const u32 s0 = u32(u64(g) * G), n = u32(std::min<u64>(G, u64(nesc) - s0));
+      const u64 pairs = start[g + 1] - start[g];
+      EscGroup e{EscArgs{esc_tiles + s0, esc_base + s0, n, esc_span, LB, esc_rows, magic_for(LB), start[g], nullptr,
+                         nullptr, pairs},
+                 nullptr, nullptr, 0, 1, 0};
+      e.a.keys = esc_k32 ? static_cast<void *>(ar.get_n<u32>(pairs)) : static_cast<void *>(ar.get_n<u64>(pairs));
+      e.a.vals = ar.get_n<u64>(pairs);
+      e.chunks = (pairs + kEscChunk - 1) / kEscChunk;
+      e.heads = ar.get_n<u32>(e.chunks);
+      e.offc = ar.get_n<u32>(e.chunks);
+      e.grid = int(std::max<u64>(1, std::min<u64>((e.chunks + 7) / 8, u64(ctx->num_sms) * 8)));
+      e.bits = bits_for(u64(n) * esc_span - 1);
+      escg.push_back(e);
+    }
   }
   const u64 words = dense ? (area + 31) / 32 : 0;
   double *gacc = nullptr;
@@ -2612,27 +2657,28 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
         k_merge_hash<ColT><<<std::min<u32>(nsplit_h, u32(ctx->num_sms) * 2), kTileThreads, 0, st>>>(ha);
         FCC_LAUNCH_CHECK();
       }
-      if (nesc > 0) {  // hub hash tiles: expand, sort, reduce
-        if (attempt == 0) {
-          const u32 xgrid = u32(std::max<u64>(1, std::min<u64>((esc_pairs + 2047) / 2048, u64(ctx->num_sms) * 8)));
+      for (const EscGroup &e : escg) {  // expanded tiles: expand, sort, reduce, group by group
+        const EscArgs &ea = e.a;
+        if (attempt == 0) {  // the sorted pairs stay for a retry
+          const u32 xgrid = u32(std::max<u64>(1, std::min<u64>((ea.total + 2047) / 2048, u64(ctx->num_sms) * 8)));
           if (esc_k32) {
             k_esc_expand<ColT, u32><<<xgrid, 256, 0, st>>>(ea, src, colptr, tile_abeg);
             FCC_LAUNCH_CHECK();
-            radix_sort_pairs64(static_cast<u32 *>(ea.keys), ea.vals, i64(esc_pairs), esc_bits, ar, st, ctx->d_err);
-            k_esc_count<u32><<<esc_grid, 256, 0, st>>>(ea, esc_heads);
+            radix_sort_pairs64(static_cast<u32 *>(ea.keys), ea.vals, i64(ea.total), e.bits, ar, st, ctx->d_err);
           } else {
             k_esc_expand<ColT, u64><<<xgrid, 256, 0, st>>>(ea, src, colptr, tile_abeg);
             FCC_LAUNCH_CHECK();
-            radix_sort_pairs64(static_cast<u64 *>(ea.keys), ea.vals, i64(esc_pairs), esc_bits, ar, st, ctx->d_err);
-            k_esc_count<u64><<<esc_grid, 256, 0, st>>>(ea, esc_heads);
+            radix_sort_pairs64(static_cast<u64 *>(ea.keys), ea.vals, i64(ea.total), e.bits, ar, st, ctx->d_err);
           }
-          FCC_LAUNCH_CHECK();
-          scan_exclusive(esc_heads, esc_off_c, i64(esc_chunks), sc32(S_ESC_RUNS), ar, st);
         }
+        if (esc_k32) k_esc_count<u32><<<e.grid, 256, 0, st>>>(ea, e.heads);
+        else k_esc_count<u64><<<e.grid, 256, 0, st>>>(ea, e.heads);
+        FCC_LAUNCH_CHECK();
+        scan_exclusive(e.heads, e.offc, i64(e.chunks), sc32(S_ESC_RUNS), ar, st);
         k_esc_reserve<<<1, 32, 0, st>>>(o, sc32(S_ESC_RUNS), d_sc + S_ESC_BASE, ctx->d_err);
         FCC_LAUNCH_CHECK();
-        if (esc_k32) k_esc_reduce<u32><<<esc_grid, 256, 0, st>>>(ea, esc_off_c, d_sc + S_ESC_BASE, tile_rank0, urow, o, dec);
-        else k_esc_reduce<u64><<<esc_grid, 256, 0, st>>>(ea, esc_off_c, d_sc + S_ESC_BASE, tile_rank0, urow, o, dec);
+        if (esc_k32) k_esc_reduce<u32><<<e.grid, 256, 0, st>>>(ea, e.offc, d_sc + S_ESC_BASE, tile_rank0, urow, o, dec);
+        else k_esc_reduce<u64><<<e.grid, 256, 0, st>>>(ea, e.offc, d_sc + S_ESC_BASE, tile_rank0, urow, o, dec);
         FCC_LAUNCH_CHECK();
       }
     };

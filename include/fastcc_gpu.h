@@ -110,17 +110,20 @@ typedef struct fcc_options {
   int32_t sched_mix_margin;   /* FCC_SCHED_LEARNED: 0 (default): per-tile choices; > 0: one class for
                                  every tile unless the model predicts the per-tile mix faster than
                                  the best single class by this many percent */
-  int32_t hash_esc;           /* hash tiles larger than their table. 0 (default): expanded to (key,
-                                 value) pairs, radix-sorted and reduced when the pairs fit in
-                                 device memory (allocation-free calls: as -1); 1: the same, also in
-                                 allocation-free calls; 2: every hash tile expanded, not only the
-                                 large ones; -1: split into items merged through a global hash
-                                 table */
+  int32_t hash_esc;           /* hash tiles expanded to (key, value) pairs, radix-sorted and
+                                 reduced instead of accumulated in shared-memory tables, when the
+                                 pairs fit in device memory. 2: every hash tile; 1: the tiles
+                                 larger than their table (the others run the tables); -1: none
+                                 (large tiles split into items merged through a global hash
+                                 table); 0 (default): 2, or 1 with a forced hash class or the
+                                 learned schedule, or -1 in allocation-free calls */
   int32_t out_waves;          /* fcc_contract_into with pinned host output buffers: the output is
                                  produced in device memory in this many waves of tiles (1..16),
                                  each wave's outputs copied to the host while the next computes.
                                  0 (default): one wave per 512 MB of output capacity */
-  int32_t pad1;
+  int32_t esc_group;          /* expanded hash tiles are sorted in groups whose keys fit 32 bits;
+                                 0 (default): as many tiles per group as that allows; > 0: at
+                                 most this many */
 } fcc_options;
 
 /* Tile classes: every output tile runs in one of them. The hash classes

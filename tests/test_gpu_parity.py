@@ -51,6 +51,8 @@ VARIANTS = [
     {"accumulator": F.ACC_HASH, "hash_slots": 64, "hash_esc": 1},
     {"schedule": F.SCHED_FORCE + F.CLASS_HASH_S, "products_per_item": 40, "hash_esc": 1},
     {"accumulator": F.ACC_HASH, "hash_esc": 2},                               # every hash tile expanded
+    {"accumulator": F.ACC_HASH, "hash_esc": 2, "esc_group": 3},               # ... sorted in groups of 3 tiles
+    {"accumulator": F.ACC_HASH, "products_per_item": 6, "esc_group": 1},
 ]
 
 
@@ -284,6 +286,7 @@ def test_long_runs_of_equal_outputs(ctx, rows, cols, k):
     args = (a_c, a_v, am, b_c, b_v, bm, [1], [0])
     o = run_oracle(*args)
     for opts in ({"accumulator": F.ACC_HASH, "hash_slots": 64},
+                 {"accumulator": F.ACC_HASH, "hash_slots": 64, "esc_group": 2},
                  {"accumulator": F.ACC_HASH, "hash_slots": 64, "hash_esc": -1},
                  {"accumulator": F.ACC_HASH, "products_per_item": 100}):
         c, v, prods = run_gpu(ctx, *args, **opts)
