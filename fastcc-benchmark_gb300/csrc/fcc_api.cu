@@ -312,6 +312,7 @@ void autotune(fcc_ctx *ctx, const std::string &sig, const fcc_options &base, int
   };
   for (int threads : {512, 1024}) {
     add(FCC_SCHED_RULE, threads, 0);
+    add(FCC_SCHED_RULE, threads, -1);
     add(FCC_SCHED_RULE, threads, 6);
     add(FCC_SCHED_FORCE + FCC_CLASS_DENSE, threads, 0);
   }

@@ -2193,7 +2193,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
                                  ? "dense accumulator: B external span exceeds the shared-memory tile"
                                  : "the forced hash class is disabled by hash_slots or tile_threads"};
   if (custom_hash && forced < 0 && opt.accumulator == FCC_ACC_HASH) forced = FCC_CLASS_HASH_L;
-  if (opt.dense_fill_log2 < 0 || opt.dense_fill_log2 > 40) throw Error{FCC_ERR_ARG, "dense_fill_log2 out of range"};
+  if (opt.dense_fill_log2 < -1 || opt.dense_fill_log2 > 40) throw Error{FCC_ERR_ARG, "dense_fill_log2 out of range"};
   if (opt.dense_staging < -1 || opt.dense_staging > 0) throw Error{FCC_ERR_ARG, "dense_staging must be -1 or 0"};
   if (opt.sched_mix_margin < 0 || opt.sched_mix_margin > 1000) throw Error{FCC_ERR_ARG, "bad sched_mix_margin"};
   if (opt.hash_esc < -1 || opt.hash_esc > 2) throw Error{FCC_ERR_ARG, "hash_esc must be -1, 0, 1 or 2"};
@@ -2272,6 +2272,29 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   k_tile_nrows<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), tile_abeg, rank, tile_rank0, tile_nrows);
   FCC_LAUNCH_CHECK();
 
+  // Hash tiles expanded, sorted and reduced instead of accumulated in tables
+  // (esc_mode 2: every hash tile; 1: tiles too big for their table, which
+  // otherwise split into items merged through a global hash table), when the
+  // pairs fit (at most 56 bytes of temporaries per multiply-add, within half
+  // of the free device memory) and the key space fits 64 bits. By default
+  // every hash tile, unless the caller chose the classes (a forced hash class
+  // or the learned schedule: then the tables run and only the oversized tiles
+  // expand); a fixed workspace (the allocation-free call) expands only on
+  // request, since the pairs may not fit where the hash tables do.
+  const u64 esc_rows = grouped ? dense_cap : TL;
+  bool esc = false;
+  int esc_mode = opt.hash_esc;
+  if (esc_mode == 0)
+    esc_mode = ar.is_fixed() ? -1 : ((forced >= 0 && forced != FCC_CLASS_DENSE) || learned) ? 1 : 2;
+  const bool esc_wanted = esc_mode > 0;
+  // (not while recording per-tile costs: expanded tiles have no work items to time)
+  if (esc_wanted && !want_record) {
+    size_t fb = 0, tb = 0;
+    FCC_CUDA(cudaMemGetInfo(&fb, &tb));
+    const unsigned __int128 keyspace = (unsigned __int128)nA2 * esc_rows * LB;
+    esc = ptotal <= 0xFFFFFFFFull && (unsigned __int128)ptotal * 56 <= fb / 2 && keyspace < ((unsigned __int128)1 << 64);
+  }
+
   // ---- class per tile ----
   ClassTable ctab{};
   for (int c = 0; c < FCC_NUM_CLASSES; c++) {
@@ -2280,7 +2303,10 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     ctab.hash[c] = hc[c].hash ? 1u : 0u;
   }
   ctab.forced = forced;
-  ctab.fill_log2 = opt.dense_fill_log2;
+  // dense_fill_log2 = 0: tiles under a quarter full leave the dense class
+  // when hash tiles are expanded (expansion beats a sparse dense tile), else
+  // every tile that fits stays dense
+  ctab.fill_log2 = opt.dense_fill_log2 > 0 ? opt.dense_fill_log2 : (opt.dense_fill_log2 == 0 && esc && esc_mode == 2) ? 2 : 0;
   ctab.override_log2 = 0.32f;  // the model must predict at least 25% cheaper to leave the rule
   const u32 *lb_or_null = dense ? tile_lb : nullptr;
   float *feat = nullptr, *pred = nullptr;
@@ -2325,28 +2351,6 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   // tiles in class order (stable), so that each class's items are contiguous
   radix_sort_pairs(ckey, corder, nA2, 3, ar, st, ctx->d_err);
 
-  // Hash tiles expanded, sorted and reduced instead of accumulated in tables
-  // (esc_mode 2: every hash tile; 1: tiles too big for their table, which
-  // otherwise split into items merged through a global hash table), when the
-  // pairs fit (at most 56 bytes of temporaries per multiply-add, within half
-  // of the free device memory) and the key space fits 64 bits. By default
-  // every hash tile, unless the caller chose the classes (a forced hash class
-  // or the learned schedule: then the tables run and only the oversized tiles
-  // expand); a fixed workspace (the allocation-free call) expands only on
-  // request, since the pairs may not fit where the hash tables do.
-  const u64 esc_rows = grouped ? dense_cap : TL;
-  bool esc = false;
-  int esc_mode = opt.hash_esc;
-  if (esc_mode == 0)
-    esc_mode = ar.is_fixed() ? -1 : ((forced >= 0 && forced != FCC_CLASS_DENSE) || learned) ? 1 : 2;
-  const bool esc_wanted = esc_mode > 0;
-  // (not while recording per-tile costs: expanded tiles have no work items to time)
-  if (esc_wanted && !want_record) {
-    size_t fb = 0, tb = 0;
-    FCC_CUDA(cudaMemGetInfo(&fb, &tb));
-    const unsigned __int128 keyspace = (unsigned __int128)nA2 * esc_rows * LB;
-    esc = ptotal <= 0xFFFFFFFFull && (unsigned __int128)ptotal * 56 <= fb / 2 && keyspace < ((unsigned __int128)1 << 64);
-  }
   u32 *t_items = ar.get_n<u32>(nA2), *t_split_d = ar.get_n<u32>(nA2), *t_split_h = ar.get_n<u32>(nA2);
   u64 *t_cap = ar.get_n<u64>(nA2), *t_hsz = ar.get_n<u64>(nA2);
   u32 *esc_flag = ar.get_n<u32>(nA2), *esc_idx = ar.get_n<u32>(nA2);

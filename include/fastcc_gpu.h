@@ -102,8 +102,9 @@ typedef struct fcc_options {
                                  0 or -1 off (default), or a count (multiple of 32) */
   int32_t schedule;           /* fcc_schedule: how each output tile picks its class */
   int32_t dense_fill_log2;    /* FCC_SCHED_RULE: a tile takes the dense class only when its
-                                 multiply-adds >= its area / 2^dense_fill_log2; 0 = whenever
-                                 the tile fits the dense accumulator */
+                                 multiply-adds >= its area / 2^dense_fill_log2; -1: whenever the
+                                 tile fits the dense accumulator; 0 (default): 2 when hash tiles
+                                 are expanded (hash_esc), else -1 */
   int32_t dense_staging;      /* 0: dense tiles stage the B segments of long A entries in shared
                                  memory with bulk copies when the ring fits beside the tile;
                                  -1: never */
