@@ -2264,12 +2264,16 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   k_row_tiles<<<grid_for(nA2, 256), 256, 0, st>>>(rowA, rflag, rank, nA2, rg, gfirst, slotA, tflag);
   FCC_LAUNCH_CHECK();
   scan_exclusive(tflag, tidx, nA2, sc32(S_NTILES), ar, st);
-  u32 *tile_abeg = ar.get_n<u32>(nA2 + 1), *tile_rank0 = ar.get_n<u32>(nA2);
-  u32 *tile_lb = ar.get_n<u32>(nA2), *tile_nrows = ar.get_n<u32>(nA2);
+  // The tile count sizes every per-tile array, scan and launch below (tiles
+  // are far fewer than A entries: 20,000 against 10M on zipf3).
+  read_scalars(ctx, d_sc);
+  const u32 NT = std::max<u32>(scalar32(ctx, S_NTILES), 1);
+  u32 *tile_abeg = ar.get_n<u32>(NT + 1), *tile_rank0 = ar.get_n<u32>(NT);
+  u32 *tile_lb = ar.get_n<u32>(NT), *tile_nrows = ar.get_n<u32>(NT);
   k_tile_write<<<grid_for(nA2, 256), 256, 0, st>>>(rowA, tflag, tidx, rank, nA2, rg, tile_abeg, tile_rank0,
                                                    tile_lb);
   FCC_LAUNCH_CHECK();
-  k_tile_nrows<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), tile_abeg, rank, tile_rank0, tile_nrows);
+  k_tile_nrows<<<grid_for(NT, 256), 256, 0, st>>>(sc32(S_NTILES), tile_abeg, rank, tile_rank0, tile_nrows);
   FCC_LAUNCH_CHECK();
 
   // Hash tiles expanded, sorted and reduced instead of accumulated in tables
@@ -2291,7 +2295,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (esc_wanted && !want_record) {
     size_t fb = 0, tb = 0;
     FCC_CUDA(cudaMemGetInfo(&fb, &tb));
-    const unsigned __int128 keyspace = (unsigned __int128)nA2 * esc_rows * LB;
+    const unsigned __int128 keyspace = (unsigned __int128)NT * esc_rows * LB;
     esc = ptotal <= 0xFFFFFFFFull && (unsigned __int128)ptotal * 56 <= fb / 2 && keyspace < ((unsigned __int128)1 << 64);
   }
 
@@ -2311,19 +2315,19 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   const u32 *lb_or_null = dense ? tile_lb : nullptr;
   float *feat = nullptr, *pred = nullptr;
   if (learned || want_record) {
-    feat = ar.get_n<float>(size_t(nA2) * FCC_SCHED_FEATURES);
-    tile_features(st, sc32(S_NTILES), u32(nA2), tile_abeg, P, tile_nrows, lb_or_null, LB, feat);
+    feat = ar.get_n<float>(size_t(NT) * FCC_SCHED_FEATURES);
+    tile_features(st, sc32(S_NTILES), u32(NT), tile_abeg, P, tile_nrows, lb_or_null, LB, feat);
   }
   if (learned) {
-    pred = ar.get_n<float>(size_t(nA2) * FCC_NUM_CLASSES);
-    predict_costs(st, sc32(S_NTILES), u32(nA2), feat, ctx->sched->model, pred);
+    pred = ar.get_n<float>(size_t(NT) * FCC_NUM_CLASSES);
+    predict_costs(st, sc32(S_NTILES), u32(NT), feat, ctx->sched->model, pred);
     // With sched_mix_margin > 0, a launch-level decision: predicted totals of
     // every class run on all tiles, and of the per-tile best; classes are mixed
     // only when the mix is predicted to win by that margin, otherwise every
     // tile takes the class of the lowest predicted total.
     if (opt.sched_mix_margin > 0) {
     FCC_CUDA(cudaMemsetAsync(d_sc + S_PSUM0, 0, sizeof(u64) * (FCC_NUM_CLASSES + 1), st));
-    k_pred_sums<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), nA2, pred, ctab,
+    k_pred_sums<<<grid_for(NT, 256), 256, 0, st>>>(sc32(S_NTILES), NT, pred, ctab,
                                                     reinterpret_cast<double *>(d_sc + S_PSUM0));
     FCC_LAUNCH_CHECK();
     read_scalars(ctx, d_sc);
@@ -2342,34 +2346,34 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     }
     }
   }
-  u32 *cls = ar.get_n<u32>(nA2);
-  u64 *ckey = ar.get_n<u64>(nA2);
-  u32 *corder = ar.get_n<u32>(nA2);
-  k_tile_class<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), nA2, tile_abeg, P, tile_nrows, lb_or_null, LB,
+  u32 *cls = ar.get_n<u32>(NT);
+  u64 *ckey = ar.get_n<u64>(NT);
+  u32 *corder = ar.get_n<u32>(NT);
+  k_tile_class<<<grid_for(NT, 256), 256, 0, st>>>(sc32(S_NTILES), NT, tile_abeg, P, tile_nrows, lb_or_null, LB,
                                                    ctab, pred, cls, ckey, corder);
   FCC_LAUNCH_CHECK();
   // tiles in class order (stable), so that each class's items are contiguous
-  radix_sort_pairs(ckey, corder, nA2, 3, ar, st, ctx->d_err);
+  radix_sort_pairs(ckey, corder, NT, 3, ar, st, ctx->d_err);
 
-  u32 *t_items = ar.get_n<u32>(nA2), *t_split_d = ar.get_n<u32>(nA2), *t_split_h = ar.get_n<u32>(nA2);
-  u64 *t_cap = ar.get_n<u64>(nA2), *t_hsz = ar.get_n<u64>(nA2);
-  u32 *esc_flag = ar.get_n<u32>(nA2), *esc_idx = ar.get_n<u32>(nA2);
-  u64 *esc_cnt = ar.get_n<u64>(nA2), *esc_off = ar.get_n<u64>(nA2);
-  k_tile_items<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), nA2, corder, cls, tile_abeg, P, tile_nrows,
+  u32 *t_items = ar.get_n<u32>(NT), *t_split_d = ar.get_n<u32>(NT), *t_split_h = ar.get_n<u32>(NT);
+  u64 *t_cap = ar.get_n<u64>(NT), *t_hsz = ar.get_n<u64>(NT);
+  u32 *esc_flag = ar.get_n<u32>(NT), *esc_idx = ar.get_n<u32>(NT);
+  u64 *esc_cnt = ar.get_n<u64>(NT), *esc_off = ar.get_n<u64>(NT);
+  k_tile_items<<<grid_for(NT, 256), 256, 0, st>>>(sc32(S_NTILES), NT, corder, cls, tile_abeg, P, tile_nrows,
                                                    lb_or_null, LB, ctab, esc ? esc_mode : 0, t_items, t_split_d, t_split_h,
                                                    t_cap, t_hsz, esc_flag, esc_cnt);
   FCC_LAUNCH_CHECK();
-  scan_exclusive(esc_flag, esc_idx, nA2, sc32(S_NESC), ar, st);
-  scan_exclusive(esc_cnt, esc_off, nA2, d_sc + S_ESC_PAIRS, ar, st);
-  u32 *item_off = ar.get_n<u32>(nA2), *split_d_idx = ar.get_n<u32>(nA2), *split_h_idx = ar.get_n<u32>(nA2);
-  u64 *t_hoff = ar.get_n<u64>(nA2);
-  scan_exclusive(t_items, item_off, nA2, sc32(S_NITEMS), ar, st);
-  scan_exclusive(t_split_d, split_d_idx, nA2, sc32(S_NSPLIT), ar, st);
-  scan_exclusive(t_split_h, split_h_idx, nA2, sc32(S_NSPLIT_H), ar, st);
-  scan_exclusive(t_cap, t_cap, nA2, d_sc + S_CAP, ar, st);
-  scan_exclusive(t_hsz, t_hoff, nA2, d_sc + S_HASH, ar, st);
+  scan_exclusive(esc_flag, esc_idx, NT, sc32(S_NESC), ar, st);
+  scan_exclusive(esc_cnt, esc_off, NT, d_sc + S_ESC_PAIRS, ar, st);
+  u32 *item_off = ar.get_n<u32>(NT), *split_d_idx = ar.get_n<u32>(NT), *split_h_idx = ar.get_n<u32>(NT);
+  u64 *t_hoff = ar.get_n<u64>(NT);
+  scan_exclusive(t_items, item_off, NT, sc32(S_NITEMS), ar, st);
+  scan_exclusive(t_split_d, split_d_idx, NT, sc32(S_NSPLIT), ar, st);
+  scan_exclusive(t_split_h, split_h_idx, NT, sc32(S_NSPLIT_H), ar, st);
+  scan_exclusive(t_cap, t_cap, NT, d_sc + S_CAP, ar, st);
+  scan_exclusive(t_hsz, t_hoff, NT, d_sc + S_HASH, ar, st);
   FCC_CUDA(cudaMemsetAsync(d_sc + S_CLS0, 0xFF, sizeof(u64) * FCC_NUM_CLASSES, st));  // ~0: class unused
-  k_class_bounds<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), ckey, item_off, d_sc + S_CLS0);
+  k_class_bounds<<<grid_for(NT, 256), 256, 0, st>>>(sc32(S_NTILES), ckey, item_off, d_sc + S_CLS0);
   FCC_LAUNCH_CHECK();
   read_scalars(ctx, d_sc);
   const u32 nitems = scalar32(ctx, S_NITEMS);
@@ -2392,13 +2396,13 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   }
 
   Item *items = ar.get_n<Item>(std::max<u32>(nitems, 1));
-  int *split_of_tile = ar.get_n<int>(nA2);
+  int *split_of_tile = ar.get_n<int>(NT);
   u32 *split_tiles_d = ar.get_n<u32>(std::max<u32>(nsplit_d, 1));
   u32 *split_tiles_h = ar.get_n<u32>(std::max<u32>(nsplit_h, 1));
-  u64 *hoff_t = ar.get_n<u64>(nA2), *hsz_t = ar.get_n<u64>(nA2);
+  u64 *hoff_t = ar.get_n<u64>(NT), *hsz_t = ar.get_n<u64>(NT);
   u32 *esc_tiles = ar.get_n<u32>(std::max<u32>(nesc, 1));
   u64 *esc_base = ar.get_n<u64>(std::max<u32>(nesc, 1));
-  k_item_write<<<grid_for(nA2, 256), 256, 0, st>>>(sc32(S_NTILES), corder, cls, tile_abeg, P, item_off, ctab, items,
+  k_item_write<<<grid_for(NT, 256), 256, 0, st>>>(sc32(S_NTILES), corder, cls, tile_abeg, P, item_off, ctab, items,
                                                    t_split_d, t_split_h, split_d_idx, split_h_idx, split_of_tile,
                                                    split_tiles_d, split_tiles_h, t_hoff, t_hsz, hoff_t, hsz_t,
                                                    esc_flag, esc_idx, esc_off, esc_tiles, esc_base);
@@ -2460,8 +2464,8 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     gvals = ar.get_n<double>(hash_total);
   }
   u64 *item_cyc = want_record ? ar.get_n<u64>(std::max<u32>(nitems, 1)) : nullptr;
-  u64 *merge_cyc = want_record ? ar.get_n<u64>(nA2) : nullptr;
-  if (merge_cyc) FCC_CUDA(cudaMemsetAsync(merge_cyc, 0, sizeof(u64) * nA2, st));
+  u64 *merge_cyc = want_record ? ar.get_n<u64>(NT) : nullptr;
+  if (merge_cyc) FCC_CUDA(cudaMemsetAsync(merge_cyc, 0, sizeof(u64) * NT, st));
   u32 *counters = ar.get_n<u32>(FCC_NUM_CLASSES * kMaxWaves);  // item counters per wave and class
   tm.mark(3);
 
