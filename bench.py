@@ -37,10 +37,10 @@ METRIC = "FP64 multiply-adds/s & ms/contraction: learned+batched vs plain, 1 GB3
 UNIT = "multiply-adds/s"
 WORKLOAD = "zipf3: A 20000x20000x500000, 10M nnz, Zipf(1.2) per mode, lognormal values; A x A over modes {1,2}"
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_contract_dense launch:
-# measured with ncu on the 2.5M-nonzero case of the same extents (0.139 GB read
-# + 3.222 GB written for 3.381 GB of algorithmic bytes) and scaled by
+# measured with ncu on the 2.5M-nonzero case of the same extents (0.142 GB read
+# + 3.132 GB written for 3.381 GB of algorithmic bytes) and scaled by
 # algorithmic bytes to this workload's 6.695 GB.
-MEASURED_TRAFFIC = 6.695e9 * (0.1394 + 3.2217) / 3.381
+MEASURED_TRAFFIC = 6.695e9 * (0.1422 + 3.1322) / 3.381
 
 
 def load_peaks():

@@ -2540,9 +2540,6 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     };
     stream_out = pinned_host(ctx->out_vals) && (out_order == 0 || pinned_host(ctx->out_coords));
   }
-  const int waves = !stream_out          ? 1
-                    : opt.out_waves > 0 ? opt.out_waves
-                                        : int(std::min<u64>(kMaxWaves, std::max<u64>(1, (cap * per_out) >> 29)));
   struct StageBufs {  // device copy of a streamed output, freed after its copies
     cudaStream_t st = nullptr, cs = nullptr;
     void *p[2] = {nullptr, nullptr};
@@ -2553,19 +2550,27 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     }
   } stage_bufs;
   stage_bufs.st = st;
-  stage_bufs.cs = stream_out ? ctx->copy_stream : nullptr;
+  if (stream_out) {  // without room for the device copy, the tile kernels store to the host themselves
+    try {
+      stage_bufs.p[0] = pool_alloc(ctx->pool, sizeof(double) * cap, st);
+      if (out_order > 0) stage_bufs.p[1] = pool_alloc(ctx->pool, sizeof(u32) * cap * out_order, st);
+      stage_bufs.cs = ctx->copy_stream;
+    } catch (const Error &e) {
+      if (e.status != FCC_ERR_OOM) throw;
+      stream_out = false;
+    }
+  }
+  const int waves = !stream_out          ? 1
+                    : opt.out_waves > 0 ? opt.out_waves
+                                        : int(std::min<u64>(kMaxWaves, std::max<u64>(1, (cap * per_out) >> 29)));
   for (int attempt = 0;; attempt++) {
     i64 stride = i64(cap);
     if (!caller_out) {
       res->d_vals = static_cast<double *>(pool_alloc(ctx->pool, sizeof(double) * cap, st));
       if (out_order > 0) res->d_coords = static_cast<u32 *>(pool_alloc(ctx->pool, sizeof(u32) * cap * out_order, st));
     } else if (stream_out) {
-      res->d_vals = static_cast<double *>(pool_alloc(ctx->pool, sizeof(double) * cap, st));
-      stage_bufs.p[0] = res->d_vals;
-      if (out_order > 0) {
-        res->d_coords = static_cast<u32 *>(pool_alloc(ctx->pool, sizeof(u32) * cap * out_order, st));
-        stage_bufs.p[1] = res->d_coords;
-      }
+      res->d_vals = static_cast<double *>(stage_bufs.p[0]);
+      res->d_coords = static_cast<u32 *>(stage_bufs.p[1]);
     } else {
       res->d_vals = ctx->out_vals;
       res->d_coords = ctx->out_coords;
