@@ -203,14 +203,35 @@ __global__ void k_seg_write(const u64 *__restrict__ key, const u32 *__restrict__
   }
 }
 
-// For each A nonzero (in row-sorted order) find the B segment of its key.
+// Segments per bucket of the key space (key >> shift); an exclusive scan
+// turns the counts into bstart[b] = the first segment of bucket b.
+__global__ void k_seg_buckets(const u64 *__restrict__ ukey, const u32 *__restrict__ nseg_p, int shift,
+                              u32 *__restrict__ count) {
+  const u32 nseg = *nseg_p;
+  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < i64(nseg); i += i64(gridDim.x) * blockDim.x) {
+    const u64 b = ukey[i] >> shift;
+    // A bucket's segments are consecutive: they are counted in pieces that
+    // start at the bucket's first segment or at a multiple of 32 and end
+    // before the next multiple of 32 (one atomic per piece).
+    if (i == 0 || (ukey[i - 1] >> shift) != b || i % 32 == 0) {
+      u32 n = 1;
+      while (i + n < nseg && (i + n) % 32 != 0 && (ukey[i + n] >> shift) == b) n++;
+      atomicAdd(&count[b], n);
+    }
+  }
+}
+
+// For each A nonzero (in row-sorted order) find the B segment of its key:
+// a binary search within the key's bucket.
 __global__ void k_lookup(const u64 *__restrict__ keyA, const u32 *__restrict__ permA, i64 n,
                          const u64 *__restrict__ ukey, const u32 *__restrict__ nseg_p,
+                         const u32 *__restrict__ bstart, int shift, u64 nbuckets,
                          u32 *__restrict__ seg, u32 *__restrict__ flag) {
   const u32 nseg = *nseg_p;
   for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
     const u64 k = keyA[permA[i]];
-    u32 lo = 0, hi = nseg;  // first index with ukey >= k
+    const u64 b = min(k >> shift, nbuckets - 1);
+    u32 lo = bstart[b], hi = bstart[b + 1];  // first index with ukey >= k lies in [lo, hi]
     while (lo < hi) {
       u32 mid = (lo + hi) >> 1;
       if (ukey[mid] < k) lo = mid + 1; else hi = mid;
@@ -2092,11 +2113,21 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   u32 *segbeg = ar.get_n<u32>(nB + 1);
   k_seg_write<<<grid_for(nB, 256), 256, 0, st>>>(keyB, flagB, idxB, nB, ukey, segbeg);
   FCC_LAUNCH_CHECK();
+  // about one bucket per B nonzero over the key space (keys < 2^kbits)
+  const int kbits = bits_for(sb.keyspace - 1), bbits = std::min(kbits, std::max(1, bits_for(u64(nB))));
+  const int bshift = kbits - bbits;
+  const u64 nbuckets = u64(1) << bbits;
+  u32 *bcount = ar.get_n<u32>(nbuckets + 1), *bstart = ar.get_n<u32>(nbuckets + 1);
+  FCC_CUDA(cudaMemsetAsync(bcount, 0, sizeof(u32) * (nbuckets + 1), st));
+  k_seg_buckets<<<grid_for(nB, 256), 256, 0, st>>>(ukey, sc32(S_NSEG), bshift, bcount);
+  FCC_LAUNCH_CHECK();
+  scan_exclusive(bcount, bstart, i64(nbuckets + 1), nullptr, ar, st);
 
   // ---- A: sort by row, look up segments, drop unmatched ----
   radix_sort_pairs(extA, permA, nA, bits_for(sa.span - 1), ar, st, ctx->d_err);
   u32 *segTmp = ar.get_n<u32>(nA), *flagA = ar.get_n<u32>(nA), *idxA = ar.get_n<u32>(nA);
-  k_lookup<<<grid_for(nA, 256), 256, 0, st>>>(keyA, permA, nA, ukey, sc32(S_NSEG), segTmp, flagA);
+  k_lookup<<<grid_for(nA, 256), 256, 0, st>>>(keyA, permA, nA, ukey, sc32(S_NSEG), bstart, bshift, nbuckets,
+                                               segTmp, flagA);
   FCC_LAUNCH_CHECK();
   scan_exclusive(flagA, idxA, nA, sc32(S_NA2), ar, st);
   u64 *rowA = ar.get_n<u64>(nA);
