@@ -409,7 +409,7 @@ __global__ void k_pred_sums(const u32 *__restrict__ ntiles_p, i64 nmax, const fl
     double mn = 1e300;
     for (int c = 0; c < FCC_NUM_CLASSES; c++) {
       if (!ct.enabled[c]) continue;
-      const double v = exp2(double(pred[t * FCC_NUM_CLASSES + c]));
+      const double v = double(exp2f(pred[t * FCC_NUM_CLASSES + c]));  // FP32 power, FP64 sums
       s[c] += v;
       mn = fmin(mn, v);
     }
@@ -1498,11 +1498,13 @@ __global__ void __launch_bounds__(kTileThreads) k_merge_hash(HashArgs<ColT> a) {
 
 // ---------------------------------------------- expand, sort, reduce ----
 //
-// Hash tiles with more multiply-adds than a table holds (hub rows) are not
-// split into table-sized items merged through a global hash; their products
-// are expanded into (key, value) pairs, key = esc index x span + slot x LB +
-// column, radix-sorted (stable, so equal keys keep the products' order) and
-// reduced run by run: every output written once, no atomics.
+// Hash tiles (by default all of them; with a forced hash class only those
+// with more multiply-adds than a table holds) are not
+// accumulated in shared-memory tables: their products are expanded into
+// (key, value) pairs, key = esc index x span + slot x LB + column (the esc
+// index local to a group of tiles whose keys fit 32 bits), radix-sorted
+// (stable, so equal keys keep the products' order) and reduced run by run:
+// every output written once, no atomics.
 
 struct EscArgs {
   const u32 *tiles;     // esc index -> tile
@@ -2312,15 +2314,15 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   // otherwise split into items merged through a global hash table), when the
   // pairs fit (at most 56 bytes of temporaries per multiply-add, within half
   // of the free device memory) and the key space fits 64 bits. By default
-  // every hash tile, unless the caller chose the classes (a forced hash class
-  // or the learned schedule: then the tables run and only the oversized tiles
-  // expand); a fixed workspace (the allocation-free call) expands only on
-  // request, since the pairs may not fit where the hash tables do.
+  // every hash tile, unless the caller forced a hash class (then its tables
+  // run and only the oversized tiles expand); a fixed workspace (the
+  // allocation-free call) expands only on request, since the pairs may not fit
+  // where the hash tables do.
   const u64 esc_rows = grouped ? dense_cap : TL;
   bool esc = false;
   int esc_mode = opt.hash_esc;
   if (esc_mode == 0)
-    esc_mode = ar.is_fixed() ? -1 : ((forced >= 0 && forced != FCC_CLASS_DENSE) || learned) ? 1 : 2;
+    esc_mode = ar.is_fixed() ? -1 : (forced >= 0 && forced != FCC_CLASS_DENSE) ? 1 : 2;
   const bool esc_wanted = esc_mode > 0;
   // (not while recording per-tile costs: expanded tiles have no work items to time)
   if (esc_wanted && !want_record) {

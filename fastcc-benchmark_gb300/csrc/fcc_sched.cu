@@ -35,38 +35,40 @@ __global__ void k_tile_features(const u32 *__restrict__ ntiles_p, u32 nmax, cons
   const u32 wstride = (gridDim.x * blockDim.x) >> 5;
   for (u32 t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntiles; t += wstride) {
     const u32 e0 = abeg[t], e1 = abeg[t + 1];
-    double sl = 0, sw = 0, sc = 0;
-    u64 mx = 0;
+    // integer sums and FP32 logarithms: FP64 issues at 1/64 of FP32 on this
+    // GPU, and a lane-0 FP64 tail per tile cost more than the whole plan
+    u64 sl = 0, sw = 0, sc = 0, mx = 0;
     for (u32 e = e0 + lane; e < e1; e += 32) {
       const u64 len = P[e + 1] - P[e];
-      if (len < 64) sl += double(len);
-      else if (len < 1024) sw += double(len);
-      else sc += double(len);
+      if (len < 64) sl += len;
+      else if (len < 1024) sw += len;
+      else sc += len;
       mx = max(mx, len);
     }
     for (int o = 16; o; o >>= 1) {
-      sl += __shfl_xor_sync(kFull, sl, o);
-      sw += __shfl_xor_sync(kFull, sw, o);
-      sc += __shfl_xor_sync(kFull, sc, o);
+      sl += __shfl_xor_sync(kFull, (unsigned long long)sl, o);
+      sw += __shfl_xor_sync(kFull, (unsigned long long)sw, o);
+      sc += __shfl_xor_sync(kFull, (unsigned long long)sc, o);
       mx = max(mx, (u64)__shfl_xor_sync(kFull, (unsigned long long)mx, o));
     }
     if (lane == 0) {
-      const double prod = double(P[e1] - P[e0]), nent = double(e1 - e0), rows = double(nrows[t]);
-      const double span = double(lb ? u64(lb[t]) : LB), area = rows * span;
-      const double pd = prod > 0 ? prod : 1.0;
+      const u64 prodi = P[e1] - P[e0];
+      const float prod = float(prodi), nent = float(e1 - e0), rows = float(nrows[t]);
+      const float span = float(lb ? u64(lb[t]) : LB), area = rows * span;
+      const float pd = prodi > 0 ? prod : 1.f;
       float *f = feat + size_t(t) * kF;
-      f[0] = float(log2(1.0 + prod));
-      f[1] = float(log2(1.0 + nent));
-      f[2] = float(log2(rows));
-      f[3] = float(log2(span));
-      f[4] = float(log2(area));
-      f[5] = float(fmin(prod, area) / area);
-      f[6] = float(sl / pd);
-      f[7] = float(sw / pd);
-      f[8] = float(sc / pd);
-      f[9] = float(log2(1.0 + prod / fmax(nent, 1.0)));
-      f[10] = float(log2(1.0 + double(mx)));
-      f[11] = float(log2(1.0 + prod / rows));
+      f[0] = log2f(1.f + prod);
+      f[1] = log2f(1.f + nent);
+      f[2] = log2f(rows);
+      f[3] = log2f(span);
+      f[4] = log2f(area);
+      f[5] = fminf(prod, area) / area;
+      f[6] = float(sl) / pd;
+      f[7] = float(sw) / pd;
+      f[8] = float(sc) / pd;
+      f[9] = log2f(1.f + prod / fmaxf(nent, 1.f));
+      f[10] = log2f(1.f + float(mx));
+      f[11] = log2f(1.f + prod / rows);
     }
   }
 }

@@ -116,8 +116,8 @@ typedef struct fcc_options {
                                  pairs fit in device memory. 2: every hash tile; 1: the tiles
                                  larger than their table (the others run the tables); -1: none
                                  (large tiles split into items merged through a global hash
-                                 table); 0 (default): 2, or 1 with a forced hash class or the
-                                 learned schedule, or -1 in allocation-free calls */
+                                 table); 0 (default): 2, or 1 with a forced hash class, or -1
+                                 in allocation-free calls */
   int32_t out_waves;          /* fcc_contract_into with pinned host output buffers: the output is
                                  produced in device memory in this many waves of tiles (1..16),
                                  each wave's outputs copied to the host while the next computes.
