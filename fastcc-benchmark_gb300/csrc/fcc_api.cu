@@ -310,7 +310,7 @@ void autotune(fcc_ctx *ctx, const std::string &sig, const fcc_options &base, int
     o.dense_fill_log2 = fill;
     cand.push_back(o);
   };
-  for (int threads : {512, 1024}) {
+  for (int threads : {640, 512, 1024}) {
     add(FCC_SCHED_RULE, threads, 0);
     add(FCC_SCHED_RULE, threads, -1);
     add(FCC_SCHED_RULE, threads, 6);

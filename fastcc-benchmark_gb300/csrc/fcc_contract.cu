@@ -579,7 +579,8 @@ __global__ void k_apply_colmap(ColT *__restrict__ col, i64 n, const u32 *__restr
 //  * shorter entries go one per lane, up to 32 at once, so rows made of many
 //    rare keys (hub rows of Zipf tensors) keep every lane busy.
 
-constexpr int kTileThreads = 512;  // default; 1024 is the other instantiation (tile_threads)
+constexpr int kTileThreads = 640;   // dense tiles by default (20 warps in 96 registers); 512, 768, 1024 on request
+constexpr int kMergeThreads = 512;  // merges of split tiles
 constexpr int kBatch = 4;
 constexpr u32 kLongRun = 64;
 constexpr u64 kNegZero = 0x8000000000000000ull;
@@ -798,7 +799,7 @@ __device__ void build_item_plan(const u64 *__restrict__ P, u32 ea, u32 eb, u64 p
 // is an mbarrier poll with a bounded count; on timeout the kernel flags
 // ERRB_INTERNAL, stops issuing, waits (bounded) for its copies in flight and
 // skips its remaining work.
-constexpr u32 kStageCh = 1920;  // 4 x 480 consumer threads of a 512-thread tile: no partial round
+constexpr u32 kStageCh = 1824;  // 3 x 608 consumer threads of a 640-thread tile: no partial round
 constexpr u32 kStageBufs = 2;
 constexpr u32 kStageValBytes = (kStageCh + 2) * 8;  // 16-byte multiple: room for a 1-element head
 constexpr u32 kStageColBytes = (kStageCh + 4) * 4;  // 16-byte multiple: room for a 3-element head
@@ -1254,7 +1255,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
   }
 }
 
-__global__ void __launch_bounds__(kTileThreads) k_merge_dense(DenseArgs a) {
+__global__ void __launch_bounds__(kMergeThreads) k_merge_dense(DenseArgs a) {
   __shared__ u32 s_warp[32];
   __shared__ u32 s_cnt[1024];
   __shared__ u64 s_base;
@@ -1481,7 +1482,7 @@ __global__ void __launch_bounds__(kThreads, kThreads == 128 ? 6 : kThreads == 25
 }
 
 template <class ColT>
-__global__ void __launch_bounds__(kTileThreads) k_merge_hash(HashArgs<ColT> a) {
+__global__ void __launch_bounds__(kMergeThreads) k_merge_hash(HashArgs<ColT> a) {
   __shared__ u32 s_wcnt[32];
   __shared__ u64 s_base;
   __shared__ u64 s_rows[kRowCache];
@@ -2184,24 +2185,23 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   // per tile; the items of one class run in one persistent launch.
   const bool custom_hash = opt.hash_slots > 0 || (opt.tile_threads > 0 && opt.accumulator == FCC_ACC_HASH);
   HostClass hc[FCC_NUM_CLASSES];
-  hc[FCC_CLASS_DENSE] = {false, opt.tile_threads > 0 ? opt.tile_threads : kTileThreads, 0u, 0, dense};
-  hc[FCC_CLASS_HASH_L] = {true, opt.tile_threads > 0 ? opt.tile_threads : 1024,
-                          opt.hash_slots > 0 ? u32(opt.hash_slots) : 8192u, 0, opt.accumulator != FCC_ACC_DENSE};
+  const int tt = opt.tile_threads;  // dense tiles: 512, 640, 768, 1024; large hash tables: 128 ... 1024
+  const bool tt_dense = tt == 512 || tt == 640 || tt == 768 || tt == 1024;
+  const bool tt_hash = tt == 128 || tt == 256 || tt == 512 || tt == 1024;
+  if (tt < 0 || (tt > 0 && !tt_dense && !tt_hash))
+    throw Error{FCC_ERR_ARG, "tile_threads must be 128, 256, 512, 640, 768 or 1024"};
+  hc[FCC_CLASS_DENSE] = {false, tt > 0 ? tt : kTileThreads, 0u, 0, dense};
+  hc[FCC_CLASS_HASH_L] = {true, tt > 0 && tt_hash ? tt : 1024, opt.hash_slots > 0 ? u32(opt.hash_slots) : 8192u, 0,
+                          opt.accumulator != FCC_ACC_DENSE};
   hc[FCC_CLASS_HASH_M] = {true, 256, 4096u, 0, opt.accumulator != FCC_ACC_DENSE && !custom_hash};
   hc[FCC_CLASS_HASH_S] = {true, 128, 2048u, 0, opt.accumulator != FCC_ACC_DENSE && !custom_hash};
   if (opt.accumulator == FCC_ACC_HASH) hc[FCC_CLASS_DENSE].enabled = false;
-  if (hc[FCC_CLASS_DENSE].threads != 512 && hc[FCC_CLASS_DENSE].threads != 1024) {
-    const int t = hc[FCC_CLASS_DENSE].threads;
-    if (opt.accumulator != FCC_ACC_HASH && t != 128 && t != 256)
-      throw Error{FCC_ERR_ARG, "tile_threads must be 128, 256, 512 or 1024"};
+  if (tt > 0 && !tt_dense) {  // 128 or 256: hash tables only
     if (opt.accumulator == FCC_ACC_DENSE) throw Error{FCC_ERR_ARG, "tile_threads 128 and 256 are for the hash accumulator"};
     hc[FCC_CLASS_DENSE].enabled = false;
     hc[FCC_CLASS_DENSE].threads = kTileThreads;
   }
   {
-    const int t = hc[FCC_CLASS_HASH_L].threads;
-    if (t != 128 && t != 256 && t != 512 && t != 1024)
-      throw Error{FCC_ERR_ARG, "tile_threads must be 128, 256, 512 or 1024"};
     const u32 hs = hc[FCC_CLASS_HASH_L].slots;
     if (hs & (hs - 1)) throw Error{FCC_ERR_ARG, "hash_slots must be a power of two"};
     if (size_t(hs) * 16 > smem_cap || hs < 64) throw Error{FCC_ERR_ARG, "hash_slots out of range"};
@@ -2650,6 +2650,10 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       const void *kern;
       if (threads == 512) kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true, 512>)
                                           : reinterpret_cast<const void *>(k_contract_dense<false, 512>);
+      else if (threads == 640) kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true, 640>)
+                                               : reinterpret_cast<const void *>(k_contract_dense<false, 640>);
+      else if (threads == 768) kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true, 768>)
+                                               : reinterpret_cast<const void *>(k_contract_dense<false, 768>);
       else kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true, 1024>)
                            : reinterpret_cast<const void *>(k_contract_dense<false, 1024>);
       FCC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
@@ -2657,6 +2661,12 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       if (threads == 512) {
         if (sentinel) k_contract_dense<true, 512><<<grid, 512, smem, st>>>(da);
         else k_contract_dense<false, 512><<<grid, 512, smem, st>>>(da);
+      } else if (threads == 640) {
+        if (sentinel) k_contract_dense<true, 640><<<grid, 640, smem, st>>>(da);
+        else k_contract_dense<false, 640><<<grid, 640, smem, st>>>(da);
+      } else if (threads == 768) {
+        if (sentinel) k_contract_dense<true, 768><<<grid, 768, smem, st>>>(da);
+        else k_contract_dense<false, 768><<<grid, 768, smem, st>>>(da);
       } else {
         if (sentinel) k_contract_dense<true, 1024><<<grid, 1024, smem, st>>>(da);
         else k_contract_dense<false, 1024><<<grid, 1024, smem, st>>>(da);
@@ -2696,11 +2706,11 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       }
       if (w >= 0) return;
       if (nsplit_d > 0) {
-        k_merge_dense<<<std::min<u32>(nsplit_d, u32(ctx->num_sms) * 2), kTileThreads, 0, st>>>(da);
+        k_merge_dense<<<std::min<u32>(nsplit_d, u32(ctx->num_sms) * 2), kMergeThreads, 0, st>>>(da);
         FCC_LAUNCH_CHECK();
       }
       if (nsplit_h > 0) {
-        k_merge_hash<ColT><<<std::min<u32>(nsplit_h, u32(ctx->num_sms) * 2), kTileThreads, 0, st>>>(ha);
+        k_merge_hash<ColT><<<std::min<u32>(nsplit_h, u32(ctx->num_sms) * 2), kMergeThreads, 0, st>>>(ha);
         FCC_LAUNCH_CHECK();
       }
       for (const EscGroup &e : escg) {  // expanded tiles: expand, sort, reduce, group by group

@@ -96,8 +96,8 @@ typedef struct fcc_options {
                                  smaller hint is not an error: the device counts every output
                                  and the call retries once with the exact count. */
   int32_t dense_mode;         /* fcc_dense_mode: how a dense tile marks touched positions */
-  int32_t tile_threads;       /* threads per tile CTA: 512 (default) or 1024; 128 or 256 for the
-                                 hash accumulator */
+  int32_t tile_threads;       /* threads per tile CTA: dense tiles 640 (default), 512, 768 or
+                                 1024; the large hash table 1024 (default), 128, 256 or 512 */
   int32_t hot_columns;        /* per-warp copies of the most frequent B columns in row tiles:
                                  0 or -1 off (default), or a count (multiple of 32) */
   int32_t schedule;           /* fcc_schedule: how each output tile picks its class */
@@ -131,7 +131,7 @@ typedef struct fcc_options {
  * differ in table size and CTA shape: the small ones run several CTAs per SM
  * so that small tiles overlap their barriers and memory latency. */
 enum {
-  FCC_CLASS_DENSE = 0,   /* shared-memory dense tile, 512 threads (tile_threads) */
+  FCC_CLASS_DENSE = 0,   /* shared-memory dense tile, 640 threads (tile_threads) */
   FCC_CLASS_HASH_L = 1,  /* hash, 8192 slots, 1024 threads (tile_threads), one CTA per SM */
   FCC_CLASS_HASH_M = 2,  /* hash, 4096 slots, 256 threads */
   FCC_CLASS_HASH_S = 3,  /* hash, 2048 slots, 128 threads */

@@ -47,6 +47,8 @@ VARIANTS = [
     {"hot_columns": 64, "accumulator": F.ACC_HASH},
     {"hot_columns": 32, "accumulator": F.ACC_HASH, "products_per_item": 6, "tile_threads": 512},
     {"tile_threads": 512, "hot_columns": -1},
+    {"tile_threads": 640},
+    {"tile_threads": 768, "products_per_item": 9},
     {"accumulator": F.ACC_HASH, "products_per_item": 5, "hash_esc": 1},    # expand-sort-reduce of split tiles
     {"accumulator": F.ACC_HASH, "hash_slots": 64, "hash_esc": 1},
     {"schedule": F.SCHED_FORCE + F.CLASS_HASH_S, "products_per_item": 40, "hash_esc": 1},
