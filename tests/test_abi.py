@@ -59,3 +59,24 @@ def test_no_device_is_a_status(tmp_path):
     h = ctypes.c_void_p()
     rc = F.lib().fcc_ctx_create(0, ctypes.byref(h))
     assert rc == 7 and not h.value
+
+
+def _c_struct_fields(header, name):
+    """(type, field) pairs of `typedef struct ... { ... } name;` in a header."""
+    txt = open(os.path.join(ROOT, "include", header)).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    m = re.search(r"typedef struct \w*\s*\{([^{}]*)\}\s*" + name + r"\s*;", txt)
+    assert m, name
+    return re.findall(r"\b(int32_t|int64_t|uint32_t|uint64_t|double|float)\s+(\w+)\s*;", m.group(1))
+
+
+def test_python_options_mirror_the_c_layout():
+    # same field names, order and widths as fcc_options in the header, so the
+    # binding cannot drift from the ABI
+    c = _c_struct_fields("fastcc_gpu.h", "fcc_options")
+    width = {"int32_t": 4, "uint32_t": 4, "int64_t": 8, "uint64_t": 8, "double": 8, "float": 4}
+    py = [(name, ctypes.sizeof(t)) for name, t in F.Options._fields_]
+    assert [n for _, n in c] == [n for n, _ in py]
+    assert [width[t] for t, _ in c] == [w for _, w in py]
+    for (t, name), (pname, _) in zip(c, py):
+        assert getattr(F.Options, pname).offset % width[t] == 0
