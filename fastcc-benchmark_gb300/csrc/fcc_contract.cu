@@ -2178,11 +2178,13 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (!dense && (unsigned __int128)TL * LB > (unsigned __int128)(~0ull) - 1)
     throw Error{FCC_ERR_OVERFLOW, "rows_per_tile x B external span exceeds 64 bits"};
   // ---- tile classes ----
-  // Every output tile runs in one class: the shared-memory dense tile, or an
-  // open-addressing hash table of 8192 slots (512 threads, one CTA per SM),
-  // 4096 or 2048 slots (256 threads, several CTAs per SM, so that small tiles
-  // overlap their barriers and memory latency). The schedule picks a class
-  // per tile; the items of one class run in one persistent launch.
+  // Every output tile runs in one class: the shared-memory dense tile (640
+  // threads by default), or an open-addressing hash table of 8192 slots (1024
+  // threads, one CTA per SM), 4096 or 2048 slots (256 / 128 threads, several
+  // CTAs per SM, so that small tiles overlap their barriers and memory
+  // latency). The schedule picks a class per tile; the items of one class run
+  // in one persistent launch. Hash-class tiles are expanded, sorted and
+  // reduced instead unless a hash class is forced (below).
   const bool custom_hash = opt.hash_slots > 0 || (opt.tile_threads > 0 && opt.accumulator == FCC_ACC_HASH);
   HostClass hc[FCC_NUM_CLASSES];
   const int tt = opt.tile_threads;  // dense tiles: 512, 640, 768, 1024; large hash tables: 128 ... 1024
