@@ -1525,7 +1525,7 @@ struct EscArgs {
 // search (over the tiles' first pairs, then over the tile's product prefix)
 // and advances both linearly from there. Hub rows have many A entries with
 // short B segments, so a warp per entry would leave most lanes idle.
-constexpr u32 kEscExpandPer = 8;
+constexpr u32 kEscExpandPer = 8;  // a multiple of 4: vector stores
 
 template <class ColT, class KeyT>
 __global__ void __launch_bounds__(256) k_esc_expand(EscArgs a, const ProdSrc src, const ColT *__restrict__ colB,
@@ -1600,8 +1600,9 @@ __global__ void __launch_bounds__(256) k_esc_expand(EscArgs a, const ProdSrc src
     if (cnt == kEscExpandPer) {  // 32 or 64 aligned bytes of keys, 64 of values
       if (sizeof(KeyT) == 4) {
         uint4 *dk = reinterpret_cast<uint4 *>(keys + q0);
-        dk[0] = make_uint4(u32(kk[0]), u32(kk[1]), u32(kk[2]), u32(kk[3]));
-        dk[1] = make_uint4(u32(kk[4]), u32(kk[5]), u32(kk[6]), u32(kk[7]));
+#pragma unroll
+        for (u32 i = 0; i < kEscExpandPer / 4; i++)
+          dk[i] = make_uint4(u32(kk[4 * i]), u32(kk[4 * i + 1]), u32(kk[4 * i + 2]), u32(kk[4 * i + 3]));
       } else {
         ulonglong2 *dk = reinterpret_cast<ulonglong2 *>(keys + q0);
 #pragma unroll
