@@ -7,17 +7,22 @@ A 20,000 x 20,000 x 500,000 with 10M distinct nonzeros, every mode Zipf(1.2),
 sign-random lognormal values, contracted over modes {1,2}.
 
   value  = FP64 multiply-adds per second, inputs resident on the device
-  e2e    = the same through the C ABI with host (pinned) operands and the full
-           output delivered to pinned host buffers inside the timed region
-           (fcc_contract_into: the output is produced on the device in waves of
-           tiles, each wave's entries copied to the host while the next computes;
-           copy_after_ms_per_step: device result, then one copy)
+  e2e    = the same through the C ABI (fcc_contract_into) with pinned host
+           operands and the full output delivered to pinned host buffers
+           inside the timed region (computed on the device, then copied once;
+           waves_ms_per_step: the output copied in 12 waves while later waves
+           compute)
   roofline: the tile contraction kernel (k_contract_dense); algorithmic bytes
            = inputs read once + outputs written once
-  cpu_baseline: the CPU oracle (restatement of the reference's OpenMP
-           fastcc_multiply) on a bounded sample of the same workload
+  cpu_baseline: the CPU port of the reference's OpenMP fastcc_multiply
+           (oracle/) on all host cores over the whole workload, timed inside
+           the library (index build, tile loop, output concatenation)
+  twomode, batched, readme: the other workloads, each with its own roofline
+           and CPU baseline; batched also against 256 autotuned plain calls
 
---impl reference times that CPU implementation alone (all host threads).
+--impl reference times that CPU implementation alone (all host threads), on
+the whole workload every step; its inputs are generated in a child process so
+that the reference arm loads no library of this package.
 Multi-GPU runs (torchrun) are replicas: every rank contracts its own copy.
 """
 import argparse
@@ -35,7 +40,10 @@ sys.path.insert(0, PKG)
 
 METRIC = "FP64 multiply-adds/s & ms/contraction: learned+batched vs plain, 1 GB300"
 UNIT = "multiply-adds/s"
-WORKLOAD = "zipf3: A 20000x20000x500000, 10M nnz, Zipf(1.2) per mode, lognormal values; A x A over modes {1,2}"
+def workload_name(nnz):
+    n = f"{nnz // 1_000_000}M" if nnz % 1_000_000 == 0 else str(nnz)
+    return (f"zipf3: A 20000x20000x500000, {n} nnz, Zipf(1.2) per mode, lognormal values; "
+            f"A x A over modes {{1,2}}")
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_contract_dense launch:
 # measured with ncu on the 2.5M-nonzero case of the same extents (0.142 GB read
 # + 3.132 GB written for 3.381 GB of algorithmic bytes) and scaled by
@@ -60,7 +68,16 @@ class Clocks:
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
-        self.index = index
+        # nvidia-smi numbers GPUs its own way: name the timed device by UUID
+        # (CUDA_VISIBLE_DEVICES may remap the index torch sees)
+        self.index = str(index)
+        try:
+            import torch
+            u = str(torch.cuda.get_device_properties(index).uuid)
+            if u:
+                self.index = u if u.startswith(("GPU-", "MIG-")) else "GPU-" + u
+        except Exception:
+            pass
         self.rows = []
         self._stop = threading.Event()
         self._t = None
@@ -125,54 +142,74 @@ def barrier(ws):
         dist.barrier()
 
 
-def cpu_sample(w, every, phase):
-    """The left operand restricted to rows i with i % every == phase; the right
-    operand is the whole tensor."""
-    a = w["a"]
-    sel = (a.coords[:, 0] % every) == phase
-    return a.coords[sel], a.values[sel]
-
-
-def time_cpu_oracle(w, every, nthreads):
+def cpu_port(a, b, ctr_a, ctr_b, nthreads=0):
+    """One call of the CPU port of the reference's fastcc_multiply
+    (oracle/fastcc_oracle.cpp, tile size 128 as benchmark.cpp:17) on all host
+    threads. Returns (multiply-adds, outputs, seconds), seconds being the
+    call's own time inside the library: index build, tile-pair loop with
+    drain, concatenation of the thread outputs and their decode."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    ac, av = cpu_sample(w, every, 0)
-    b = w["b"]
-    t0 = time.perf_counter()
-    o = oracle.fastcc_multiply(ac, av, w["a"].max_index, b.coords, b.values, b.max_index,
-                               w["ctr_a"], w["ctr_b"], tile_size=128, nthreads=nthreads)
-    dt = time.perf_counter() - t0
-    return o["products"], dt, len(o["values"])
+    o = oracle.fastcc_multiply(a.coords, a.values, a.max_index, b.coords, b.values, b.max_index, ctr_a, ctr_b,
+                               tile_size=128, nthreads=nthreads or (os.cpu_count() or 1), keep=False)
+    return o["products"], o["nnz"], o["total_ms"] / 1000.0
+
+
+class _HostTensor:
+    def __init__(self, coords, values, max_index):
+        self.coords, self.values, self.max_index = coords, values, max_index
+
+    @property
+    def nnz(self):
+        return int(self.values.shape[0])
+
+
+def dump_inputs(path, nnz):
+    """--dump-inputs: the benchmark operand, written for the reference arm."""
+    import numpy as np
+    import workloads
+    w = workloads.zipf3(seed=1, nnz=nnz)
+    a = w["a"]
+    np.savez(path, coords=a.coords, values=a.values, max_index=a.max_index)
 
 
 def run_reference(args, ws, rank):
-    """--impl reference: the reference's CPU algorithm (the oracle restatement,
-    compiled here; the reference's own sources are not on this machine) on all
-    host threads, one bounded sample of the workload per step."""
+    """--impl reference: the CPU port of the reference's fastcc_multiply
+    (the reference's own sources do not exist on the GPU machine; the port's
+    speed relative to them is measured where they do) on all host threads,
+    the whole workload every step."""
     if rank != 0:
         return
-    import workloads
+    import tempfile
+
+    import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
-    w = workloads.zipf3(seed=1)
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "zipf3.npz")
+        subprocess.check_call([sys.executable, os.path.abspath(__file__), "--dump-inputs", path,
+                               "--nnz", str(args.nnz)])
+        d = np.load(path)
+        a = _HostTensor(d["coords"], d["values"], d["max_index"])
     ncores = os.cpu_count() or 1
-    every = 64
     prods, secs = [], []
+    outs = 0
     for s in range(args.warmup + args.steps):
-        p, dt, _ = time_cpu_oracle(w, every, ncores)
+        p, outs, dt = cpu_port(a, a, [1, 2], [1, 2], ncores)
         if s >= args.warmup:
             prods.append(p)
             secs.append(dt)
     value = sum(prods) / sum(secs)
+    sample = (f"the whole workload every step ({prods[0]} multiply-adds, {outs} outputs); time inside the "
+              f"library: index build, tile loop, output concatenation and decode")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(secs) / len(secs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": f"left operand rows i % {every} == 0, right operand whole",
-                       "products_per_step": prods[0]},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port",
-                             "sample": f"rows i % {every} == 0 of the left operand ({prods[0]} multiply-adds)"},
+            "config": {"workload": workload_name(a.nnz), "nnz": a.nnz, "multiply_adds": prods[0], "outputs": outs,
+                       "sample": "whole workload"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -392,63 +429,71 @@ def run_sweep(name, variants, reps=3):
                               "contract_ms": med["contract"], "phases_ms": med}), flush=True)
 
 
-def run_twomode(steps, stream, local):
+def hbm_roofline(alg_bytes, ms, what):
+    """Achieved algorithmic bytes per second against the measured HBM peak."""
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (ms / 1000.0) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "algorithmic_bytes": alg_bytes, "ms": ms, "over": what, "peak_kind": peak_kind}
+
+
+def coo_bytes(nnz, order):
+    return nnz * (4 * order + 8)
+
+
+def run_twomode(steps, stream, local, cpu=True):
     """The two-mode self-contraction (A 5000x5000x2000x50, 5M nnz, over {0,2}):
     GPU time per contraction with the default schedule, device-resident, next
-    to the CPU oracle on all host cores over a row sample of the same
-    workload (rows j % 8 == 0 of the left operand)."""
-    import numpy as np
+    to the CPU port on all host cores over the same workload."""
     import torch
 
     import fastcc_gpu as F
     import workloads
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
     w = workloads.twomode(seed=1)
     a = w["a"]
     A = F.Tensor(torch.from_numpy(a.coords).cuda(), torch.from_numpy(a.values).cuda(), a.max_index)
     ctx = F.Context(local)
     ctx.set_stream(stream.cuda_stream)
+    opts = F.Options(timing=1)
     for _ in range(3):
-        ctx.contract(A, A, w["ctr_a"], w["ctr_b"]).free()
+        ctx.contract(A, A, w["ctr_a"], w["ctr_b"], opts).free()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     n = max(steps, 5)
+    phases = []
     e0.record(stream)
     for _ in range(n):
-        ctx.contract(A, A, w["ctr_a"], w["ctr_b"]).free()
+        ctx.contract(A, A, w["ctr_a"], w["ctr_b"], opts).free()
+        phases.append(ctx.timings())
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / n
     r = ctx.contract(A, A, w["ctr_a"], w["ctr_b"])
-    prods, outs = r.products, r.nnz
+    prods, outs, order = r.products, r.nnz, r.order
     r.free()
     ctx.close()
-    oracle.build()
-    sel = (a.coords[:, 1] % 8) == 0
-    threads = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    o = oracle.fastcc_multiply(a.coords[sel], a.values[sel], a.max_index, a.coords, a.values, a.max_index,
-                               w["ctr_a"], w["ctr_b"], tile_size=128, nthreads=threads)
-    dt = time.perf_counter() - t0
-    cpu_rate = o["products"] / dt
-    return {"workload": w["name"], "multiply_adds": prods, "outputs": outs, "gpu_ms": ms,
-            "multiply_adds_per_s": prods / (ms / 1000.0),
-            "cpu_oracle": {"multiply_adds_per_s": cpu_rate, "threads": threads,
-                           "sample": f"left operand rows with j % 8 == 0 ({o['products']} multiply-adds, {dt:.2f} s)"},
-            "gpu_vs_cpu": prods / (ms / 1000.0) / cpu_rate}
+    med = {k: round(statistics.median(p[k] for p in phases), 4) for k in phases[0]}
+    alg = 2 * coo_bytes(a.nnz, a.order) + coo_bytes(outs, order)
+    out = {"workload": w["name"], "multiply_adds": prods, "outputs": outs, "gpu_ms": ms,
+           "multiply_adds_per_s": prods / (ms / 1000.0), "phases_ms": med,
+           "roofline": hbm_roofline(alg, ms, "whole contraction (index, plan, expanded hash tiles: expand, "
+                                             "radix sort, reduce)")}
+    if cpu:
+        p, _, dt = cpu_port(a, a, w["ctr_a"], w["ctr_b"])
+        out["cpu_baseline"] = {"value": p / dt, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": f"the whole workload ({p} multiply-adds, {dt:.2f} s inside the library)"}
+        out["gpu_vs_cpu"] = (prods / (ms / 1000.0)) / (p / dt)
+    return out
 
 
-def run_readme(steps, stream, local):
+def run_readme(steps, stream, local, cpu=True):
     """The README contraction (256x64x256x64, 200k nnz, x 512x64x64, 100k
     nnz over {1,3} x {1,2}): GPU ms per contraction (device-resident and end to
-    end through the C ABI) next to the CPU oracle on all host cores."""
+    end through the C ABI) next to the CPU port on all host cores."""
     import torch
 
     import fastcc_gpu as F
     import workloads
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
     w = workloads.readme(seed=1)
     a, b = w["a"], w["b"]
     cuda = lambda t: F.Tensor(torch.from_numpy(t.coords).cuda(), torch.from_numpy(t.values).cuda(), t.max_index)
@@ -474,30 +519,27 @@ def run_readme(steps, stream, local):
     ms = timed(A, B, max(steps, 10))
     ms_e2e = timed(a, b, 3)
     r = ctx.contract(A, B, w["ctr_a"], w["ctr_b"])
-    prods, outs = r.products, r.nnz
+    prods, outs, order = r.products, r.nnz, r.order
     r.free()
     ctx.close()
-    threads = os.cpu_count() or 1
-    oracle.build()
-    cpu = []
-    for _ in range(3):
-        t0 = time.perf_counter()
-        oracle.fastcc_multiply(a.coords, a.values, a.max_index, b.coords, b.values, b.max_index, w["ctr_a"],
-                               w["ctr_b"], tile_size=128, nthreads=threads)
-        cpu.append(time.perf_counter() - t0)
-    cpu_ms = 1000 * statistics.median(cpu)
-    return {"workload": w["name"], "multiply_adds": prods, "outputs": outs, "gpu_ms": ms, "gpu_e2e_ms": ms_e2e,
-            "cpu_oracle_ms": cpu_ms, "cpu_threads": threads, "gpu_vs_cpu": cpu_ms / ms,
-            "gpu_e2e_vs_cpu": cpu_ms / ms_e2e}
+    alg = coo_bytes(a.nnz, a.order) + coo_bytes(b.nnz, b.order) + coo_bytes(outs, order)
+    out = {"workload": w["name"], "multiply_adds": prods, "outputs": outs, "gpu_ms": ms, "gpu_e2e_ms": ms_e2e,
+           "roofline": hbm_roofline(alg, ms, "whole contraction")}
+    if cpu:
+        cpu_s = sorted(cpu_port(a, b, w["ctr_a"], w["ctr_b"])[2] for _ in range(5))[2]
+        out.update({"cpu_ms": 1000 * cpu_s, "cpu_threads": os.cpu_count() or 1, "cpu_kind": "port",
+                    "gpu_vs_cpu": 1000 * cpu_s / ms, "gpu_e2e_vs_cpu": 1000 * cpu_s / ms_e2e})
+    return out
 
 
-def run_batched(steps, warmup, stream, local):
+def run_batched(steps, warmup, stream, local, cpu=True):
     """The batched workload: 256 contractions of the readme pattern with
-    uneven sizes. Times, per step, 256 sequential plain contractions and one
-    batched call (fcc_contract_batch) on device-resident operands, and the
-    same pair end to end (pinned host operands in, every output copied back).
-    Returns the JSON sub-object."""
-    import numpy as np
+    uneven sizes. Times, per step, 256 sequential plain contractions (default
+    options, and each with its autotuned options, tuned before timing), one
+    batched call (fcc_contract_batch) with the rule schedule and with the
+    learned schedule, on device-resident operands; then plain and batched end
+    to end (pinned host operands in, every output copied back). Returns the
+    JSON sub-object."""
     import torch
 
     import fastcc_gpu as F
@@ -513,25 +555,17 @@ def run_batched(steps, warmup, stream, local):
     ctx = F.Context(local)
     ctx.set_stream(stream.cuda_stream)
 
-    def plain():
+    def plain(opts_list=None):
         n = p = 0
-        for a, b in dev:
-            r = ctx.contract(a, b, ctr_a, ctr_b)
+        for i, (a, b) in enumerate(dev):
+            r = ctx.contract(a, b, ctr_a, ctr_b, opts_list[i] if opts_list else None)
             n += r.nnz
             p += r.products
             r.free()
         return n, p
 
-    def batched():
-        r, counts = ctx.contract_batch(As, Bs, ctr_a, ctr_b)
-        n, p = r.nnz, r.products
-        r.free()
-        return n, p
-
-    learned_opts = F.Options(schedule=F.SCHED_LEARNED)
-
-    def batched_learned():
-        r, counts = ctx.contract_batch(As, Bs, ctr_a, ctr_b, learned_opts)
+    def batched(opts=None):
+        r, counts = ctx.contract_batch(As, Bs, ctr_a, ctr_b, opts)
         n, p = r.nnz, r.products
         r.free()
         return n, p
@@ -552,9 +586,13 @@ def run_batched(steps, warmup, stream, local):
     ms_plain, (n_plain, prods), l_plain = timed(plain)
     ms_batch, (n_batch, prods_b), l_batch = timed(batched)
     assert n_plain == n_batch and prods == prods_b, "batched and plain results differ in size"
+    # every instance autotuned (fcc_autotune, cached per shape signature) before the timed region
+    tuned = [ctx.autotune(a, b, ctr_a, ctr_b, F.Options(), 1)[0] for a, b in dev]
+    ms_tuned, (n_t, _), _ = timed(lambda: plain(tuned))
+    assert n_t == n_batch, "autotuned plain calls changed the output size"
     ms_learned = None
     if ctx.load_default_model():
-        ms_learned, (n_l, _), _ = timed(batched_learned)
+        ms_learned, (n_l, _), _ = timed(lambda: batched(F.Options(schedule=F.SCHED_LEARNED)))
         assert n_l == n_batch, "learned schedule changed the output size"
         ctx.sched_set_model(None)
 
@@ -594,24 +632,43 @@ def run_batched(steps, warmup, stream, local):
                    for h in host)
     ctx.close()
     count = len(inst)
-    return {
+    alg = sum(coo_bytes(w["a"].nnz, w["a"].order) + coo_bytes(w["b"].nnz, w["b"].order) for w in inst) + \
+        coo_bytes(n_batch, order)
+    out = {
         "workload": "256 contractions a(i,c0,j,c1) x b(k,c0,c1), nnz(a) log-uniform [1e3, 2e6], "
                     "nnz(b) = nnz(a)/2, extents uniform [32, 1024], Zipf s uniform [1.0, 1.5]",
         "contractions": count, "multiply_adds": prods, "outputs": n_batch,
         "plain": {"ms_per_contraction": ms_plain / count, "multiply_adds_per_s": prods / (ms_plain / 1000.0),
                   "launches_per_step": l_plain,
                   "e2e_ms_per_contraction": ms_plain_e2e / count},
+        "plain_autotuned": {"ms_per_contraction": ms_tuned / count,
+                            "multiply_adds_per_s": prods / (ms_tuned / 1000.0),
+                            "options": "fcc_autotune per instance (cached per shape signature), tuned before "
+                                       "the timed region"},
         "batched": {"ms_per_contraction": ms_batch / count, "multiply_adds_per_s": prods / (ms_batch / 1000.0),
                     "launches_per_step": l_batch,
                     "e2e_ms_per_contraction": ms_batch_e2e / count},
         "batched_learned": None if ms_learned is None else {
             "ms_per_contraction": ms_learned / count, "multiply_adds_per_s": prods / (ms_learned / 1000.0),
-            "speedup_vs_plain": ms_plain / ms_learned},
-        "speedup": ms_plain / ms_batch, "e2e_speedup": ms_plain_e2e / ms_batch_e2e,
+            "speedup_vs_plain": ms_plain / ms_learned, "speedup_vs_plain_autotuned": ms_tuned / ms_learned},
+        "speedup": ms_plain / ms_batch, "speedup_vs_plain_autotuned": ms_tuned / ms_batch,
+        "e2e_speedup": ms_plain_e2e / ms_batch_e2e,
         "e2e_h2d_bytes_per_step": in_bytes,
         "e2e_d2h_bytes_per_step": {"plain": n_batch * ((order - 1) * 4 + 8), "batched": n_batch * (order * 4 + 8)},
+        "roofline": hbm_roofline(alg, ms_batch, "one batched call (index, plan, tile kernels)"),
         "steps": steps, "e2e_steps": e2e_steps, "warmup": warmup,
     }
+    if cpu:
+        p = dt = 0
+        for w in inst:
+            pi, _, di = cpu_port(w["a"], w["b"], ctr_a, ctr_b)
+            p += pi
+            dt += di
+        out["cpu_baseline"] = {"value": p / dt, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": f"all 256 instances, one call each ({p} multiply-adds, {dt:.2f} s "
+                                         f"inside the library)"}
+        out["gpu_vs_cpu"] = (prods / (ms_batch / 1000.0)) / (p / dt)
+    return out
 
 
 def main():
@@ -620,6 +677,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nnz", type=int, default=10_000_000,
+                    help="nonzeros of the benchmark operand (10M: the benchmark workload; smaller for tests)")
+    ap.add_argument("--dump-inputs", metavar="PATH", default=None, help=argparse.SUPPRESS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--profile", choices=["zipf3-small", "twomode-small", "readme"],
@@ -638,6 +698,11 @@ def main():
                     help="time the library's radix sort on N seeded uniform keys of BITS bits "
                          "(32-bit payloads; 32-bit keys with 64-bit payloads when BITS <= 32 and N < 0)")
     args = ap.parse_args()
+    if args.dump_inputs:
+        import build_lib
+        build_lib.build_synth()
+        dump_inputs(args.dump_inputs, args.nnz)
+        return
     if args.sort:
         import numpy as np
         import build_lib
@@ -716,7 +781,7 @@ def main():
     import workloads
 
     torch.cuda.set_device(local)
-    w = workloads.zipf3(seed=1)
+    w = workloads.zipf3(seed=1, nnz=args.nnz)
     a = w["a"]
     nnz = a.nnz
     dev_c = torch.from_numpy(a.coords).cuda()
@@ -764,17 +829,13 @@ def main():
     H = F.Tensor(pin_c.numpy(), pin_v.numpy(), a.max_index)
     out_c = torch.empty((out_order, out_nnz), dtype=torch.int32).pin_memory()
     out_v = torch.empty(out_nnz, dtype=torch.float64).pin_memory()
-    e2e_opts = F.Options(timing=1)
     oc, ov = out_c.numpy(), out_v.numpy()
 
-    def e2e_into():  # the tile kernels write the output straight into the pinned host buffers
-        n, _ = ctx.contract_into(H, H, w["ctr_a"], w["ctr_b"], oc, ov, e2e_opts)
-        assert n == out_nnz
-
-    def e2e_copy():  # device result, then one copy to the host
-        r = ctx.contract(H, H, w["ctr_a"], w["ctr_b"], e2e_opts)
-        r.to_numpy_soa(oc, ov)
-        r.free()
+    def e2e_into(waves):  # fcc_contract_into: pinned host operands in, pinned host output
+        def call():
+            n, _ = ctx.contract_into(H, H, w["ctr_a"], w["ctr_b"], oc, ov, F.Options(timing=1, out_waves=waves))
+            assert n == out_nnz
+        return call
 
     def e2e_time(fn):
         fn()
@@ -788,9 +849,9 @@ def main():
         torch.cuda.synchronize()
         return dist_max(e0.elapsed_time(e1) / args.e2e_steps, ws)
 
-    e2e_ms = e2e_time(e2e_into)
+    e2e_ms = e2e_time(e2e_into(0))
     e2e_phases = ctx.timings()
-    e2e_copy_ms = e2e_time(e2e_copy)
+    e2e_waves_ms = e2e_time(e2e_into(12))
     h2d = 2 * (pin_c.numel() * 4 + pin_v.numel() * 8)
     d2h = out_nnz * (4 * out_order + 8)
 
@@ -803,11 +864,11 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "nnz": nnz, "multiply_adds": products, "outputs": out_nnz,
+        "config": {"workload": workload_name(nnz), "nnz": nnz, "multiply_adds": products, "outputs": out_nnz,
                    "l2": "inputs 200 MB and outputs 6.4 GB exceed the 129 MB L2; no flush",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": MEASURED_TRAFFIC,
+                     "frac": achieved / peak, "traffic": MEASURED_TRAFFIC * alg_bytes / 6.695e9,
                      "kernel": "k_contract_dense", "kernel_ms": kms, "algorithmic_bytes": alg_bytes,
                      "peak_kind": peak_kind,
                      "fp64": {"achieved": products / (kms / 1000.0), "peak": fma_peak, "unit": "FMA/s",
@@ -815,31 +876,24 @@ def main():
                               "note": "every multiply-add is one FP64 FMA; peak measured by fcc_diag_fp64_fma_rate"}},
         "e2e": {"value": products * ws / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
-                "path": "fcc_contract_into: pinned host operands in, output produced on the device in waves "
-                        "of tiles and copied to pinned host buffers while later waves compute",
-                "copy_after_ms_per_step": e2e_copy_ms,
+                "path": "fcc_contract_into: pinned host operands in, output computed in device memory, then "
+                        "copied to pinned host buffers",
+                "waves_ms_per_step": e2e_waves_ms,
                 "phases_ms": {k: round(v, 4) for k, v in e2e_phases.items()}},
         "gpu_launches": launches,
         "clocks": clk,
         "phases_ms": {k: round(v, 4) for k, v in phases.items()},
     }
+    cpu = rank == 0 and ws == 1 and not args.no_cpu_baseline
     if not args.no_batched:
-        line["batched"] = run_batched(min(args.steps, 5), 3, stream, local)
-        line["readme"] = run_readme(args.steps, stream, local)
-        line["twomode"] = run_twomode(args.steps, stream, local)
-    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        # bounded sample: grow it (halve `every`) until one run takes >= 8 s
-        every = 256
-        while True:
-            p, dt, _ = time_cpu_oracle(w, every, os.cpu_count() or 1)
-            if dt >= 8.0 or every == 1:
-                break
-            grow = 2
-            while grow < 16 and dt * grow * 2 < 12.0:
-                grow *= 2
-            every = max(1, every // grow)
+        line["batched"] = run_batched(min(args.steps, 5), 3, stream, local, cpu)
+        line["readme"] = run_readme(args.steps, stream, local, cpu)
+        line["twomode"] = run_twomode(args.steps, stream, local, cpu)
+    if cpu:
+        p, _, dt = cpu_port(a, a, w["ctr_a"], w["ctr_b"])
         line["cpu_baseline"] = {"value": p / dt, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-                                "sample": f"left operand rows i % {every} == 0 ({p} multiply-adds, {dt:.1f} s)"}
+                                "sample": f"the whole workload ({p} multiply-adds, {dt:.1f} s inside the library: "
+                                          f"index build, tile loop, output concatenation and decode)"}
     ctx.close()
     if rank == 0:
         print(json.dumps(line))

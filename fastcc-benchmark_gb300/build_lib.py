@@ -4,6 +4,9 @@
   (include/fastcc_gpu.h), compiled for sm_103a only.
 * ``_build/libfastcc_synth.so``: the seeded synthetic-tensor generator
   (include/fastcc_synth.h), host code.
+* ``_build/fcc_benchmark``: the command-line benchmark (host/fcc_benchmark.cpp,
+  the reference's benchmark driver's arguments and report) over the drop-in
+  header, linked against libfastcc_gpu.so.
 
 Translation units compile in parallel; a library is rebuilt only when a source
 is newer than it.
@@ -21,6 +24,8 @@ INCLUDE = os.path.join(ROOT, "include")
 
 GPU_LIB = os.path.join(BUILD, "libfastcc_gpu.so")
 SYNTH_LIB = os.path.join(BUILD, "libfastcc_synth.so")
+CLI = os.path.join(BUILD, "fcc_benchmark")
+HOST = os.path.join(HERE, "host")
 
 CU_SOURCES = ["fcc_prims.cu", "fcc_contract.cu", "fcc_api.cu", "fcc_noalloc.cu", "fcc_diag.cu", "fcc_batch.cu", "fcc_sched.cu"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -84,11 +89,28 @@ def build_synth(verbose=False, force=False):
     return SYNTH_LIB
 
 
+def build_cli(verbose=False, force=False):
+    src = os.path.join(HOST, "fcc_benchmark.cpp")
+    deps = [src, GPU_LIB] + [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".hpp")]
+    if not force and not _stale(CLI, deps):
+        return CLI
+    tmp = CLI + ".tmp"
+    cmd = ["g++", "-std=c++17", "-O2", "-I", HOST, "-I", INCLUDE, src, "-L", BUILD, "-lfastcc_gpu",
+           "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    os.replace(tmp, CLI)
+    return CLI
+
+
 def build_all(verbose=False, force=False):
     with ThreadPoolExecutor(max_workers=2) as ex:
         f1 = ex.submit(build_gpu, verbose, force)
         f2 = ex.submit(build_synth, verbose, force)
-        return f1.result(), f2.result()
+        out = f1.result(), f2.result()
+    build_cli(verbose, force)
+    return out
 
 
 if __name__ == "__main__":

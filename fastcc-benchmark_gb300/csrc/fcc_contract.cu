@@ -796,9 +796,11 @@ __device__ void build_item_plan(const u64 *__restrict__ P, u32 ea, u32 eb, u64 p
 // wait for each other only where a new entry starts. The producer runs up
 // to kStageBufs chunks ahead, so segment loads and entry metadata overlap the
 // accumulation. Every wait, including the consumers' wait between entries,
-// is an mbarrier poll with a bounded count; on timeout the kernel flags
-// ERRB_INTERNAL, stops issuing, waits (bounded) for its copies in flight and
-// skips its remaining work.
+// is an mbarrier poll with a bounded count (DenseArgs::wait_polls); on timeout
+// the kernel flags ERRB_TIMEOUT, stops issuing, waits (at the full limit) for
+// its copies in flight and skips its remaining phase-1 work. With
+// DenseArgs::fault_wait the consumers first wait on `never`, an mbarrier that
+// nothing arrives at: the injected wait that tests make run out.
 constexpr u32 kStageCh = 1824;  // 3 x 608 consumer threads of a 640-thread tile: no partial round
 constexpr u32 kStageBufs = 2;
 constexpr u32 kStageValBytes = (kStageCh + 2) * 8;  // 16-byte multiple: room for a 1-element head
@@ -814,6 +816,7 @@ struct StageHdr {  // one staged chunk (written by the producer before the copie
 
 struct StageCtl {
   unsigned long long full[kStageBufs], empty[kStageBufs];
+  unsigned long long never;  // never completed: the target of an injected wait
   StageHdr hdr[kStageBufs];
   u32 seq;    // chunks staged so far by this CTA (sets buffer and mbarrier parity)
   u32 fail;   // a wait timed out: skip the remaining work
@@ -826,6 +829,7 @@ __device__ __forceinline__ void stage_init(StageCtl &c, u32 consumers) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&c.empty[b])), "r"(consumers)
                    : "memory");
     }
+    mbar_init(&c.never, 1);
     c.seq = 0;
     c.fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -838,7 +842,7 @@ __device__ __forceinline__ void stage_init(StageCtl &c, u32 consumers) {
 template <bool kSentinel>
 __device__ void dense_phase1_staged(const ProdSrc &s, const u32 *__restrict__ colB, u64 p0, u64 p1, u32 LB,
                                     double *acc, u32 *mask, const ItemPlan &pl, unsigned char *stage,
-                                    StageCtl &ctl, u32 *err) {
+                                    StageCtl &ctl, u32 *err, long long polls, u32 fault_wait) {
   const u32 nlong = min(pl.nlong, kListMax);
   const u32 tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const u32 nconsumers = blockDim.x - 32;
@@ -847,11 +851,11 @@ __device__ void dense_phase1_staged(const ProdSrc &s, const u32 *__restrict__ co
     __syncthreads();
     return;
   }
+  u32 issued_last[kStageBufs] = {};  // producer: last chunk copied into each buffer by this item
+  bool issued[kStageBufs] = {};
   if (warp == 0) {
     if (lane == 0) {  // producer
       bool ok = true;
-      u32 issued_last[kStageBufs];
-      bool issued[kStageBufs] = {};
       // entry metadata one entry ahead: its loads overlap this entry's copies
       u32 e = pl.list[0];
       u64 npb = __ldg(&s.P[e]), npe = __ldg(&s.P[e + 1]);
@@ -874,7 +878,7 @@ __device__ void dense_phase1_staged(const ProdSrc &s, const u32 *__restrict__ co
         }
         for (u32 off = 0; off < n; off += kStageCh, seq++) {
           const u32 b = seq % kStageBufs;
-          if (seq >= kStageBufs && !mbar_wait(&ctl.empty[b], ((seq / kStageBufs) - 1) & 1)) {
+          if (seq >= kStageBufs && !mbar_wait(&ctl.empty[b], ((seq / kStageBufs) - 1) & 1, polls)) {
             ok = false;
             break;
           }
@@ -899,20 +903,22 @@ __device__ void dense_phase1_staged(const ProdSrc &s, const u32 *__restrict__ co
           issued_last[b] = seq;
         }
       }
-      if (!ok) {  // stop; let the copies in flight land before the buffers are reused
-        atomicOr(err, ERRB_INTERNAL);
+      if (!ok) {  // stop issuing
+        atomicOr(err, ERRB_TIMEOUT);
         ctl.fail = 1;
-        for (u32 b = 0; b < kStageBufs; b++)
-          if (issued[b]) mbar_wait(&ctl.full[b], (issued_last[b] / kStageBufs) & 1);
       }
       ctl.seq = seq;
     }
   } else {  // consumers
     const u32 ctid = tid - 32;
-    for (;;) {
+    if (fault_wait && !mbar_wait(&ctl.never, 0, polls)) {  // injected: always runs out
+      atomicOr(err, ERRB_TIMEOUT);
+      ctl.fail = 1;
+    }
+    while (!ctl.fail) {
       const u32 b = seq % kStageBufs;
-      if (!mbar_wait(&ctl.full[b], (seq / kStageBufs) & 1)) {
-        atomicOr(err, ERRB_INTERNAL);
+      if (!mbar_wait(&ctl.full[b], (seq / kStageBufs) & 1, polls)) {
+        atomicOr(err, ERRB_TIMEOUT);
         ctl.fail = 1;
         break;
       }
@@ -922,8 +928,8 @@ __device__ void dense_phase1_staged(const ProdSrc &s, const u32 *__restrict__ co
       // a named barrier)
       if (h.first) {
         const u32 pseq = seq - 1, pb = pseq % kStageBufs;
-        if (!mbar_wait(&ctl.empty[pb], (pseq / kStageBufs) & 1)) {
-          atomicOr(err, ERRB_INTERNAL);
+        if (!mbar_wait(&ctl.empty[pb], (pseq / kStageBufs) & 1, polls)) {
+          atomicOr(err, ERRB_TIMEOUT);
           ctl.fail = 1;
           break;
         }
@@ -942,16 +948,23 @@ __device__ void dense_phase1_staged(const ProdSrc &s, const u32 *__restrict__ co
     }
   }
   __syncthreads();
+  // After a failed wait (here or in another role) copies of this item may
+  // still be in flight, unconsumed: the producer lets them land (full limit)
+  // before the CTA can reuse or release the ring.
+  if (ctl.fail && tid == 0)
+    for (u32 b = 0; b < kStageBufs; b++)
+      if (issued[b]) mbar_wait(&ctl.full[b], (issued_last[b] / kStageBufs) & 1);
+  __syncthreads();
 }
 
 template <bool kSentinel, class Add>
 __device__ void dense_item(const ProdSrc &s, const u32 *__restrict__ colB, u32 alo, u32 ahi, u64 p0, u64 p1,
                            u32 ea, u32 eb, u32 LB, double *acc, u32 *mask, ItemPlan &pl, Add &add,
-                           unsigned char *stage, StageCtl &ctl, u32 *err) {
+                           unsigned char *stage, StageCtl &ctl, u32 *err, long long polls, u32 fault_wait) {
   build_item_plan(s.P, ea, eb, p0, p1, 256, pl);
   const u32 tid = threadIdx.x, lane = tid & 31;
   const u32 nlong = stage ? 0u : min(pl.nlong, kListMax);
-  if (stage) dense_phase1_staged<kSentinel>(s, colB, p0, p1, LB, acc, mask, pl, stage, ctl, err);
+  if (stage) dense_phase1_staged<kSentinel>(s, colB, p0, p1, LB, acc, mask, pl, stage, ctl, err, polls, fault_wait);
   for (u32 li = 0; li < nlong; li++) {
     const u32 e = pl.list[li];
     const u64 pb = __ldg(&s.P[e]);
@@ -1018,6 +1031,8 @@ struct DenseArgs {
   u64 *item_cyc;  // per item: SM cycles from fetch to drained (NULL: not recorded)
   u32 stage_off;  // byte offset of phase 1's staging ring in dynamic shared memory; 0: no staging
   u64 *merge_cyc; // per tile: SM cycles of its split-tile merge (NULL: not recorded)
+  long long wait_polls = kWaitPolls;  // poll limit of the staging ring's waits
+  u32 fault_wait = 0;                 // 1: injected wait that runs out (tests)
 };
 
 // The touched mask of positions [32w, 32w+32) of a dense tile, in every lane.
@@ -1238,7 +1253,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
     const u32 t = item.tile;
     const u32 LB = a.tile_lb[t], used = a.tile_nrows[t] * LB;
     dense_item<kSentinel>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, item.ea, item.eb, LB,
-                          acc, mask, plan, add, stage, ctl, a.err);
+                          acc, mask, plan, add, stage, ctl, a.err, a.wait_polls, a.fault_wait);
     __syncthreads();
     if (a.hot) {
       merge_hot_dense<kSentinel>(acc, mask, priv, pmask, a.hot);
@@ -1972,6 +1987,9 @@ void read_scalars(Runtime *ctx, u64 *d_sc) {
   const u32 err = u32(ctx->h_scalars[S_ERR]);
   if (err & ERRB_COORD) throw Error{FCC_ERR_ARG, "a coordinate lies outside [0, max_index]"};
   if (err & ERRB_HASH) throw Error{FCC_ERR_HASH_FULL, "hash accumulator probe limit reached"};
+  if (err & ERRB_TIMEOUT)
+    throw Error{FCC_ERR_TIMEOUT, "a bounded device wait gave up (bulk-copy ring or injected wait); the kernels "
+                                 "stopped after their copies in flight landed"};
   if (err & ERRB_INTERNAL) throw Error{FCC_ERR_CUDA, "internal plan invariant violated"};
 }
 
@@ -2234,6 +2252,8 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (opt.sched_mix_margin < 0 || opt.sched_mix_margin > 1000) throw Error{FCC_ERR_ARG, "bad sched_mix_margin"};
   if (opt.hash_esc < -1 || opt.hash_esc > 2) throw Error{FCC_ERR_ARG, "hash_esc must be -1, 0, 1 or 2"};
   if (opt.out_waves < 0 || opt.out_waves > kMaxWaves) throw Error{FCC_ERR_ARG, "out_waves must be in 0..16"};
+  if (opt.wait_polls < 0) throw Error{FCC_ERR_ARG, "wait_polls must be >= 0"};
+  if (opt.fault_wait != 0 && opt.fault_wait != 1) throw Error{FCC_ERR_ARG, "fault_wait must be 0 or 1"};
   if (opt.esc_group < 0) throw Error{FCC_ERR_ARG, "esc_group must be >= 0"};
   const bool learned = forced < 0 && opt.schedule == FCC_SCHED_LEARNED && ctx->sched && ctx->sched->model;
   const bool want_record = opt.timing == 2 && ctx->sched;
@@ -2596,9 +2616,10 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       stream_out = false;
     }
   }
-  const int waves = !stream_out          ? 1
-                    : opt.out_waves > 0 ? opt.out_waves
-                                        : int(std::min<u64>(kMaxWaves, std::max<u64>(1, (cap * per_out) >> 29)));
+  // One wave (compute, then one copy) unless more are asked for: the copies
+  // of a wave slow the tile kernels running beside them, by a factor that
+  // differs from box to box (measured 1.9x to 6x on the contract phase).
+  const int waves = !stream_out || opt.out_waves <= 0 ? 1 : opt.out_waves;
   for (int attempt = 0;; attempt++) {
     i64 stride = i64(cap);
     if (!caller_out) {
@@ -2629,6 +2650,8 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
                  tile_rank0, tile_lb, tile_nrows, urow, split_of_tile, split_tiles_d, nsplit_d, src,
                  static_cast<const u32 *>(colB), u32(area), u32(words), hot, gacc, gmask, o, dec, ctx->d_err,
                  item_cyc ? item_cyc + cbeg[FCC_CLASS_DENSE] : nullptr, 0u, merge_cyc};
+    if (opt.wait_polls > 0) da.wait_polls = opt.wait_polls;
+    da.fault_wait = opt.fault_wait ? 1u : 0u;
     // Items of class c in wave w: a contiguous slice of the class's items.
     auto wave_items = [&](int c, int w, u32 &lo, u32 &n) {
       lo = u32(u64(ccount[c]) * u64(w) / u64(waves));

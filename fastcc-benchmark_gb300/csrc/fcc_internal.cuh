@@ -28,19 +28,22 @@ enum ErrBits : u32 {
   ERRB_OVERFLOW = 2u,  // output capacity exceeded (host retries with the exact count)
   ERRB_HASH = 4u,      // hash probe limit reached
   ERRB_INTERNAL = 8u,  // an invariant of the plan did not hold
+  ERRB_TIMEOUT = 16u,  // a bounded wait for a bulk copy (or an injected wait) gave up
 };
 
 #ifdef __CUDACC__
 // Bulk asynchronous copies (cp.async.bulk) completed on shared-memory
-// mbarriers. Every wait polls at most kWaitPolls times; a caller whose wait
-// fails flags ERRB_INTERNAL and stops.
+// mbarriers. Every wait polls at most `polls` times (kWaitPolls unless a
+// caller passes a shorter limit); a caller whose wait fails flags
+// ERRB_TIMEOUT, waits (at the full limit) for its own copies in flight and
+// stops.
 constexpr long long kWaitPolls = 1ll << 24;
 
 __device__ __forceinline__ u32 smem_addr(const void *p) { return u32(__cvta_generic_to_shared(p)); }
 
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, u32 parity) {
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, u32 parity, long long polls = kWaitPolls) {
   const u32 a = smem_addr(bar);
-  for (long long it = 0; it < kWaitPolls; it++) {
+  for (long long it = 0; it < polls; it++) {
     u32 done;
     asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
                  : "=r"(done) : "r"(a), "r"(parity) : "memory");

@@ -71,6 +71,16 @@ extern "C" int fcc_contract_noalloc(const fcc_tensor *A, const fcc_tensor *B, co
   *out_nnz = 0;
   if (out_products) *out_products = 0;
   fcc_result res;
+  cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
+  bool launched = false;  // work of this call may be queued on `stream`
+  // An error return also means that no work of this call still runs: wait
+  // for what was queued before the error (its own error, if any, is dropped).
+  auto drain = [&] {
+    if (launched) {
+      cudaStreamSynchronize(stream);
+      cudaGetLastError();
+    }
+  };
   try {
     if (!A || !B) throw Error{FCC_ERR_ARG, "A or B is NULL"};
     if (A->nnz < 0 || B->nnz < 0 || A->nnz + B->nnz > FCC_NOALLOC_MAX_NNZ)
@@ -85,7 +95,7 @@ extern "C" int fcc_contract_noalloc(const fcc_tensor *A, const fcc_tensor *B, co
     arena.init_fixed(d.scratch + kReserved, FCC_NOALLOC_SCRATCH_BYTES - kReserved);
     fcc::u64 host_scalars[32] = {};
     fcc::Runtime rt(arena);
-    rt.stream = static_cast<cudaStream_t>(cuda_stream);
+    rt.stream = stream;
     rt.d_err = reinterpret_cast<fcc::u32 *>(d.scratch);
     rt.h_scalars = host_scalars;
     rt.num_sms = d.num_sms;
@@ -104,15 +114,18 @@ extern "C" int fcc_contract_noalloc(const fcc_tensor *A, const fcc_tensor *B, co
     o.timing = 0;
     o.capacity_hint = 0;
     fcc::i64 products = 0;
+    launched = true;
     fcc::contract(&rt, A, B, ctrA, ctrB, k, o, &res, &products, false, nullptr, 0);
     *out_nnz = res.nnz;
     if (out_products) *out_products = products;
     return FCC_OK;
   } catch (const Error &e) {
+    drain();
     fcc::set_thread_error(e.msg);
     *out_nnz = res.nnz;
     return e.status;
   } catch (...) {
+    drain();
     fcc::set_thread_error("unexpected exception");
     return FCC_ERR_CUDA;
   }

@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const K *__restrict__
     __syncthreads();
   }
   if (S.fail && tid == 0) {
-    atomicOr(err, ERRB_INTERNAL);
+    atomicOr(err, ERRB_TIMEOUT);
     // The current and the next tile's copies may be in flight: wait for them
     // (bounded) before the CTA's shared memory is released.
     const int t = int(blockIdx.x) + it * G;

@@ -55,7 +55,8 @@ class Options(ctypes.Structure):
                 ("hot_columns", ctypes.c_int32), ("schedule", ctypes.c_int32),
                 ("dense_fill_log2", ctypes.c_int32), ("dense_staging", ctypes.c_int32),
                 ("sched_mix_margin", ctypes.c_int32), ("hash_esc", ctypes.c_int32),
-                ("out_waves", ctypes.c_int32), ("esc_group", ctypes.c_int32)]
+                ("out_waves", ctypes.c_int32), ("esc_group", ctypes.c_int32),
+                ("wait_polls", ctypes.c_int32), ("fault_wait", ctypes.c_int32)]
 
     def __init__(self, **kw):
         super().__init__()

@@ -8,7 +8,9 @@
 // ListTensor<DT>, TileAccumulator<DT>, TileAccumulatorMap<DT>; the
 // fastcc_multiply signature and its template arguments; the caller's duty to
 // run _infer_dimensionality() / _infer_shape() first (benchmark.cpp:47-48);
-// ListTensor::compute_nnz_count() and run_through_nnz().
+// ListTensor::compute_nnz_count() and run_through_nnz();
+// fastcc_multiply_timing (contract.hpp:670-822) with its five microsecond
+// figures, so the reference's benchmark.cpp compiles against this header.
 // Different: ListTensor owns its entries and exposes them (size, coords,
 // value); output coordinates are decoded correctly; errors throw fcc::Error.
 // Compute is FP64 whatever DT and RES are (values are converted).
@@ -17,6 +19,7 @@
 
 #include <cstdint>
 #include <initializer_list>
+#include <iostream>
 #include <memory>
 #include <mutex>
 #include <random>
@@ -219,6 +222,49 @@ template <class DT> class Tensor {
   ListTensor<RES> fastcc_multiply(Tensor<RIGHT> &other, CoOrdinate left_contr, CoOrdinate right_contr,
                                   int tile_size = 100) {
     static_assert(std::is_floating_point<RES>::value, "RES must be float or double");
+    ListTensor<RES> out;
+    run_contraction(other, left_contr, right_contr, tile_size, 0, [&](fcc_result *r) { out.take(r); });
+    return out;
+  }
+
+  // The reference's instrumented twin (contract.hpp:670-822): runs the same
+  // contraction, discards the result and returns, in microseconds,
+  //   [0] index build            (the reference's TileIndexedTensor pair; here
+  //                               upload + linearise + sort + segments + lookup)
+  //   [1] compute                (its tile-pair loop with drain; here the tile
+  //                               plan, the tile kernels and the split-tile merge)
+  //   [2] drain                  (its separate re-drain pass; here the merge
+  //                               drain of tiles cut into several work items)
+  //   [3] compute - drain - indexing
+  //   [4] indexing               (its join replayed without arithmetic; here the
+  //                               planning of tiles and work items)
+  // measured with CUDA events on the device. Prints "Got <n> nonzeros" as the
+  // reference does.
+  template <class AccType, class RES, class RIGHT>
+  std::vector<long long> fastcc_multiply_timing(Tensor<RIGHT> &other, CoOrdinate left_contr,
+                                                CoOrdinate right_contr, int tile_size = 100) {
+    static_assert(std::is_floating_point<RES>::value, "RES must be float or double");
+    double ms[FCC_NUM_PHASES] = {};
+    int64_t n = 0;
+    run_contraction(other, left_contr, right_contr, tile_size, 1, [&](fcc_result *r) {
+      fcc_result_info(r, nullptr, &n, nullptr);
+      fcc_last_timings(fcc::default_context(), ms, FCC_NUM_PHASES);
+    });
+    std::cout << "Got " << n << " nonzeros" << std::endl;
+    auto us = [](double m) { return static_cast<long long>(m * 1000.0 + 0.5); };
+    const long long index = us(ms[FCC_PHASE_UPLOAD] + ms[FCC_PHASE_INDEX]);
+    const long long indexing = us(ms[FCC_PHASE_PLAN]);
+    const long long drain = us(ms[FCC_PHASE_MERGE]);
+    const long long compute = indexing + us(ms[FCC_PHASE_CONTRACT]) + drain;
+    return {index, compute, drain, compute - drain - indexing, indexing};
+  }
+
+ private:
+  // Packs both operands (AoS, FP64), runs fcc_contract on the process's
+  // context and hands the device result to `take` before freeing it.
+  template <class RIGHT, class Take>
+  void run_contraction(Tensor<RIGHT> &other, CoOrdinate &left_contr, CoOrdinate &right_contr, int tile_size,
+                       int timing, Take take) {
     if (left_contr.get_dimensionality() != right_contr.get_dimensionality())
       throw fcc::Error(FCC_ERR_ARG, "contracted mode lists differ in length");
     std::vector<int32_t> ca(left_contr.begin(), left_contr.end()), cb(right_contr.begin(), right_contr.end());
@@ -246,20 +292,19 @@ template <class DT> class Tensor {
     fcc_options o;
     fcc_options_default(&o);
     o.tile_size = tile_size;
+    o.timing = timing;
     std::lock_guard<std::mutex> lock(fcc::context_mutex());
     fcc_ctx *ctx = fcc::default_context();
     fcc_result *r = nullptr;
     int st = fcc_contract(ctx, &A, &B, ca.data(), cb.data(), int32_t(ca.size()), &o, &r);
     if (st != FCC_OK) throw fcc::Error(st, std::string("fcc_contract: ") + fcc_last_error(ctx));
-    ListTensor<RES> out(dA + dB - 2 * int(ca.size()));
     try {
-      out.take(r);
+      take(r);
     } catch (...) {
       fcc_result_free(r);
       throw;
     }
     fcc_result_free(r);
-    return out;
   }
 };
 

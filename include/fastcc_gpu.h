@@ -36,7 +36,7 @@ extern "C" {
 #endif
 
 #define FCC_MAX_ORDER 8
-#define FCC_ABI_VERSION 3
+#define FCC_ABI_VERSION 4
 
 typedef enum fcc_status {
   FCC_OK = 0,
@@ -121,10 +121,21 @@ typedef struct fcc_options {
   int32_t out_waves;          /* fcc_contract_into with pinned host output buffers: the output is
                                  produced in device memory in this many waves of tiles (1..16),
                                  each wave's outputs copied to the host while the next computes.
-                                 0 (default): one wave per 512 MB of output capacity */
+                                 0 (default): one wave, i.e. the whole output computed, then
+                                 copied once */
   int32_t esc_group;          /* expanded hash tiles are sorted in groups whose keys fit 32 bits;
                                  0 (default): as many tiles per group as that allows; > 0: at
                                  most this many */
+  int32_t wait_polls;         /* poll limit of the dense tiles' waits on their staging ring
+                                 (consumers waiting for a chunk, the producer waiting for a free
+                                 buffer); a wait that runs out ends the call with
+                                 FCC_ERR_TIMEOUT. 0 (default): 2^24. The final wait for a CTA's
+                                 own copies in flight always uses 2^24 */
+  int32_t fault_wait;         /* fault injection for tests: 1 makes the consumer warps of every
+                                 staged dense item first wait on an mbarrier that nothing
+                                 completes, so that the wait runs out after wait_polls polls and
+                                 the call returns FCC_ERR_TIMEOUT; the context stays usable.
+                                 0 (default): off */
 } fcc_options;
 
 /* Tile classes: every output tile runs in one of them. The hash classes

@@ -228,16 +228,9 @@ void build_index(const orc_tensor *t, const Operand &op, u64 T, TileIndex &ix) {
   ix.ent_beg[K] = n;
 }
 
-template <class T> T *dup_vec(const std::vector<T> &v) {
-  T *p = (T *)std::malloc(sizeof(T) * (v.size() ? v.size() : 1));
-  if (!v.empty()) std::memcpy(p, v.data(), sizeof(T) * v.size());
-  return p;
-}
-
-void decode_into(const Operand &a, const Operand &b, const std::vector<u64> &left,
-                 const std::vector<u64> &right, int32_t *coords) {
+void decode_into(const Operand &a, const Operand &b, const u64 *left, const u64 *right, int64_t n,
+                 int32_t *coords) {
   const int la = int(a.ext.size()), lb = int(b.ext.size()), d = la + lb;
-  const int64_t n = int64_t(left.size());
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; i++) {
     u64 l = left[i], r = right[i];
@@ -343,22 +336,39 @@ extern "C" int orc_fastcc_multiply(const orc_tensor *A, const orc_tensor *B, con
   }
   out->compute_ms = ms_since(t1);
 
-  std::vector<u64> left, right;
-  std::vector<double> val, absv;
-  for (auto &L : loc) {
-    left.insert(left.end(), L.left.begin(), L.left.end());
-    right.insert(right.end(), L.right.begin(), L.right.end());
-    val.insert(val.end(), L.val.begin(), L.val.end());
-    absv.insert(absv.end(), L.absv.begin(), L.absv.end());
-    out->products += L.products;
+  // Concatenate the per-thread outputs (ListTensor::concatenate,
+  // contract.hpp:906-909) straight into the result arrays, each thread
+  // copying its own range.
+  std::vector<int64_t> off(loc.size() + 1, 0);
+  for (size_t q = 0; q < loc.size(); q++) {
+    off[q + 1] = off[q] + int64_t(loc[q].val.size());
+    out->products += loc[q].products;
   }
-  out->nnz = int64_t(val.size());
-  out->left = dup_vec(left);
-  out->right = dup_vec(right);
-  out->values = dup_vec(val);
-  out->abs_sum = want_abs ? dup_vec(absv) : nullptr;
-  out->coords = (int32_t *)std::malloc(sizeof(int32_t) * std::max<int64_t>(1, out->nnz * out->order));
-  decode_into(oa, ob, left, right, out->coords);
+  const int64_t n = off.back();
+  out->nnz = n;
+  const size_t cap = size_t(std::max<int64_t>(n, 1));
+  out->left = (u64 *)std::malloc(sizeof(u64) * cap);
+  out->right = (u64 *)std::malloc(sizeof(u64) * cap);
+  out->values = (double *)std::malloc(sizeof(double) * cap);
+  out->abs_sum = want_abs ? (double *)std::malloc(sizeof(double) * cap) : nullptr;
+  out->coords = (int32_t *)std::malloc(sizeof(int32_t) * std::max<int64_t>(1, n * out->order));
+#pragma omp parallel for schedule(static, 1)
+  for (int64_t q = 0; q < int64_t(loc.size()); q++) {
+    Local &L = loc[q];
+    const size_t m = L.val.size();
+    if (m) {
+      std::memcpy(out->left + off[q], L.left.data(), m * sizeof(u64));
+      std::memcpy(out->right + off[q], L.right.data(), m * sizeof(u64));
+      std::memcpy(out->values + off[q], L.val.data(), m * sizeof(double));
+      if (want_abs) std::memcpy(out->abs_sum + off[q], L.absv.data(), m * sizeof(double));
+    }
+    std::vector<u64>().swap(L.left);
+    std::vector<u64>().swap(L.right);
+    std::vector<double>().swap(L.val);
+    std::vector<double>().swap(L.absv);
+  }
+  decode_into(oa, ob, out->left, out->right, n, out->coords);
+  out->total_ms = ms_since(t0);
 #ifdef _OPENMP
   omp_set_num_threads(saved);
 #endif

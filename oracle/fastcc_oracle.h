@@ -35,6 +35,8 @@ typedef struct orc_result {
   int64_t products; /* multiply-adds performed */
   double index_ms;  /* tile index build (contract.hpp:854-862) */
   double compute_ms;/* tile-pair loop incl. drain (contract.hpp:876-904) */
+  double total_ms;  /* the whole call: index, tile-pair loop, concatenation of the
+                       per-thread outputs and their coordinate decode */
 } orc_result;
 
 /* Max index per mode, as Tensor::_infer_shape (contract.hpp:124-144). */

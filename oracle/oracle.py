@@ -17,6 +17,19 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def reference_sources():
+    """Directory of the reference's sources (contract.hpp, benchmark.cpp, ...):
+    $FASTCC_REFERENCE, else the read-only checkout this build was made
+    against. Absent on machines that only run the tests."""
+    return os.environ.get("FASTCC_REFERENCE", "/root/reference")
+
+
+def reference_present():
+    return os.path.exists(os.path.join(reference_sources(), "contract.hpp"))
+
+
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libfastcc_ref.so")
 
@@ -35,12 +48,13 @@ class _Result(ctypes.Structure):
                 ("values", ctypes.POINTER(ctypes.c_double)),
                 ("abs_sum", ctypes.POINTER(ctypes.c_double)),
                 ("products", ctypes.c_int64),
-                ("index_ms", ctypes.c_double), ("compute_ms", ctypes.c_double)]
+                ("index_ms", ctypes.c_double), ("compute_ms", ctypes.c_double),
+                ("total_ms", ctypes.c_double)]
 
 
 def build(ref=False):
     """Compile liboracle.so (and the reference harness when ref=True)."""
-    subprocess.check_call(["make", "-s", "-C", HERE] + (["ref"] if ref else ["all"]))
+    subprocess.check_call(["make", "-s", "-C", HERE] + (["ref", f"REF={reference_sources()}"] if ref else ["all"]))
 
 
 _lib = None
@@ -96,27 +110,32 @@ def infer_shape(coords):
     return coords.max(axis=0).astype(np.int32)
 
 
-def _take(res, want_abs):
+def _take(res, want_abs, keep=True):
     n, d = res.nnz, res.order
     out = {
         "order": d,
+        "nnz": n,
         "products": res.products,
         "index_ms": res.index_ms,
         "compute_ms": res.compute_ms,
-        "left": np.ctypeslib.as_array(res.left, (max(n, 1),))[:n].copy(),
-        "right": np.ctypeslib.as_array(res.right, (max(n, 1),))[:n].copy(),
-        "values": np.ctypeslib.as_array(res.values, (max(n, 1),))[:n].copy(),
-        "coords": np.ctypeslib.as_array(res.coords, (max(n * d, 1),))[: n * d].reshape(n, d).copy(),
+        "total_ms": res.total_ms,
     }
-    if want_abs:
-        out["abs_sum"] = np.ctypeslib.as_array(res.abs_sum, (max(n, 1),))[:n].copy()
+    if keep:
+        out["left"] = np.ctypeslib.as_array(res.left, (max(n, 1),))[:n].copy()
+        out["right"] = np.ctypeslib.as_array(res.right, (max(n, 1),))[:n].copy()
+        out["values"] = np.ctypeslib.as_array(res.values, (max(n, 1),))[:n].copy()
+        out["coords"] = np.ctypeslib.as_array(res.coords, (max(n * d, 1),))[: n * d].reshape(n, d).copy()
+        if want_abs:
+            out["abs_sum"] = np.ctypeslib.as_array(res.abs_sum, (max(n, 1),))[:n].copy()
     lib().orc_free(ctypes.byref(res))
     return out
 
 
 def fastcc_multiply(a_coords, a_vals, a_max, b_coords, b_vals, b_max, ctr_a, ctr_b,
-                    tile_size=100, nthreads=0, want_abs=False):
-    """The restatement; returns dict of numpy arrays (unsorted, reference order)."""
+                    tile_size=100, nthreads=0, want_abs=False, keep=True):
+    """The restatement; returns dict of numpy arrays (unsorted, reference order).
+    keep=False returns only the counts and the in-library times (index_ms,
+    compute_ms, total_ms) and drops the entries."""
     ka, kb = _Keep(a_coords, a_vals, a_max), _Keep(b_coords, b_vals, b_max)
     ca = np.ascontiguousarray(ctr_a, np.int32)
     cb = np.ascontiguousarray(ctr_b, np.int32)
@@ -127,7 +146,7 @@ def fastcc_multiply(a_coords, a_vals, a_max, b_coords, b_vals, b_max, ctr_a, ctr
                                    ctypes.byref(res))
     if rc != 0:
         raise ValueError("oracle rejected the arguments")
-    return _take(res, want_abs)
+    return _take(res, want_abs, keep)
 
 
 def bruteforce(a_coords, a_vals, a_max, b_coords, b_vals, b_max, ctr_a, ctr_b):

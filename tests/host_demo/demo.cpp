@@ -44,6 +44,11 @@ int main(int argc, char **argv) {
       ListTensor<double> r2 = a.fastcc_multiply<TileAccumulatorMap<double>, double>(b, {1, 3}, {1, 2});
       if (r2.compute_nnz_count() != r.compute_nnz_count()) return 3;
     }
+    // the instrumented twin: five non-negative microsecond figures, [3] the
+    // rest of [1] after [2] and [4]
+    std::vector<long long> t = a.fastcc_multiply_timing<TileAccumulator<double>, double>(
+        b, CoOrdinate(modes(argv[3])), CoOrdinate(modes(argv[4])));
+    if (t.size() != 5 || t[0] < 0 || t[1] < 0 || t[2] < 0 || t[4] < 0 || t[3] != t[1] - t[2] - t[4]) return 5;
   } catch (const fcc::Error &e) {
     std::fprintf(stderr, "fcc error %d: %s\n", e.status, e.what());
     return 2;

@@ -37,12 +37,12 @@ def test_synth_library_exports_every_declared_symbol():
 
 def test_library_loads_and_reports_status_strings():
     L = F.lib()
-    assert L.fcc_abi_version() == 3
+    assert L.fcc_abi_version() == 4
     assert L.fcc_status_string(0) == b"ok"
     assert L.fcc_status_string(3) == b"hash accumulator full"
     o = F.Options()
     assert L.fcc_options_default(ctypes.byref(o)) == 0 and o.tile_size == 100
-    assert ctypes.sizeof(F.Options) == 88
+    assert ctypes.sizeof(F.Options) == 96
 
 
 def test_bad_arguments_return_status_not_crash():

@@ -1,23 +1,30 @@
-"""GPU checks at the benchmark sizes, through size-independent properties.
+"""GPU parity at the benchmark sizes, against the oracle in full.
 
-The oracle cannot contract these workloads in seconds, so each full-size
-result is checked by properties that O(nnz) host arithmetic can verify:
-  * linearity: sum over outputs of v*w[row]*u[col] equals
-    sum_c (sum_{a in c} va*w[row_a]) * (sum_{b in c} vb*u[col_b]) for random
-    weights w, u (a Freivalds-style checksum of the whole product);
-  * row sums: sum_col C[row, col] = sum_{a in row} va * sB(key_a);
-  * exact rows: a handful of rows, the heaviest included, recomputed exactly
-    on the host and compared coordinate by coordinate (1e-12 * S);
-  * structure: coordinates inside the extents and no duplicate outputs.
+The workloads are the ones bench.py times, with the same seeds:
+  * zipf3: A 20,000 x 20,000 x 500,000, 10M nonzeros, A x A over {1,2}
+    (4.36e9 multiply-adds, 3.9e8 outputs);
+  * twomode: A 5,000 x 5,000 x 2,000 x 50, 5M nonzeros, A x A over {0,2}
+    (4.2e8 multiply-adds, 2.0e8 outputs);
+  * batched: the 256-instance batch of the readme pattern, one
+    fcc_contract_batch call, every instance against the oracle alone.
+
+Each output is identified by its linearised (A external, B external) pair,
+the oracle's (left, right) (contract.hpp:876-909 with the drain decode fixed).
+Both sides are sorted by that key on the device and compared whole: equal
+output counts, equal key arrays (the coordinate sets bit for bit) and every
+value within 1e-12 * S, S the oracle's sum of |a*b| for that output
+(tests/helpers.py states the bar).
 """
 import numpy as np
 import pytest
 
 import fastcc_gpu as F
+import oracle
 import workloads
-from helpers import check_parity
 
 pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
 
 
 class _Dev:
@@ -28,121 +35,131 @@ class _Dev:
                                          "version": 3, "strides": None}
 
 
-def _lin(coords, modes, radix):
-    out = np.zeros(coords.shape[0], np.int64)
-    for m in modes:
-        out = out * np.int64(radix[m]) + coords[:, m].astype(np.int64)
+def _radices(t, ctr):
+    return [int(t.max_index[m]) + 1 for m in range(t.order) if m not in ctr]
+
+
+def _device_columns(r):
+    import torch
+    cptr, stride, vptr = r.device_pointers()
+    n = r.nnz
+    vals = torch.as_tensor(_Dev(vptr, n, "<f8"), device="cuda")
+    cols = [torch.as_tensor(_Dev(cptr + 4 * m * stride, n, "<i4"), device="cuda") for m in range(r.order)]
+    return cols, vals
+
+
+def _horner(cols, radices):
+    import torch
+    out = torch.zeros(cols[0].numel() if cols else 0, dtype=torch.int64, device="cuda")
+    for c, rad in zip(cols, radices):
+        out = out * rad + c.long()
     return out
 
 
-def _host_model(w):
+def _compare(key_g, val_g, o, LB):
+    """Sorted-key comparison of a device result (key_g, val_g) with an oracle
+    result o (left, right, values, abs_sum). Returns (outputs, cancellation
+    cases)."""
+    import torch
+    left = torch.from_numpy(o["left"].view(np.int64)).cuda()
+    right = torch.from_numpy(o["right"].view(np.int64)).cuda()
+    key_o = left * LB + right
+    del left, right
+    assert key_g.numel() == key_o.numel(), f"output count {key_g.numel()} != oracle {key_o.numel()}"
+    kg, ig = torch.sort(key_g)
+    ko, io = torch.sort(key_o)
+    del key_o
+    assert torch.equal(kg, ko), "output coordinate sets differ"
+    if kg.numel() > 1:
+        assert bool((kg[1:] != kg[:-1]).all()), "duplicate output coordinates"
+    del kg, ko
+    vg = val_g[ig]
+    vo = torch.from_numpy(o["values"]).cuda()[io]
+    so = torch.from_numpy(o["abs_sum"]).cuda()[io]
+    err = (vg - vo).abs()
+    bad = err > RTOL * torch.maximum(vo.abs(), so)
+    nbad = int(bad.sum())
+    assert nbad == 0, f"{nbad} values exceed 1e-12*S; worst {float(err[bad].max()):.3e}"
+    canc = int((err > RTOL * vo.abs()).sum())
+    return int(vg.numel()), canc
+
+
+def _oracle(w):
     a, b = w["a"], w["b"]
-    ra, rb = a.max_index.astype(np.int64) + 1, b.max_index.astype(np.int64) + 1
-    ea = [m for m in range(a.order) if m not in w["ctr_a"]]
-    eb = [m for m in range(b.order) if m not in w["ctr_b"]]
-    rowA = _lin(a.coords, ea, ra)
-    keyA = _lin(a.coords, w["ctr_a"], ra)
-    colB = _lin(b.coords, eb, rb)
-    keyB = _lin(b.coords, w["ctr_b"], rb)
-    LA = int(np.prod(ra[ea])) if ea else 1
-    LB = int(np.prod(rb[eb])) if eb else 1
-    return dict(rowA=rowA, keyA=keyA, colB=colB, keyB=keyB, LA=LA, LB=LB, ea=ea, eb=eb, ra=ra, rb=rb)
+    return oracle.fastcc_multiply(a.coords, a.values, a.max_index, b.coords, b.values, b.max_index,
+                                  w["ctr_a"], w["ctr_b"], tile_size=128, want_abs=True)
 
 
-def _key_sums(keys, vals, ukeys):
-    idx = np.searchsorted(ukeys, keys)
-    ok = (idx < ukeys.size) & (ukeys[np.minimum(idx, ukeys.size - 1)] == keys)
-    s = np.zeros(ukeys.size)
-    np.add.at(s, idx[ok], vals[ok])
-    return s
+def _device_tensor(t):
+    import torch
+    return F.Tensor(torch.from_numpy(t.coords).cuda(), torch.from_numpy(t.values).cuda(), t.max_index)
 
 
-def _check_workload(ctx, w, sample_rows):
+def _check_single(ctx, w, opts=None):
     import torch
     a, b = w["a"], w["b"]
-    h = _host_model(w)
-    r = ctx.contract(a, b, w["ctr_a"], w["ctr_b"])
+    A = _device_tensor(a)
+    B = A if b is a else _device_tensor(b)
+    r = ctx.contract(A, B, w["ctr_a"], w["ctr_b"], opts)
     try:
-        n, order = r.nnz, r.order
-        cptr, stride, vptr = r.device_pointers()
-        vals = torch.as_tensor(_Dev(vptr, n, "<f8"), device="cuda")
-        cols = [torch.as_tensor(_Dev(cptr + 4 * m * stride, n, "<i4"), device="cuda").long()
-                for m in range(order)]
-        na = len(h["ea"])
-        ext_r = [int(h["ra"][m]) for m in h["ea"]] + [int(h["rb"][m]) for m in h["eb"]]
-        for m in range(order):
-            assert int(cols[m].min()) >= 0 and int(cols[m].max()) < ext_r[m]
-        row = torch.zeros(n, dtype=torch.long, device="cuda")
-        for m in range(na):
-            row = row * ext_r[m] + cols[m]
-        col = torch.zeros(n, dtype=torch.long, device="cuda")
-        for m in range(na, order):
-            col = col * ext_r[m] + cols[m]
-        # structure: no duplicate (row, col)
-        lin = row * h["LB"] + col
-        assert torch.unique(lin).numel() == n
-        del lin
-        # linearity checksum with random weights
-        rng = np.random.Generator(np.random.PCG64(2024))
-        wr = rng.uniform(-1, 1, h["LA"])
-        uc = rng.uniform(-1, 1, h["LB"])
-        ukeys = np.unique(np.concatenate([h["keyA"], h["keyB"]]))
-        sa = _key_sums(h["keyA"], a.values * wr[h["rowA"]], ukeys)
-        sb = _key_sums(h["keyB"], b.values * uc[h["colB"]], ukeys)
-        want = float(np.dot(sa, sb))
-        sa_abs = _key_sums(h["keyA"], np.abs(a.values * wr[h["rowA"]]), ukeys)
-        sb_abs = _key_sums(h["keyB"], np.abs(b.values * uc[h["colB"]]), ukeys)
-        scale = float(np.dot(sa_abs, sb_abs))
-        wr_t = torch.from_numpy(wr).cuda()
-        uc_t = torch.from_numpy(uc).cuda()
-        got = float((vals * wr_t[row] * uc_t[col]).sum())
-        assert abs(got - want) <= 1e-10 * scale, (got, want, scale)
-        # row sums
-        sB = _key_sums(h["keyB"], b.values, ukeys)
-        sB_abs = _key_sums(h["keyB"], np.abs(b.values), ukeys)
-        kidx = np.searchsorted(ukeys, h["keyA"])
-        rs_want = np.zeros(h["LA"])
-        rs_abs = np.zeros(h["LA"])
-        np.add.at(rs_want, h["rowA"], a.values * sB[kidx])
-        np.add.at(rs_abs, h["rowA"], np.abs(a.values) * sB_abs[kidx])
-        rs_got = torch.zeros(h["LA"], dtype=torch.float64, device="cuda").index_add_(0, row, vals).cpu().numpy()
-        assert np.all(np.abs(rs_got - rs_want) <= 1e-11 * rs_abs + 1e-300)
-        # exact rows
-        orderB = np.argsort(h["keyB"], kind="stable")
-        kB = h["keyB"][orderB]
-        for rr in sample_rows:
-            sel = np.nonzero(h["rowA"] == rr)[0]
-            if sel.size == 0:
-                continue
-            lo = np.searchsorted(kB, h["keyA"][sel], side="left")
-            hi = np.searchsorted(kB, h["keyA"][sel], side="right")
-            cnt = hi - lo
-            tot = int(cnt.sum())
-            rep = np.repeat(np.arange(sel.size), cnt)
-            offs = np.arange(tot) - np.repeat(np.cumsum(cnt) - cnt, cnt)
-            bidx = orderB[np.repeat(lo, cnt) + offs]
-            prods = a.values[sel][rep] * b.values[bidx]
-            ucol, inv = np.unique(h["colB"][bidx], return_inverse=True)
-            wv = np.zeros(ucol.size)
-            ws = np.zeros(ucol.size)
-            np.add.at(wv, inv, prods)
-            np.add.at(ws, inv, np.abs(prods))
-            m = (row == rr).nonzero().flatten()
-            gc = col[m].cpu().numpy()
-            gv = vals[m].cpu().numpy()
-            check_parity(gc[:, None], gv, ucol[:, None], wv, ws)
-        return n, r.products
+        ra, rb = _radices(a, w["ctr_a"]), _radices(b, w["ctr_b"])
+        cols, vals = _device_columns(r)
+        LB = int(np.prod(rb))
+        key = _horner(cols[:len(ra)], ra) * LB + _horner(cols[len(ra):], rb)
+        vals = vals.clone()
+        products = r.products
     finally:
         r.free()
+    del A, B
+    torch.cuda.synchronize()
+    o = _oracle(w)
+    assert products == o["products"]
+    n, canc = _compare(key, vals, o, LB)
+    return n, products, canc
 
 
-def test_zipf3_full_size(ctx):
-    w = workloads.zipf3(seed=1)
-    n, p = _check_workload(ctx, w, sample_rows=[0, 1, 2, 17, 1000, 19999])
-    assert p > 4e9 and n > 1e8
+def test_zipf3_full_size_matches_oracle(ctx):
+    n, p, canc = _check_single(ctx, workloads.zipf3(seed=1))
+    assert p == 4_362_229_740 and n == 393_466_340
+    print(f"zipf3: {n} outputs, {p} multiply-adds, {canc} cancellation cases")
 
 
-def test_twomode_full_size(ctx):
-    w = workloads.twomode(seed=1)
-    n, p = _check_workload(ctx, w, sample_rows=[0, 1, 50, 4999 * 50 + 49, 123456])
-    assert p > 1e8
+def test_twomode_full_size_matches_oracle(ctx):
+    n, p, canc = _check_single(ctx, workloads.twomode(seed=1))
+    assert p == 415_279_252 and n == 199_932_409
+    print(f"twomode: {n} outputs, {p} multiply-adds, {canc} cancellation cases")
+
+
+def test_batched_benchmark_batch_matches_oracle(ctx):
+    """The 256-instance batch that bench.py times, in one fcc_contract_batch
+    call, every instance against the oracle run on that instance alone."""
+    import torch
+    inst = workloads.batched(seed=1, count=256)
+    As = [_device_tensor(x["a"]) for x in inst]
+    Bs = [_device_tensor(x["b"]) for x in inst]
+    ctr_a, ctr_b = inst[0]["ctr_a"], inst[0]["ctr_b"]
+    r, counts = ctx.contract_batch(As, Bs, ctr_a, ctr_b)
+    total_out = total_prod = 0
+    try:
+        cols, vals = _device_columns(r)
+        inst_col = cols[0]
+        assert int(counts.sum()) == r.nnz
+        for t, x in enumerate(inst):
+            ra, rb = _radices(x["a"], ctr_a), _radices(x["b"], ctr_b)
+            LB = int(np.prod(rb))
+            sel = (inst_col == t).nonzero().flatten()
+            assert sel.numel() == int(counts[t]), f"instance {t}: count {int(counts[t])} != {sel.numel()}"
+            sub = [c[sel] for c in cols[1:]]
+            key = _horner(sub[:len(ra)], ra) * LB + _horner(sub[len(ra):], rb)
+            o = _oracle(x)
+            n, _ = _compare(key, vals[sel], o, LB)
+            total_out += n
+            total_prod += o["products"]
+            del sub, key, sel, o
+        assert r.products == total_prod
+        assert total_out == r.nnz
+    finally:
+        r.free()
+    del As, Bs
+    torch.cuda.synchronize()
+    print(f"batched: 256 instances, {total_out} outputs, {total_prod} multiply-adds")

@@ -31,6 +31,49 @@ def test_header_compiles_and_links():
     assert os.path.exists(DEMO)
 
 
+@pytest.mark.skipif(not oracle.reference_present(), reason="the reference's sources are not on this machine")
+def test_reference_benchmark_compiles_unmodified_against_the_dropin(tmp_path):
+    """The reference's own driver (benchmark.cpp: fastcc_multiply_timing and
+    fastcc_multiply over TileAccumulator / TileAccumulatorMap) compiles and
+    links against host/contract.hpp, read.hpp and libfastcc_gpu.so. The source
+    is fed on standard input from an empty directory, so that its quoted
+    includes resolve to the drop-in headers, not to the reference's."""
+    src = os.path.join(oracle.reference_sources(), "benchmark.cpp")
+    lib_dir = os.path.join(PKG, "_build")
+    exe = tmp_path / "benchmark"
+    with open(src) as f:
+        subprocess.check_call(["g++", "-std=c++17", "-O1", "-x", "c++", "-I", os.path.join(PKG, "host"), "-I",
+                               os.path.join(ROOT, "include"), "-", "-L", lib_dir, "-lfastcc_gpu",
+                               f"-Wl,-rpath,{lib_dir}", "-o", str(exe)], stdin=f, cwd=tmp_path)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 1 and "Usage" in out.stdout
+
+
+@pytest.mark.gpu
+def test_benchmark_cli_self_contraction_matches_oracle(tmp_path):
+    """fcc_benchmark (host/fcc_benchmark.cpp, the reference driver's
+    arguments and report) on a .tns self-contraction: every run reports the
+    oracle's output count and the six medians are printed."""
+    import build_lib
+    cli = build_lib.build_cli()
+    rng = np.random.Generator(np.random.PCG64(5))
+    dims = [40, 12, 30]
+    lin = rng.choice(int(np.prod(dims)), size=2000, replace=False)
+    c = np.stack(np.unravel_index(lin, dims), axis=1).astype(np.int32)
+    v = rng.uniform(-1, 1, 2000)
+    _write_tns(tmp_path / "t.tns", c, v, dims)
+    o = oracle.fastcc_multiply(c, v, oracle.infer_shape(c), c, v, oracle.infer_shape(c), [1, 2], [1, 2])
+    for dense in ("0", "1"):
+        out = subprocess.run([cli, str(tmp_path / "t.tns"), "1,2", "64", dense], capture_output=True, text=True,
+                             timeout=300)
+        assert out.returncode == 0, out.stderr
+        runs = [l for l in out.stdout.splitlines() if l.startswith("run ")]
+        assert len(runs) == 3 and all(l.endswith(f": {len(o['values'])} nonzeros") for l in runs), out.stdout
+        assert out.stdout.count(f"Got {len(o['values'])} nonzeros") == 3
+        for name in ("Index build", "Compute", "Drain", "Accumulate", "Indexing", "Total"):
+            assert f"{name} time: " in out.stdout
+
+
 def _write_tns(path, coords, vals, dims):
     with open(path, "w") as f:
         f.write(" ".join(str(d) for d in dims) + "\n")  # header line (skipped: has_header)
