@@ -75,7 +75,7 @@ void set_thread_error(const std::string &msg) { g_last_error = msg; }
 
 extern "C" {
 
-static_assert(sizeof(fcc_options) == 96, "fcc_options layout is part of the ABI");
+static_assert(sizeof(fcc_options) == 104, "fcc_options layout is part of the ABI");
 
 int fcc_abi_version(void) { return FCC_ABI_VERSION; }
 

@@ -1007,6 +1007,122 @@ __device__ void dense_item(const ProdSrc &s, const u32 *__restrict__ colB, u32 a
   }
 }
 
+// ---- dense items, flat ----
+//
+// The item's multiply-adds [p0, p1) are numbered by the prefix P over its A
+// entries; warps pull chunks of consecutive numbers and give each lane one
+// multiply-add per round, kBatch rounds at a time (their loads in flight
+// together). The A entries of a chunk are read 32 at a time into a window
+// (lane k: entry e + k's end, first B element, row slot and value). A batch
+// that lies inside one entry (the long entries that hold most multiply-adds)
+// takes that entry's data by one shuffle each; a batch that crosses entries
+// finds each lane's entry by a five-step search over the shuffled ends. So
+// every lane is busy whatever the entries' lengths, and B is read coalesced
+// along each segment. Updates are compare-and-swap FMAs (other warps run other
+// entries of the same tile); lanes of one round that fall into different
+// entries may share a column and are combined first.
+__device__ __forceinline__ u32 window_count_le(u64 endk, u64 x) {  // window ends <= x (at most 31 for x < end[31])
+  u32 j = 0;
+#pragma unroll
+  for (u32 step = 16; step >= 1; step >>= 1) {
+    const u64 v = __shfl_sync(kFull, endk, j + step - 1);
+    if (v <= x) j += step;
+  }
+  return j;
+}
+
+template <class Add>
+__device__ void dense_item_flat(const ProdSrc &s, const u32 *__restrict__ colB, u32 ahi, u64 p0, u64 p1, u32 ea,
+                                u32 eb, u32 LB, ItemPlan &pl, Add &add) {
+  build_item_plan(s.P, ea, eb, p0, p1, 256, pl);
+  const u32 lane = threadIdx.x & 31;
+  const u64 chunk = pl.chunk;
+  const u32 nch = pl.nchunk;
+  constexpr u64 kSpan = 32 * kBatch;
+  for (;;) {
+    u32 c = 0;
+    if (lane == 0) c = atomicAdd(&pl.next, 1u);
+    c = __shfl_sync(kFull, c, 0);
+    if (c >= nch) break;
+    u64 q = p0 + u64(c) * chunk;
+    const u64 q1 = min(q + chunk, p1);
+    u32 e = pl.start[c];  // the entry holding q
+    while (q < q1) {
+      // window: entries e .. e + 31
+      const u32 ek = e + lane;
+      u64 endk = ~0ull, begk = ~0ull;
+      u32 sbk = 0, basek = 0;
+      double vak = 0.0;
+      if (ek < ahi) {
+        begk = __ldg(&s.P[ek]);
+        endk = __ldg(&s.P[ek + 1]);
+        sbk = __ldg(&s.sbA[ek]);
+        basek = __ldg(&s.slotA[ek]) * LB;
+        vak = __ldg(&s.valA[ek]);
+      }
+      const u64 wend = min(__shfl_sync(kFull, endk, 31), q1);  // the window covers [q, wend)
+      u32 jc = window_count_le(endk, q);                       // the entry holding q
+      while (q < wend) {
+        const u64 ec = __shfl_sync(kFull, endk, jc);
+        const u64 bend = min(q + kSpan, wend);
+        u32 key[kBatch];
+        double m[kBatch], x[kBatch];
+        u32 valid = 0;
+        if (ec >= bend) {  // the batch lies inside entry jc: distinct columns
+          const u64 bj = __shfl_sync(kFull, begk, jc);
+          const u32 g0 = __shfl_sync(kFull, sbk, jc) + u32(q - bj) + lane;
+          const u32 basej = __shfl_sync(kFull, basek, jc);
+          const double vaj = __shfl_sync(kFull, vak, jc);
+          const u32 n = u32(bend - q);
+#pragma unroll
+          for (int r = 0; r < kBatch; r++) {
+            const u32 i = u32(r) * 32 + lane;
+            key[r] = 0;
+            x[r] = 0.0;
+            m[r] = vaj;
+            if (i < n) {
+              key[r] = basej + __ldg(&colB[g0 + u32(r) * 32]);
+              x[r] = __ldg(&s.valB[g0 + u32(r) * 32]);
+              valid |= 1u << r;
+            }
+          }
+          add.batch(key, m, x, valid);
+          q = bend;
+          if (q == ec) jc++;
+        } else {  // the batch crosses entries: each lane finds its own
+#pragma unroll
+          for (int r = 0; r < kBatch; r++) {
+            const u64 pr = q + u64(r) * 32 + lane;
+            const bool in = pr < bend;
+            u32 j = window_count_le(endk, pr);  // every lane shuffles; lanes past the batch keep jc
+            if (!in) j = jc;
+            const u64 bj = __shfl_sync(kFull, begk, j);
+            const u32 sbj = __shfl_sync(kFull, sbk, j);
+            const u32 basej = __shfl_sync(kFull, basek, j);
+            const double vaj = __shfl_sync(kFull, vak, j);
+            key[r] = 0;
+            x[r] = 0.0;
+            m[r] = vaj;
+            if (in) {
+              const u32 g = sbj + u32(pr - bj);
+              key[r] = basej + __ldg(&colB[g]);
+              x[r] = __ldg(&s.valB[g]);
+              valid |= 1u << r;
+            }
+          }
+#pragma unroll
+          for (int r = 0; r < kBatch; r++)
+            if (((valid >> r) & 1u) && !aggregate_lanes(key[r], &m[r], &x[r])) valid &= ~(1u << r);
+          add.batch(key, m, x, valid);
+          q = bend;
+          if (q < wend) jc = window_count_le(endk, q);
+        }
+      }
+      e += 32;
+    }
+  }
+}
+
 struct DenseArgs {
   const Item *items;
   u32 nitems;
@@ -1216,7 +1332,7 @@ __device__ __forceinline__ void merge_hot_dense(double *acc, u32 *mask, double *
     for (u32 i = threadIdx.x; i < nwarps * pw; i += blockDim.x) pmask[i] = 0u;
 }
 
-template <bool kSentinel, int kThreads>
+template <bool kSentinel, int kThreads, bool kFlat>
 __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   // layout: acc[area] | mask[words] (bitmask mode) | priv[nwarps*hot] | pmask[nwarps*hot/32]
@@ -1252,8 +1368,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
     const Item item = a.items[it];
     const u32 t = item.tile;
     const u32 LB = a.tile_lb[t], used = a.tile_nrows[t] * LB;
-    dense_item<kSentinel>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, item.ea, item.eb, LB,
-                          acc, mask, plan, add, stage, ctl, a.err, a.wait_polls, a.fault_wait);
+    if constexpr (kFlat)
+      dense_item_flat(a.src, a.colB, a.tile_abeg[t + 1], item.p0, item.p1, item.ea, item.eb, LB, plan, add);
+    else
+      dense_item<kSentinel>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, item.ea, item.eb,
+                            LB, acc, mask, plan, add, stage, ctl, a.err, a.wait_polls, a.fault_wait);
     __syncthreads();
     if (a.hot) {
       merge_hot_dense<kSentinel>(acc, mask, priv, pmask, a.hot);
@@ -1283,6 +1402,20 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_dense(DenseArgs a) {
                        magic_for(LB), a.urow, a.tile_rank0[t], a.out, a.dec, a.err, s_cnt, s_warp, &s_base, s_rows);
     __syncthreads();
     if (a.merge_cyc && threadIdx.x == 0) a.merge_cyc[t] = u64(clock64() - c0);
+  }
+}
+
+using DenseKernel = void (*)(DenseArgs);
+
+// The dense tile kernel for a tile shape: touched positions by sentinel or
+// bitmask, threads per CTA, two-phase or flat items.
+template <bool kFlat>
+DenseKernel dense_kernel_for(bool sentinel, int threads) {
+  switch (threads) {
+    case 512: return sentinel ? k_contract_dense<true, 512, kFlat> : k_contract_dense<false, 512, kFlat>;
+    case 768: return sentinel ? k_contract_dense<true, 768, kFlat> : k_contract_dense<false, 768, kFlat>;
+    case 1024: return sentinel ? k_contract_dense<true, 1024, kFlat> : k_contract_dense<false, 1024, kFlat>;
+    default: return sentinel ? k_contract_dense<true, 640, kFlat> : k_contract_dense<false, 640, kFlat>;
   }
 }
 
@@ -2254,6 +2387,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (opt.out_waves < 0 || opt.out_waves > kMaxWaves) throw Error{FCC_ERR_ARG, "out_waves must be in 0..16"};
   if (opt.wait_polls < 0) throw Error{FCC_ERR_ARG, "wait_polls must be >= 0"};
   if (opt.fault_wait != 0 && opt.fault_wait != 1) throw Error{FCC_ERR_ARG, "fault_wait must be 0 or 1"};
+  if (opt.dense_kernel < 0 || opt.dense_kernel > 2) throw Error{FCC_ERR_ARG, "dense_kernel must be 0, 1 or 2"};
   if (opt.esc_group < 0) throw Error{FCC_ERR_ARG, "esc_group must be >= 0"};
   const bool learned = forced < 0 && opt.schedule == FCC_SCHED_LEARNED && ctx->sched && ctx->sched->model;
   const bool want_record = opt.timing == 2 && ctx->sched;
@@ -2652,6 +2786,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
                  item_cyc ? item_cyc + cbeg[FCC_CLASS_DENSE] : nullptr, 0u, merge_cyc};
     if (opt.wait_polls > 0) da.wait_polls = opt.wait_polls;
     da.fault_wait = opt.fault_wait ? 1u : 0u;
+    const bool flat = opt.dense_kernel == 2;
     // Items of class c in wave w: a contiguous slice of the class's items.
     auto wave_items = [&](int c, int w, u32 &lo, u32 &n) {
       lo = u32(u64(ccount[c]) * u64(w) / u64(waves));
@@ -2669,34 +2804,16 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       size_t smem = class_smem(FCC_CLASS_DENSE, hot);
       // phase 1's staging ring, when it fits beside the tile
       const size_t soff = (smem + 15) & ~size_t(15);
-      if (opt.dense_staging >= 0 && soff + kStageBytes <= dense_dyn_cap) {
+      if (!flat && opt.dense_staging >= 0 && soff + kStageBytes <= dense_dyn_cap) {
         da.stage_off = u32(soff);
         smem = soff + kStageBytes;
       }
-      const void *kern;
-      if (threads == 512) kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true, 512>)
-                                          : reinterpret_cast<const void *>(k_contract_dense<false, 512>);
-      else if (threads == 640) kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true, 640>)
-                                               : reinterpret_cast<const void *>(k_contract_dense<false, 640>);
-      else if (threads == 768) kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true, 768>)
-                                               : reinterpret_cast<const void *>(k_contract_dense<false, 768>);
-      else kern = sentinel ? reinterpret_cast<const void *>(k_contract_dense<true, 1024>)
-                           : reinterpret_cast<const void *>(k_contract_dense<false, 1024>);
-      FCC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-      const int grid = grid_tiles(ctx, kern, threads, smem, da.nitems, &ctas_per_sm[FCC_CLASS_DENSE]);
-      if (threads == 512) {
-        if (sentinel) k_contract_dense<true, 512><<<grid, 512, smem, st>>>(da);
-        else k_contract_dense<false, 512><<<grid, 512, smem, st>>>(da);
-      } else if (threads == 640) {
-        if (sentinel) k_contract_dense<true, 640><<<grid, 640, smem, st>>>(da);
-        else k_contract_dense<false, 640><<<grid, 640, smem, st>>>(da);
-      } else if (threads == 768) {
-        if (sentinel) k_contract_dense<true, 768><<<grid, 768, smem, st>>>(da);
-        else k_contract_dense<false, 768><<<grid, 768, smem, st>>>(da);
-      } else {
-        if (sentinel) k_contract_dense<true, 1024><<<grid, 1024, smem, st>>>(da);
-        else k_contract_dense<false, 1024><<<grid, 1024, smem, st>>>(da);
-      }
+      const DenseKernel kern = flat ? dense_kernel_for<true>(sentinel, threads) : dense_kernel_for<false>(sentinel, threads);
+      FCC_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void *>(kern), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    int(smem)));
+      const int grid = grid_tiles(ctx, reinterpret_cast<const void *>(kern), threads, smem, da.nitems,
+                                  &ctas_per_sm[FCC_CLASS_DENSE]);
+      kern<<<grid, threads, smem, st>>>(da);
       FCC_LAUNCH_CHECK();
     };
     // w >= 0: the hash classes' items of wave w; w < 0: the merges of split

@@ -56,7 +56,8 @@ class Options(ctypes.Structure):
                 ("dense_fill_log2", ctypes.c_int32), ("dense_staging", ctypes.c_int32),
                 ("sched_mix_margin", ctypes.c_int32), ("hash_esc", ctypes.c_int32),
                 ("out_waves", ctypes.c_int32), ("esc_group", ctypes.c_int32),
-                ("wait_polls", ctypes.c_int32), ("fault_wait", ctypes.c_int32)]
+                ("wait_polls", ctypes.c_int32), ("fault_wait", ctypes.c_int32),
+                ("dense_kernel", ctypes.c_int32), ("pad1", ctypes.c_int32)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -367,7 +368,7 @@ class Context:
 
     @staticmethod
     def options_dict(o):
-        return {name: getattr(o, name) for name, _ in Options._fields_ if name not in ("pad0", "reserved")}
+        return {name: getattr(o, name) for name, _ in Options._fields_ if name not in ("pad0", "pad1", "reserved")}
 
     def load_default_model(self):
         """Installs the cost model shipped with the package (sched_model.f32); False when absent."""

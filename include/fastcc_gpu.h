@@ -136,6 +136,13 @@ typedef struct fcc_options {
                                  completes, so that the wait runs out after wait_polls polls and
                                  the call returns FCC_ERR_TIMEOUT; the context stays usable.
                                  0 (default): off */
+  int32_t dense_kernel;       /* how a dense tile runs its multiply-adds. 1: two phases (A entries
+                                 with long B segments by the whole CTA through a bulk-copy ring
+                                 with plain read-modify-writes, the rest by warps with
+                                 compare-and-swap); 2: flat (warps take runs of consecutive
+                                 multiply-adds, one per lane, compare-and-swap updates).
+                                 0 (default): 1 */
+  int32_t pad1;
 } fcc_options;
 
 /* Tile classes: every output tile runs in one of them. The hash classes

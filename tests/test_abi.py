@@ -42,7 +42,7 @@ def test_library_loads_and_reports_status_strings():
     assert L.fcc_status_string(3) == b"hash accumulator full"
     o = F.Options()
     assert L.fcc_options_default(ctypes.byref(o)) == 0 and o.tile_size == 100
-    assert ctypes.sizeof(F.Options) == 96
+    assert ctypes.sizeof(F.Options) == 104
 
 
 def test_bad_arguments_return_status_not_crash():

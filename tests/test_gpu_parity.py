@@ -55,6 +55,11 @@ VARIANTS = [
     {"accumulator": F.ACC_HASH, "hash_esc": 2},                               # every hash tile expanded
     {"accumulator": F.ACC_HASH, "hash_esc": 2, "esc_group": 3},               # ... sorted in groups of 3 tiles
     {"accumulator": F.ACC_HASH, "products_per_item": 6, "esc_group": 1},
+    {"dense_kernel": 2},                                                     # flat dense items
+    {"dense_kernel": 2, "products_per_item": 7, "dense_mode": F.DENSE_BITMASK},
+    {"dense_kernel": 2, "rows_per_tile": 1, "dense_mode": F.DENSE_SENTINEL},
+    {"dense_kernel": 2, "hot_columns": 32, "rows_per_tile": 1, "tile_threads": 512},
+    {"dense_kernel": 1},
 ]
 
 

@@ -21,8 +21,12 @@ pytestmark = pytest.mark.gpu
 
 def _staged_case():
     # Zipf(1.2) self-contraction: hub contraction keys have B segments of
-    # thousands of entries, so dense items run phase 1 through the ring.
+    # thousands of entries, so dense items run phase 1 through the ring (one
+    # row per tile leaves room for the ring beside the 5,000-column tile).
     return workloads.zipf3(seed=3, nnz=400_000, dims=(5_000, 2_000, 5_000))
+
+
+STAGED = {"rows_per_tile": 1, "dense_kernel": 1}
 
 
 def _check(ctx, w, opts=None):
@@ -43,16 +47,17 @@ def test_injected_wait_times_out_and_context_recovers():
     with F.Context(0) as ctx:
         for polls in (1, 64):
             with pytest.raises(F.FccError) as e:
-                ctx.contract(a, b, w["ctr_a"], w["ctr_b"], F.Options(fault_wait=1, wait_polls=polls))
+                ctx.contract(a, b, w["ctr_a"], w["ctr_b"], F.Options(fault_wait=1, wait_polls=polls, **STAGED))
             assert e.value.status == 4, e.value  # FCC_ERR_TIMEOUT
             assert "bounded device wait" in str(e.value)
-            _check(ctx, w)  # the same context, right after the timeout
+            _check(ctx, w, F.Options(**STAGED))  # the same context, right after the timeout
+            _check(ctx, w)
 
 
 def test_default_and_short_poll_limits_without_injection_are_exact(ctx):
     # without the injected wait, a limit of 2^16 polls is ample for the ring
     w = _staged_case()
-    _check(ctx, w, F.Options(wait_polls=1 << 16))
+    _check(ctx, w, F.Options(wait_polls=1 << 16, **STAGED))
 
 
 def test_wait_options_are_validated(ctx):
