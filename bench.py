@@ -385,18 +385,23 @@ def run_sweep_batched(variants, reps):
         for v in variants:
             opts = F.Options(timing=1, **v)
             ph = []
+            clk = Clocks(0)
             for rep in range(reps + 1):
+                if rep == 1:
+                    clk.start()
                 r, _ = ctx.contract_batch(As, Bs, [1, 3], [1, 2], opts)
                 n = r.nnz
                 r.free()
                 if rep:
                     ph.append(ctx.timings())
+            c = clk.stop()
             med = {k: statistics.median(p[k] for p in ph) for k in ph[0]}
             print(json.dumps({"workload": "batched", "options": v, "outputs": n,
-                              "phases_ms": {k: round(x, 3) for k, x in med.items()}}), flush=True)
+                              "phases_ms": {k: round(x, 3) for k, x in med.items()}, "sm_mhz": c["sm_mhz"],
+                              "reasons": c["reasons"]}), flush=True)
 
 
-def run_sweep(name, variants, reps=3):
+def run_sweep(name, variants, reps=10):
     """Times option sets on one workload (device-resident, median of reps),
     one JSON line per option set."""
     import torch
@@ -418,15 +423,20 @@ def run_sweep(name, variants, reps=3):
         for v in variants:
             opts = F.Options(timing=1, **v)
             ph = []
+            clk = Clocks(0)
             for rep in range(reps + 1):
+                if rep == 1:
+                    clk.start()
                 r = ctx.contract(A, B, w["ctr_a"], w["ctr_b"], opts)
                 t = ctx.timings()
                 r.free()
                 if rep:
                     ph.append(t)
+            c = clk.stop()
             med = {k: round(statistics.median(p[k] for p in ph), 4) for k in ph[0]}
             print(json.dumps({"workload": name, "options": v, "total_ms": med["total"],
-                              "contract_ms": med["contract"], "phases_ms": med}), flush=True)
+                              "contract_ms": med["contract"], "sm_mhz": c["sm_mhz"], "reasons": c["reasons"],
+                              "phases_ms": med}), flush=True)
 
 
 def hbm_roofline(alg_bytes, ms, what):

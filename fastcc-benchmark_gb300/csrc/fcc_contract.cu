@@ -579,6 +579,7 @@ __global__ void k_apply_colmap(ColT *__restrict__ col, i64 n, const u32 *__restr
 //  * shorter entries go one per lane, up to 32 at once, so rows made of many
 //    rare keys (hub rows of Zipf tensors) keep every lane busy.
 
+constexpr int kDefaultDenseMode = 1;  // fcc_options.dense_kernel 0 means this
 constexpr int kTileThreads = 640;   // dense tiles by default (20 warps in 96 registers); 512, 768, 1024 on request
 constexpr int kMergeThreads = 512;  // merges of split tiles
 constexpr int kBatch = 4;
@@ -693,7 +694,7 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
           m[k] = wva;
           if (i < wn) valid |= 1u << k;
         }
-        add.batch(key, m, v, valid);
+        add.batch(key, m, v, valid, true, false);
       }
     }
     if (mine) {  // one entry per lane
@@ -713,7 +714,7 @@ __device__ __forceinline__ void products_chunk(const ProdSrc &s, const ColT *__r
           m[k] = va;
           if (o + k < cnt && aggregate_lanes(key[k], &m[k], &v[k])) valid |= 1u << k;
         }
-        add.batch(key, m, v, valid);
+        add.batch(key, m, v, valid, false, false);
       }
     }
     if (!any_left) break;
@@ -957,7 +958,143 @@ __device__ void dense_phase1_staged(const ProdSrc &s, const u32 *__restrict__ co
   __syncthreads();
 }
 
-template <bool kSentinel, class Add>
+// ---- dense items, flat ----
+//
+// The item's multiply-adds [p0, p1) are numbered by the prefix P over its A
+// entries; warps pull chunks of consecutive numbers and give each lane one
+// multiply-add per round, kBatch rounds at a time (their loads in flight
+// together). The A entries of a chunk are read 32 at a time into a window
+// (lane k: entry e + k's end, first B element, row slot and value). A batch
+// that lies inside one entry (the long entries that hold most multiply-adds)
+// takes that entry's data by one shuffle each; a batch that crosses entries
+// finds each lane's entry by a five-step search over the shuffled ends. So
+// every lane is busy whatever the entries' lengths, and B is read coalesced
+// along each segment. Updates are compare-and-swap FMAs (other warps run other
+// entries of the same tile); lanes of one round that fall into different
+// entries may share a column and are combined first. The most frequent
+// columns (renumbered to [0, hot)) go to the warp's private copy with plain
+// read-modify-writes (see DenseAdd).
+__device__ __forceinline__ u32 window_count_le(u64 endk, u64 x) {  // window ends <= x (at most 31 for x < end[31])
+  u32 j = 0;
+#pragma unroll
+  for (u32 step = 16; step >= 1; step >>= 1) {
+    const u64 v = __shfl_sync(kFull, endk, j + step - 1);
+    if (v <= x) j += step;
+  }
+  return j;
+}
+
+// Warps pull the item plan's chunks and run their multiply-adds flat. Entries
+// with at least `skip` multiply-adds in [p0, p1) are left out (phase 1 of a
+// two-phase item ran them); kNoSkip runs every entry.
+template <class Add>
+__device__ void flat_chunks(const ProdSrc &s, const u32 *__restrict__ colB, u32 ahi, u64 p0, u64 p1, u32 LB,
+                            ItemPlan &pl, Add &add, u64 skip) {
+  const u32 lane = threadIdx.x & 31;
+  const u64 chunk = pl.chunk;
+  const u32 nch = pl.nchunk;
+  constexpr u64 kSpan = 32 * kBatch;
+  for (;;) {
+    u32 c = 0;
+    if (lane == 0) c = atomicAdd(&pl.next, 1u);
+    c = __shfl_sync(kFull, c, 0);
+    if (c >= nch) break;
+    u64 q = p0 + u64(c) * chunk;
+    const u64 q1 = min(q + chunk, p1);
+    u32 e = pl.start[c];  // the entry holding q
+    while (q < q1) {
+      // window: entries e .. e + 31
+      const u32 ek = e + lane;
+      u64 endk = ~0ull, begk = ~0ull;
+      u32 sbk = 0, basek = 0, longk = 0;
+      double vak = 0.0;
+      if (ek < ahi) {
+        begk = __ldg(&s.P[ek]);
+        endk = __ldg(&s.P[ek + 1]);
+        sbk = __ldg(&s.sbA[ek]);
+        basek = __ldg(&s.slotA[ek]) * LB;
+        vak = __ldg(&s.valA[ek]);
+        longk = skip != kNoSkip && min(endk, p1) - max(begk, p0) >= skip;
+      }
+      const u64 wend = min(__shfl_sync(kFull, endk, 31), q1);  // the window covers [q, wend)
+      u32 jc = window_count_le(endk, q);                       // the entry holding q
+      while (q < wend) {
+        const u64 ec = __shfl_sync(kFull, endk, jc);
+        if (__shfl_sync(kFull, longk, jc)) {  // run by phase 1
+          q = min(ec, wend);
+          if (q == ec) jc++;
+          continue;
+        }
+        const u64 bend = min(q + kSpan, wend);
+        u32 key[kBatch];
+        double m[kBatch], x[kBatch];
+        u32 valid = 0;
+        if (ec >= bend) {  // the batch lies inside entry jc: distinct columns
+          const u64 bj = __shfl_sync(kFull, begk, jc);
+          const u32 g0 = __shfl_sync(kFull, sbk, jc) + u32(q - bj) + lane;
+          const u32 basej = __shfl_sync(kFull, basek, jc);
+          const double vaj = __shfl_sync(kFull, vak, jc);
+          const u32 n = u32(bend - q);
+#pragma unroll
+          for (int r = 0; r < kBatch; r++) {
+            const u32 i = u32(r) * 32 + lane;
+            key[r] = 0;
+            x[r] = 0.0;
+            m[r] = vaj;
+            if (i < n) {
+              key[r] = basej + __ldg(&colB[g0 + u32(r) * 32]);
+              x[r] = __ldg(&s.valB[g0 + u32(r) * 32]);
+              valid |= 1u << r;
+            }
+          }
+          add.batch(key, m, x, valid, true, true);
+          q = bend;
+          if (q == ec) jc++;
+        } else {  // the batch crosses entries: each lane finds its own
+#pragma unroll
+          for (int r = 0; r < kBatch; r++) {
+            const u64 pr = q + u64(r) * 32 + lane;
+            u32 j = window_count_le(endk, pr);  // every lane shuffles; lanes past the batch keep jc
+            if (pr >= bend) j = jc;
+            const u64 bj = __shfl_sync(kFull, begk, j);
+            const u32 sbj = __shfl_sync(kFull, sbk, j);
+            const u32 basej = __shfl_sync(kFull, basek, j);
+            const double vaj = __shfl_sync(kFull, vak, j);
+            const u32 lj = __shfl_sync(kFull, longk, j);
+            key[r] = 0;
+            x[r] = 0.0;
+            m[r] = vaj;
+            if (pr < bend && !lj) {
+              const u32 g = sbj + u32(pr - bj);
+              key[r] = basej + __ldg(&colB[g]);
+              x[r] = __ldg(&s.valB[g]);
+              valid |= 1u << r;
+            }
+          }
+#pragma unroll
+          for (int r = 0; r < kBatch; r++)
+            if (((valid >> r) & 1u) && !aggregate_lanes(key[r], &m[r], &x[r])) valid &= ~(1u << r);
+          __syncwarp();
+          add.batch(key, m, x, valid, false, true);
+          q = bend;
+          if (q < wend) jc = window_count_le(endk, q);
+        }
+      }
+      e += 32;
+    }
+  }
+}
+
+template <class Add>
+__device__ void dense_item_flat(const ProdSrc &s, const u32 *__restrict__ colB, u32 ahi, u64 p0, u64 p1, u32 ea,
+                                u32 eb, u32 LB, ItemPlan &pl, Add &add) {
+  build_item_plan(s.P, ea, eb, p0, p1, 256, pl);
+  flat_chunks(s, colB, ahi, p0, p1, LB, pl, add, kNoSkip);
+}
+
+// kFlat2: phase 2 runs flat (flat_chunks, the phase-1 entries left out)
+// instead of products_chunk's windows of one entry per lane.
+template <bool kSentinel, bool kFlat2, class Add>
 __device__ void dense_item(const ProdSrc &s, const u32 *__restrict__ colB, u32 alo, u32 ahi, u64 p0, u64 p1,
                            u32 ea, u32 eb, u32 LB, double *acc, u32 *mask, ItemPlan &pl, Add &add,
                            unsigned char *stage, StageCtl &ctl, u32 *err, long long polls, u32 fault_wait) {
@@ -994,6 +1131,10 @@ __device__ void dense_item(const ProdSrc &s, const u32 *__restrict__ colB, u32 a
     __syncthreads();
   }
   // phase 2
+  if (kFlat2) {
+    flat_chunks(s, colB, ahi, p0, p1, LB, pl, add, u64(kCtaRun));
+    return;
+  }
   const u64 chunk = pl.chunk;
   const u32 nch = pl.nchunk;
   for (;;) {
@@ -1004,122 +1145,6 @@ __device__ void dense_item(const ProdSrc &s, const u32 *__restrict__ colB, u32 a
     const u64 q0 = p0 + u64(c) * chunk;
     const u64 q1 = min(q0 + chunk, p1);
     products_chunk<u32, u32>(s, colB, alo, ahi, pl.start[c], q0, q1, p0, p1, u64(kCtaRun), LB, add);
-  }
-}
-
-// ---- dense items, flat ----
-//
-// The item's multiply-adds [p0, p1) are numbered by the prefix P over its A
-// entries; warps pull chunks of consecutive numbers and give each lane one
-// multiply-add per round, kBatch rounds at a time (their loads in flight
-// together). The A entries of a chunk are read 32 at a time into a window
-// (lane k: entry e + k's end, first B element, row slot and value). A batch
-// that lies inside one entry (the long entries that hold most multiply-adds)
-// takes that entry's data by one shuffle each; a batch that crosses entries
-// finds each lane's entry by a five-step search over the shuffled ends. So
-// every lane is busy whatever the entries' lengths, and B is read coalesced
-// along each segment. Updates are compare-and-swap FMAs (other warps run other
-// entries of the same tile); lanes of one round that fall into different
-// entries may share a column and are combined first.
-__device__ __forceinline__ u32 window_count_le(u64 endk, u64 x) {  // window ends <= x (at most 31 for x < end[31])
-  u32 j = 0;
-#pragma unroll
-  for (u32 step = 16; step >= 1; step >>= 1) {
-    const u64 v = __shfl_sync(kFull, endk, j + step - 1);
-    if (v <= x) j += step;
-  }
-  return j;
-}
-
-template <class Add>
-__device__ void dense_item_flat(const ProdSrc &s, const u32 *__restrict__ colB, u32 ahi, u64 p0, u64 p1, u32 ea,
-                                u32 eb, u32 LB, ItemPlan &pl, Add &add) {
-  build_item_plan(s.P, ea, eb, p0, p1, 256, pl);
-  const u32 lane = threadIdx.x & 31;
-  const u64 chunk = pl.chunk;
-  const u32 nch = pl.nchunk;
-  constexpr u64 kSpan = 32 * kBatch;
-  for (;;) {
-    u32 c = 0;
-    if (lane == 0) c = atomicAdd(&pl.next, 1u);
-    c = __shfl_sync(kFull, c, 0);
-    if (c >= nch) break;
-    u64 q = p0 + u64(c) * chunk;
-    const u64 q1 = min(q + chunk, p1);
-    u32 e = pl.start[c];  // the entry holding q
-    while (q < q1) {
-      // window: entries e .. e + 31
-      const u32 ek = e + lane;
-      u64 endk = ~0ull, begk = ~0ull;
-      u32 sbk = 0, basek = 0;
-      double vak = 0.0;
-      if (ek < ahi) {
-        begk = __ldg(&s.P[ek]);
-        endk = __ldg(&s.P[ek + 1]);
-        sbk = __ldg(&s.sbA[ek]);
-        basek = __ldg(&s.slotA[ek]) * LB;
-        vak = __ldg(&s.valA[ek]);
-      }
-      const u64 wend = min(__shfl_sync(kFull, endk, 31), q1);  // the window covers [q, wend)
-      u32 jc = window_count_le(endk, q);                       // the entry holding q
-      while (q < wend) {
-        const u64 ec = __shfl_sync(kFull, endk, jc);
-        const u64 bend = min(q + kSpan, wend);
-        u32 key[kBatch];
-        double m[kBatch], x[kBatch];
-        u32 valid = 0;
-        if (ec >= bend) {  // the batch lies inside entry jc: distinct columns
-          const u64 bj = __shfl_sync(kFull, begk, jc);
-          const u32 g0 = __shfl_sync(kFull, sbk, jc) + u32(q - bj) + lane;
-          const u32 basej = __shfl_sync(kFull, basek, jc);
-          const double vaj = __shfl_sync(kFull, vak, jc);
-          const u32 n = u32(bend - q);
-#pragma unroll
-          for (int r = 0; r < kBatch; r++) {
-            const u32 i = u32(r) * 32 + lane;
-            key[r] = 0;
-            x[r] = 0.0;
-            m[r] = vaj;
-            if (i < n) {
-              key[r] = basej + __ldg(&colB[g0 + u32(r) * 32]);
-              x[r] = __ldg(&s.valB[g0 + u32(r) * 32]);
-              valid |= 1u << r;
-            }
-          }
-          add.batch(key, m, x, valid);
-          q = bend;
-          if (q == ec) jc++;
-        } else {  // the batch crosses entries: each lane finds its own
-#pragma unroll
-          for (int r = 0; r < kBatch; r++) {
-            const u64 pr = q + u64(r) * 32 + lane;
-            const bool in = pr < bend;
-            u32 j = window_count_le(endk, pr);  // every lane shuffles; lanes past the batch keep jc
-            if (!in) j = jc;
-            const u64 bj = __shfl_sync(kFull, begk, j);
-            const u32 sbj = __shfl_sync(kFull, sbk, j);
-            const u32 basej = __shfl_sync(kFull, basek, j);
-            const double vaj = __shfl_sync(kFull, vak, j);
-            key[r] = 0;
-            x[r] = 0.0;
-            m[r] = vaj;
-            if (in) {
-              const u32 g = sbj + u32(pr - bj);
-              key[r] = basej + __ldg(&colB[g]);
-              x[r] = __ldg(&s.valB[g]);
-              valid |= 1u << r;
-            }
-          }
-#pragma unroll
-          for (int r = 0; r < kBatch; r++)
-            if (((valid >> r) & 1u) && !aggregate_lanes(key[r], &m[r], &x[r])) valid &= ~(1u << r);
-          add.batch(key, m, x, valid);
-          q = bend;
-          if (q < wend) jc = window_count_le(endk, q);
-        }
-      }
-      e += 32;
-    }
   }
 }
 
@@ -1293,20 +1318,32 @@ struct DenseAdd {
   double *priv;  // this warp's copy of the hot columns
   u32 *pmask;    // its touched bits (bitmask mode)
   u32 hot;
+  // Applies a lane's kBatch updates (key[k] += m[k] * x[k] where valid).
+  // distinct: the warp's updates of this batch have distinct keys (one A
+  // entry's B segment); otherwise only the lanes of one round k are distinct
+  // (combined beforehand). plain_priv: the whole warp calls converged, so
+  // its private hot-column copy, which no other warp touches, takes plain
+  // read-modify-writes (rounds of different keys ordered by __syncwarp);
+  // otherwise it takes compare-and-swap like the shared tile.
   __device__ __forceinline__ void batch(const u32 (&key)[kBatch], const double (&m)[kBatch],
-                                        const double (&x)[kBatch], u32 valid) const {
+                                        const double (&x)[kBatch], u32 valid, bool distinct,
+                                        bool plain_priv) const {
 #pragma unroll
-    for (int k = 0; k < kBatch; k++)
+    for (int k = 0; k < kBatch; k++) {
       if ((valid >> k) & 1u) {
         const u32 q = key[k];
         if (q < hot) {
-          fma_shared(&priv[q], m[k], x[k]);
+          if (plain_priv) priv[q] = fma(m[k], x[k], priv[q]);
+          else fma_shared(&priv[q], m[k], x[k]);
           if (!kSentinel) atomicOr(&pmask[q >> 5], 1u << (q & 31));
         } else {
           fma_shared(&acc[q], m[k], x[k]);
           if (!kSentinel) atomicOr(&mask[q >> 5], 1u << (q & 31));
         }
       }
+      if (plain_priv && !distinct && hot) __syncwarp();
+    }
+    if (plain_priv && distinct && hot) __syncwarp();  // before the warp's next batch
   }
 };
 
@@ -1332,7 +1369,9 @@ __device__ __forceinline__ void merge_hot_dense(double *acc, u32 *mask, double *
     for (u32 i = threadIdx.x; i < nwarps * pw; i += blockDim.x) pmask[i] = 0u;
 }
 
-template <bool kSentinel, int kThreads, bool kFlat>
+// kMode 1: two-phase items (dense_item); 2: flat items (dense_item_flat);
+// 3: two-phase items whose phase 2 runs flat.
+template <bool kSentinel, int kThreads, int kMode>
 __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   // layout: acc[area] | mask[words] (bitmask mode) | priv[nwarps*hot] | pmask[nwarps*hot/32]
@@ -1368,11 +1407,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_contract_dense(DenseArgs a) {
     const Item item = a.items[it];
     const u32 t = item.tile;
     const u32 LB = a.tile_lb[t], used = a.tile_nrows[t] * LB;
-    if constexpr (kFlat)
+    if constexpr (kMode == 2)
       dense_item_flat(a.src, a.colB, a.tile_abeg[t + 1], item.p0, item.p1, item.ea, item.eb, LB, plan, add);
     else
-      dense_item<kSentinel>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1, item.ea, item.eb,
-                            LB, acc, mask, plan, add, stage, ctl, a.err, a.wait_polls, a.fault_wait);
+      dense_item<kSentinel, kMode == 3>(a.src, a.colB, a.tile_abeg[t], a.tile_abeg[t + 1], item.p0, item.p1,
+                                        item.ea, item.eb, LB, acc, mask, plan, add, stage, ctl, a.err,
+                                        a.wait_polls, a.fault_wait);
     __syncthreads();
     if (a.hot) {
       merge_hot_dense<kSentinel>(acc, mask, priv, pmask, a.hot);
@@ -1409,13 +1449,13 @@ using DenseKernel = void (*)(DenseArgs);
 
 // The dense tile kernel for a tile shape: touched positions by sentinel or
 // bitmask, threads per CTA, two-phase or flat items.
-template <bool kFlat>
+template <int kMode>
 DenseKernel dense_kernel_for(bool sentinel, int threads) {
   switch (threads) {
-    case 512: return sentinel ? k_contract_dense<true, 512, kFlat> : k_contract_dense<false, 512, kFlat>;
-    case 768: return sentinel ? k_contract_dense<true, 768, kFlat> : k_contract_dense<false, 768, kFlat>;
-    case 1024: return sentinel ? k_contract_dense<true, 1024, kFlat> : k_contract_dense<false, 1024, kFlat>;
-    default: return sentinel ? k_contract_dense<true, 640, kFlat> : k_contract_dense<false, 640, kFlat>;
+    case 512: return sentinel ? k_contract_dense<true, 512, kMode> : k_contract_dense<false, 512, kMode>;
+    case 768: return sentinel ? k_contract_dense<true, 768, kMode> : k_contract_dense<false, 768, kMode>;
+    case 1024: return sentinel ? k_contract_dense<true, 1024, kMode> : k_contract_dense<false, 1024, kMode>;
+    default: return sentinel ? k_contract_dense<true, 640, kMode> : k_contract_dense<false, 640, kMode>;
   }
 }
 
@@ -1542,7 +1582,8 @@ struct HashAdd {
     atomicOr(err, ERRB_HASH);
   }
   __device__ __forceinline__ void batch(const u64 (&key)[kBatch], const double (&m)[kBatch],
-                                        const double (&x)[kBatch], u32 valid) const {
+                                        const double (&x)[kBatch], u32 valid, bool /*distinct*/,
+                                        bool /*plain_priv*/) const {
 #pragma unroll
     for (int k = 0; k < kBatch; k++)
       if ((valid >> k) & 1u) (*this)(key[k], m[k], x[k]);
@@ -2387,7 +2428,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (opt.out_waves < 0 || opt.out_waves > kMaxWaves) throw Error{FCC_ERR_ARG, "out_waves must be in 0..16"};
   if (opt.wait_polls < 0) throw Error{FCC_ERR_ARG, "wait_polls must be >= 0"};
   if (opt.fault_wait != 0 && opt.fault_wait != 1) throw Error{FCC_ERR_ARG, "fault_wait must be 0 or 1"};
-  if (opt.dense_kernel < 0 || opt.dense_kernel > 2) throw Error{FCC_ERR_ARG, "dense_kernel must be 0, 1 or 2"};
+  if (opt.dense_kernel < 0 || opt.dense_kernel > 3) throw Error{FCC_ERR_ARG, "dense_kernel must be 0, 1, 2 or 3"};
   if (opt.esc_group < 0) throw Error{FCC_ERR_ARG, "esc_group must be >= 0"};
   const bool learned = forced < 0 && opt.schedule == FCC_SCHED_LEARNED && ctx->sched && ctx->sched->model;
   const bool want_record = opt.timing == 2 && ctx->sched;
@@ -2786,7 +2827,8 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
                  item_cyc ? item_cyc + cbeg[FCC_CLASS_DENSE] : nullptr, 0u, merge_cyc};
     if (opt.wait_polls > 0) da.wait_polls = opt.wait_polls;
     da.fault_wait = opt.fault_wait ? 1u : 0u;
-    const bool flat = opt.dense_kernel == 2;
+    const int dmode = opt.dense_kernel == 0 ? kDefaultDenseMode : opt.dense_kernel;
+    const bool flat = dmode == 2;
     // Items of class c in wave w: a contiguous slice of the class's items.
     auto wave_items = [&](int c, int w, u32 &lo, u32 &n) {
       lo = u32(u64(ccount[c]) * u64(w) / u64(waves));
@@ -2808,7 +2850,9 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
         da.stage_off = u32(soff);
         smem = soff + kStageBytes;
       }
-      const DenseKernel kern = flat ? dense_kernel_for<true>(sentinel, threads) : dense_kernel_for<false>(sentinel, threads);
+      const DenseKernel kern = dmode == 2   ? dense_kernel_for<2>(sentinel, threads)
+                               : dmode == 3 ? dense_kernel_for<3>(sentinel, threads)
+                                            : dense_kernel_for<1>(sentinel, threads);
       FCC_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void *>(kern), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     int(smem)));
       const int grid = grid_tiles(ctx, reinterpret_cast<const void *>(kern), threads, smem, da.nitems,

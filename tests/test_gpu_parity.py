@@ -60,6 +60,11 @@ VARIANTS = [
     {"dense_kernel": 2, "rows_per_tile": 1, "dense_mode": F.DENSE_SENTINEL},
     {"dense_kernel": 2, "hot_columns": 32, "rows_per_tile": 1, "tile_threads": 512},
     {"dense_kernel": 1},
+    {"dense_kernel": 3},                                                     # flat phase 2
+    {"dense_kernel": 3, "products_per_item": 7, "dense_mode": F.DENSE_BITMASK, "rows_per_tile": 1},
+    {"dense_kernel": 3, "hot_columns": 32, "rows_per_tile": 1},             # private hot columns, plain updates
+    {"dense_kernel": 2, "hot_columns": 64, "rows_per_tile": 1, "dense_mode": F.DENSE_BITMASK,
+     "products_per_item": 9},
 ]
 
 
