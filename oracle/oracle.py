@@ -220,8 +220,9 @@ def reference_multiply(a_coords, a_vals, a_max, b_coords, b_vals, b_max, ctr_a, 
     coords = ctypes.POINTER(ctypes.c_int32)()
     order = ctypes.c_int32()
     ms = ctypes.c_double()
-    rc = r.ref_fastcc_multiply(ac.shape[1], ac.shape[0], _ptr(ac), _ptr(av), _ptr(am),
-                               bc.shape[1], bc.shape[0], _ptr(bc), _ptr(bv), _ptr(bm),
+    i32, i64 = ctypes.c_int32, ctypes.c_int64
+    rc = r.ref_fastcc_multiply(i32(ac.shape[1]), i64(ac.shape[0]), _ptr(ac), _ptr(av), _ptr(am),
+                               i32(bc.shape[1]), i64(bc.shape[0]), _ptr(bc), _ptr(bv), _ptr(bm),
                                _ptr(ca), _ptr(cb), ctypes.c_int32(len(ca)),
                                ctypes.c_int32(tile_size), ctypes.c_int32(1 if shipped else 0),
                                ctypes.byref(n), ctypes.byref(left), ctypes.byref(right),
@@ -243,6 +244,37 @@ def reference_multiply(a_coords, a_vals, a_max, b_coords, b_vals, b_max, ctr_a, 
         r.ref_free(right)
     r.ref_free(vals)
     return out
+
+
+def reference_multiply_modes(a_coords, a_vals, a_max, b_coords, b_vals, b_max, ctr_a, ctr_b, batch_a, batch_b):
+    """The reference's own Tensor<double>::multiply with batch modes
+    (contract.hpp:286-367; needs oracle/_ref). Returns (coords (n, order)
+    int32 in the reference's entry order, values)."""
+    r = ref_lib()
+    r.ref_multiply_modes.restype = ctypes.c_int
+    arr = lambda x, t: np.ascontiguousarray(x, t)
+    ac, bc = arr(a_coords, np.int32), arr(b_coords, np.int32)
+    av, bv = arr(a_vals, np.float64), arr(b_vals, np.float64)
+    am, bm = arr(a_max, np.int32), arr(b_max, np.int32)
+    ca, cb, ba, bb = (arr(x, np.int32) for x in (ctr_a, ctr_b, batch_a, batch_b))
+    n = ctypes.c_int64()
+    coords = ctypes.POINTER(ctypes.c_int32)()
+    vals = ctypes.POINTER(ctypes.c_double)()
+    order = ctypes.c_int32()
+    i32, i64 = ctypes.c_int32, ctypes.c_int64
+    rc = r.ref_multiply_modes(i32(ac.shape[1]), i64(ac.shape[0]), _ptr(ac), _ptr(av), _ptr(am),
+                              i32(bc.shape[1]), i64(bc.shape[0]), _ptr(bc), _ptr(bv), _ptr(bm),
+                              _ptr(ca), _ptr(cb), ctypes.c_int32(len(ca)), _ptr(ba), _ptr(bb),
+                              ctypes.c_int32(len(ba)), ctypes.byref(n), ctypes.byref(coords),
+                              ctypes.byref(order), ctypes.byref(vals))
+    if rc != 0:
+        raise ValueError("reference harness rejected the arguments")
+    k, d = n.value, order.value
+    out_c = np.ctypeslib.as_array(coords, (k * d + 1,))[: k * d].reshape(k, d).copy()
+    out_v = np.ctypeslib.as_array(vals, (k + 1,))[:k].copy()
+    r.ref_free(coords)
+    r.ref_free(vals)
+    return out_c, out_v
 
 
 def external_radices(max_index, ctr):

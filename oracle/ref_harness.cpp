@@ -155,6 +155,39 @@ int ref_fastcc_multiply(int32_t ordA, int64_t nnzA, const int32_t *cA, const dou
   return 0;
 }
 
+// The reference's Tensor<double>::multiply with batch modes
+// (contract.hpp:286-367): A's modes batchA[0..nb) are matched with B's
+// batchB and kept in the output, ctrA with ctrB are contracted. Its output
+// tensor's nonzeros (coordinates: batch, A external, B external) are copied
+// to malloc'ed arrays (free with ref_free). Shapes are inferred from the data
+// by the reference itself (IndexedTensor calls _infer_shape).
+int ref_multiply_modes(int32_t ordA, int64_t nnzA, const int32_t *cA, const double *vA, const int32_t *maxA,
+                       int32_t ordB, int64_t nnzB, const int32_t *cB, const double *vB, const int32_t *maxB,
+                       const int32_t *ctrA, const int32_t *ctrB, int32_t k, const int32_t *batchA,
+                       const int32_t *batchB, int32_t nb, int64_t *n_out, int32_t **out_coords,
+                       int32_t *out_order, double **values) {
+  if (nnzA < 1 || nnzB < 1) return 1;
+  std::vector<int> sa, sb;
+  Tensor<double> *a = make_tensor(ordA, nnzA, cA, vA, maxA, sa);
+  Tensor<double> *b = make_tensor(ordB, nnzB, cB, vB, maxB, sb);
+  CoOrdinate lc(std::vector<int>(ctrA, ctrA + k)), rc(std::vector<int>(ctrB, ctrB + k));
+  CoOrdinate lb(std::vector<int>(batchA, batchA + nb)), rb(std::vector<int>(batchB, batchB + nb));
+  Tensor<double> res = a->multiply<double, double>(*b, lc, lb, rc, rb);
+  auto &nz = res.get_nonzeros();
+  const int d = ordA + ordB - 2 * k - nb;
+  *out_order = d;
+  *n_out = int64_t(nz.size());
+  *values = (double *)malloc(sizeof(double) * (nz.size() + 1));
+  *out_coords = (int32_t *)malloc(sizeof(int32_t) * (nz.size() * size_t(d) + 1));
+  for (size_t i = 0; i < nz.size(); i++) {
+    (*values)[i] = nz[i].get_data();
+    for (int m = 0; m < d; m++) (*out_coords)[i * d + m] = nz[i].get_coords().get_index(m);
+  }
+  delete a;
+  delete b;
+  return 0;
+}
+
 void ref_free(void *p) { free(p); }
 
 }  // extern "C"

@@ -3,15 +3,22 @@
 Run where the reference sources are present (it builds oracle/_ref with
 `make -C oracle ref`):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [fastcc | modes]
 
-Each fixture stores the seeded inputs and the reference's output triples
+Each fastcc fixture stores the seeded inputs and the reference's output triples
 (A external linear index, B external linear index, value) as produced by the
 reference's tile-pair loop with the recording accumulator of
 oracle/ref_harness.cpp, sorted by (left, right). It also stores the entry
 count and sorted value multiset returned by the shipped
 TileAccumulator<double> path. Inputs come from a fixed numpy PCG64 stream
 and are stored in the fixture, so nothing is regenerated at test time.
+
+The modes_*.npz fixtures hold the reference's Tensor::multiply with batch
+modes (contract.hpp:286-367) on seeded inputs: its output coordinates (batch
+modes, A external, B external) sorted lexicographically, with their values.
+The reference infers each operand's shape from its nonzeros, so every operand
+holds its corner nonzero (every mode at its largest index), which makes the
+paired modes of the two operands share their extents.
 """
 import os
 import sys
@@ -83,7 +90,55 @@ def make(case):
     print(f"{name}: {len(order)} outputs, shipped {len(shipped['values'])} -> {os.path.basename(path)}")
 
 
+MODE_CASES = [
+    # name, seed, A extents, B extents, ctr_a, ctr_b, batch_a, batch_b, nnz_a, nnz_b
+    ("modes_bik_bkj", 31, [6, 7, 5], [6, 5, 8], [2], [1], [0], [0], 150, 120),
+    ("modes_two_ctr", 32, [4, 9, 3, 5], [5, 3, 4, 7], [1, 2], [2, 1], [3], [0], 300, 250),
+    ("modes_no_a_ext", 33, [5, 6], [6, 5], [1], [0], [0], [1], 25, 25),
+    ("modes_batched_outer", 34, [3, 4, 5], [5, 4, 3], [], [], [0, 1], [2, 1], 40, 50),
+    ("modes_mid_batch", 35, [8, 6, 4], [4, 6, 9], [1], [1], [2], [0], 120, 150),
+]
+
+
+def corner_tensor(rng, ext, n):
+    """n distinct uniform coordinates, the first at the corner (every mode at
+    its largest index)."""
+    space = int(np.prod(ext))
+    n = min(n, space)
+    lin = rng.choice(space, size=n, replace=False)
+    lin[0] = space - 1 if (space - 1) not in lin[1:] else lin[0]
+    if lin[0] != space - 1:
+        lin[np.nonzero(lin == space - 1)[0][0]] = lin[0]
+        lin[0] = space - 1
+    c = np.stack(np.unravel_index(lin, ext), axis=1).astype(np.int32).reshape(n, len(ext))
+    return c, rng.uniform(-1.0, 1.0, n)
+
+
+def make_modes(case):
+    name, seed, ea, eb, ca, cb, ba, bb, na, nb = case
+    eb = list(eb)
+    for x, y in list(zip(ca, cb)) + list(zip(ba, bb)):  # paired modes share their extent
+        eb[y] = ea[x]
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ac, av = corner_tensor(rng, ea, na)
+    bc, bv = corner_tensor(rng, eb, nb)
+    am, bm = ac.max(axis=0).astype(np.int32), bc.max(axis=0).astype(np.int32)
+    coords, vals = oracle.reference_multiply_modes(ac, av, am, bc, bv, bm, ca, cb, ba, bb)
+    order = np.lexsort(coords.T[::-1]) if coords.shape[0] and coords.shape[1] else np.arange(len(vals))
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(
+        path, a_coords=ac, a_vals=av, a_max=am, b_coords=bc, b_vals=bv, b_max=bm,
+        ctr_a=np.asarray(ca, np.int32), ctr_b=np.asarray(cb, np.int32), batch_a=np.asarray(ba, np.int32),
+        batch_b=np.asarray(bb, np.int32), coords=coords[order], values=vals[order])
+    print(f"{name}: {len(vals)} outputs -> {os.path.basename(path)}")
+
+
 if __name__ == "__main__":
     oracle.build(ref=True)
-    for c in CASES:
-        make(c)
+    which = sys.argv[1] if len(sys.argv) > 1 else "all"
+    if which in ("all", "fastcc"):
+        for c in CASES:
+            make(c)
+    if which in ("all", "modes"):
+        for c in MODE_CASES:
+            make_modes(c)

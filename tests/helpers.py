@@ -47,4 +47,10 @@ def load_golden(name):
 
 
 def golden_names():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+    """Fixtures of the reference's fastcc_multiply."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("modes_"))
+
+
+def mode_golden_names():
+    """Fixtures of the reference's Tensor::multiply with batch modes."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and f.startswith("modes_"))

@@ -1,12 +1,14 @@
 """GPU parity of the contraction with batch modes (fcc_contract_modes)
-against a dictionary restatement of the reference's Tensor::multiply
-(oracle.multiply_batch_modes), under the bar of tests/helpers.py."""
+against the reference's own Tensor::multiply (contract.hpp:286-367) recorded
+in tests/golden/modes_*.npz, and against a dictionary restatement of it
+(oracle.multiply_batch_modes, pinned to those fixtures on the CPU), under the
+bar of tests/helpers.py."""
 import numpy as np
 import pytest
 
 import fastcc_gpu as F
 import oracle
-from helpers import check_parity
+from helpers import check_parity, load_golden, mode_golden_names
 
 pytestmark = pytest.mark.gpu
 
@@ -78,3 +80,19 @@ def test_batch_modes_errors(ctx):
     big = F.Tensor(np.zeros((1, 7), np.int32), np.ones(1), np.zeros(7, np.int32))
     with pytest.raises(F.FccError):
         ctx.contract_modes(big, big, [], [], [0, 1], [0, 1])  # 7 + 2 modes > 8
+
+
+@pytest.mark.parametrize("name", mode_golden_names())
+@pytest.mark.parametrize("opts", [{}, {"accumulator": F.ACC_HASH}, {"products_per_item": 5}])
+def test_batch_modes_match_reference_fixtures(ctx, name, opts):
+    g = load_golden(name)
+    A = F.Tensor(g["a_coords"], g["a_vals"], g["a_max"])
+    B = F.Tensor(g["b_coords"], g["b_vals"], g["b_max"])
+    _, _, want_s = oracle.multiply_batch_modes(g["a_coords"], g["a_vals"], g["b_coords"], g["b_vals"], g["ctr_a"],
+                                               g["ctr_b"], g["batch_a"], g["batch_b"])
+    r = ctx.contract_modes(A, B, g["ctr_a"], g["ctr_b"], g["batch_a"], g["batch_b"], F.Options(**opts))
+    try:
+        c, v = r.to_numpy()
+    finally:
+        r.free()
+    check_parity(c, v, g["coords"], g["values"], want_s)

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import golden_names, load_golden, sort_rows
+from helpers import golden_names, load_golden, mode_golden_names, sort_rows
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -128,3 +128,30 @@ def test_batch_mode_restatement_reduces_to_fastcc_and_to_batched_slices():
     rows.sort()
     assert np.array_equal(c1, np.array([r[0] for r in rows], np.int64).reshape(len(rows), 3))
     assert np.allclose(v1, [r[1] for r in rows], rtol=1e-12)
+
+
+def _mode_args(g):
+    return (g["a_coords"], g["a_vals"], g["b_coords"], g["b_vals"], g["ctr_a"], g["ctr_b"], g["batch_a"],
+            g["batch_b"])
+
+
+@pytest.mark.parametrize("name", mode_golden_names())
+def test_batch_mode_restatement_matches_reference_fixture(name):
+    """oracle.multiply_batch_modes against the reference's own Tensor::multiply
+    (contract.hpp:286-367) recorded in tests/golden/modes_*.npz: the same
+    output coordinates, values within 1e-12 * S (the two sum in different
+    orders: the reference in its hash maps' iteration order)."""
+    g = load_golden(name)
+    c, v, s = oracle.multiply_batch_modes(*_mode_args(g))
+    assert np.array_equal(c, g["coords"].astype(np.int64))
+    assert np.all(np.abs(v - g["values"]) <= 1e-12 * np.maximum(np.abs(g["values"]), s))
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference sources not compiled here")
+@pytest.mark.parametrize("name", mode_golden_names())
+def test_batch_mode_fixture_reproduces_from_the_reference(name):
+    g = load_golden(name)
+    c, v = oracle.reference_multiply_modes(g["a_coords"], g["a_vals"], g["a_max"], g["b_coords"], g["b_vals"],
+                                           g["b_max"], g["ctr_a"], g["ctr_b"], g["batch_a"], g["batch_b"])
+    c, v = sort_rows(c, v)
+    assert np.array_equal(c, g["coords"]) and np.array_equal(v, g["values"])
