@@ -371,7 +371,9 @@ def run_sched_eval(model_path, reps=3):
 
 def run_sweep_batched(variants, reps):
     """The batched workload: each option set timed on one fcc_contract_batch
-    call (median of reps, per-phase times)."""
+    call (median of reps, per-phase times); the learned schedule uses the
+    package's cost model."""
+    import numpy as np
     import torch
 
     import fastcc_gpu as F
@@ -384,6 +386,8 @@ def run_sweep_batched(variants, reps):
     with F.Context(0) as ctx:
         for v in variants:
             opts = F.Options(timing=1, **v)
+            if opts.schedule == F.SCHED_LEARNED:
+                ctx.load_default_model()
             ph = []
             clk = Clocks(0)
             for rep in range(reps + 1):
@@ -396,7 +400,9 @@ def run_sweep_batched(variants, reps):
                     ph.append(ctx.timings())
             c = clk.stop()
             med = {k: statistics.median(p[k] for p in ph) for k in ph[0]}
-            print(json.dumps({"workload": "batched", "options": v, "outputs": n,
+            cls = np.bincount(ctx.sched_last_tiles(features=False, cost=False)["cls"], minlength=F.NUM_CLASSES)
+            ctx.sched_set_model(None)
+            print(json.dumps({"workload": "batched", "options": v, "outputs": n, "tiles_per_class": cls.tolist(),
                               "phases_ms": {k: round(x, 3) for k, x in med.items()}, "sm_mhz": c["sm_mhz"],
                               "reasons": c["reasons"]}), flush=True)
 

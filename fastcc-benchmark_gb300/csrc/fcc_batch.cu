@@ -62,12 +62,39 @@ __global__ void k_batch_pack(const PackSrc *__restrict__ src, int n, int order, 
   }
 }
 
+// Entries per instance (mode 0 of the batched result). Warps take contiguous
+// runs of entries: the tile kernels write each tile's entries together and a
+// tile belongs to one instance, so a run usually holds one instance, counted
+// in a register and added once when the run ends (one atomic per warp and
+// instance instead of one per 32 entries on a few hot counters).
 __global__ void k_instance_counts(const u32 *__restrict__ inst, i64 n, unsigned long long *counts) {
-  for (i64 i = i64(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += i64(gridDim.x) * blockDim.x) {
-    const u32 t = inst[i];
-    const u32 peers = __match_any_sync(__activemask(), t);
-    if ((threadIdx.x & 31) == u32(__ffs(peers) - 1)) atomicAdd(&counts[t], (unsigned long long)__popc(peers));
+  const u32 lane = threadIdx.x & 31;
+  const i64 nw = (i64(gridDim.x) * blockDim.x) >> 5, w = (i64(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const i64 per = (n + nw - 1) / nw, lo = w * per, hi = min(n, lo + per);
+  u32 cur = 0xFFFFFFFFu;       // the run's instance (warp-uniform)
+  unsigned long long cnt = 0;  // its entries so far (lane 0)
+  for (i64 base = lo; base < hi; base += 32) {
+    const i64 i = base + lane;
+    const bool in = i < hi;
+    const u32 t = in ? inst[i] : 0xFFFFFFFEu;  // lanes past the run match no instance
+    const u32 valid = __ballot_sync(kFull, in);  // every lane takes part in the vote
+    if (__all_sync(kFull, !in || t == cur)) {
+      if (lane == 0) cnt += __popc(valid);
+      continue;
+    }
+    if (lane == 0 && cnt) atomicAdd(&counts[cur], cnt);
+    cnt = 0;
+    // the last valid lane's instance continues as the run; other groups are added now
+    const u32 last = 31 - __clz(valid);
+    const u32 tl = __shfl_sync(kFull, t, last);
+    const u32 peers = __match_any_sync(kFull, t);
+    const bool leader = in && lane == u32(__ffs(peers) - 1);
+    if (leader && t != tl) atomicAdd(&counts[t], (unsigned long long)__popc(peers));
+    const u32 run = __shfl_sync(kFull, __popc(peers), last);
+    cur = tl;
+    if (lane == 0) cnt = run;
   }
+  if (lane == 0 && cnt) atomicAdd(&counts[cur], cnt);
 }
 
 struct Concat {
@@ -208,7 +235,7 @@ void contract_batch(Runtime *ctx, int n, const fcc_tensor *A, const fcc_tensor *
     dc = static_cast<unsigned long long *>(p);
     FCC_CUDA(cudaMemsetAsync(dc, 0, sizeof(unsigned long long) * size_t(n), ctx->stream));
     if (res->nnz > 0) {
-      k_instance_counts<<<grid_for(res->nnz, 256), 256, 0, ctx->stream>>>(res->d_coords, res->nnz, dc);
+      k_instance_counts<<<std::max(ctx->num_sms, 1) * 8, 256, 0, ctx->stream>>>(res->d_coords, res->nnz, dc);
       FCC_LAUNCH_CHECK();
     }
     FCC_CUDA(cudaMemcpyAsync(counts, dc, sizeof(unsigned long long) * size_t(n), cudaMemcpyDeviceToHost,

@@ -350,6 +350,7 @@ struct ClassTable {
   int forced;     // >= 0: every tile takes this class
   int fill_log2;  // rule: dense only when multiply-adds >= area >> fill_log2 (0: whenever it fits)
   float override_log2;  // learned: leave the rule's class only for a class predicted cheaper by this (log2)
+  float dense_switch_log2;  // learned, between the two dense classes (same tile, other kernel)
 };
 
 __device__ __forceinline__ u64 tile_area(const u32 *nrows, const u32 *lb, u64 LB, u32 t) {
@@ -382,15 +383,25 @@ __global__ void k_tile_class(const u32 *__restrict__ ntiles_p, i64 nmax, const u
         c = FCC_CLASS_DENSE;
       } else {
         c = FCC_CLASS_HASH_L;
-        for (int k = FCC_NUM_CLASSES - 1; k > FCC_CLASS_HASH_L; k--)
+        for (int k = FCC_CLASS_HASH_S; k > FCC_CLASS_HASH_L; k--)
           if (ct.enabled[k] && prod <= ct.pmax[k]) { c = k; break; }
         if (!ct.enabled[c]) c = FCC_CLASS_DENSE;  // only dense is enabled
       }
       if (pred) {  // the model overrides the rule where it predicts a clearly cheaper class
         const float *pt = pred + t * FCC_NUM_CLASSES;
-        float best = pt[c] - ct.override_log2;
-        for (int k = 0; k < FCC_NUM_CLASSES; k++)
-          if (ct.enabled[k] && pt[k] < best) { best = pt[k]; c = k; }
+        float bestv = 3.0e38f;
+        int pick = c;
+        for (int k = 0; k < FCC_NUM_CLASSES; k++) {
+          if (!ct.enabled[k] || k == c) continue;
+          // the other dense class runs the same tile with another kernel: a smaller margin
+          const float margin =
+              (c == FCC_CLASS_DENSE && k == FCC_CLASS_DENSE_FLAT) ? ct.dense_switch_log2 : ct.override_log2;
+          if (pt[k] < pt[c] - margin && pt[k] < bestv) {
+            bestv = pt[k];
+            pick = k;
+          }
+        }
+        c = pick;
       }
     }
     cls[t] = u32(c);
@@ -2396,6 +2407,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     hc[FCC_CLASS_DENSE].enabled = false;
     hc[FCC_CLASS_DENSE].threads = kTileThreads;
   }
+  hc[FCC_CLASS_DENSE_FLAT] = hc[FCC_CLASS_DENSE];  // the same tile, flat items
   {
     const u32 hs = hc[FCC_CLASS_HASH_L].slots;
     if (hs & (hs - 1)) throw Error{FCC_ERR_ARG, "hash_slots must be a power of two"};
@@ -2404,9 +2416,10 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   {
     u64 pd = opt.products_per_item > 0 ? u64(opt.products_per_item) : (u64(1) << 20);
     hc[FCC_CLASS_DENSE].pmax = std::min<u64>(pd, u64(kListMax) * kCtaRun);
+    hc[FCC_CLASS_DENSE_FLAT].pmax = hc[FCC_CLASS_DENSE].pmax;
     // an item's distinct outputs never exceed its multiply-adds, and the probe
     // loop covers the whole table: 3/4 of the slots bounds the load at 0.75
-    for (int c = FCC_CLASS_HASH_L; c < FCC_NUM_CLASSES; c++) {
+    for (int c = FCC_CLASS_HASH_L; c <= FCC_CLASS_HASH_S; c++) {
       const u64 cap = hc[c].slots / 4 * 3;
       hc[c].pmax = opt.products_per_item > 0 ? std::min<u64>(u64(opt.products_per_item), cap) : cap;
     }
@@ -2417,7 +2430,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (opt.schedule < 0 || opt.schedule >= FCC_SCHED_FORCE + FCC_NUM_CLASSES)
     throw Error{FCC_ERR_ARG, "bad schedule"};
   if (forced >= 0 && !hc[forced].enabled)
-    throw Error{FCC_ERR_ARG, forced == FCC_CLASS_DENSE
+    throw Error{FCC_ERR_ARG, (forced == FCC_CLASS_DENSE || forced == FCC_CLASS_DENSE_FLAT)
                                  ? "dense accumulator: B external span exceeds the shared-memory tile"
                                  : "the forced hash class is disabled by hash_slots or tile_threads"};
   if (custom_hash && forced < 0 && opt.accumulator == FCC_ACC_HASH) forced = FCC_CLASS_HASH_L;
@@ -2430,7 +2443,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (opt.fault_wait != 0 && opt.fault_wait != 1) throw Error{FCC_ERR_ARG, "fault_wait must be 0 or 1"};
   if (opt.dense_kernel < 0 || opt.dense_kernel > 3) throw Error{FCC_ERR_ARG, "dense_kernel must be 0, 1, 2 or 3"};
   if (opt.esc_group < 0) throw Error{FCC_ERR_ARG, "esc_group must be >= 0"};
-  const bool learned = forced < 0 && opt.schedule == FCC_SCHED_LEARNED && ctx->sched && ctx->sched->model;
+  bool learned = forced < 0 && opt.schedule == FCC_SCHED_LEARNED && ctx->sched && ctx->sched->model;
   const bool want_record = opt.timing == 2 && ctx->sched;
   // Row groups (batched contractions): dense tiles hold rows of one group,
   // group_tl rows of the group's own column span each.
@@ -2520,7 +2533,9 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   bool esc = false;
   int esc_mode = opt.hash_esc;
   if (esc_mode == 0)
-    esc_mode = ar.is_fixed() ? -1 : (forced >= 0 && forced != FCC_CLASS_DENSE) ? 1 : 2;
+    esc_mode = ar.is_fixed()                                                                  ? -1
+               : (forced >= 0 && forced != FCC_CLASS_DENSE && forced != FCC_CLASS_DENSE_FLAT) ? 1
+                                                                                                : 2;
   const bool esc_wanted = esc_mode > 0;
   // (not while recording per-tile costs: expanded tiles have no work items to time)
   if (esc_wanted && !want_record) {
@@ -2542,12 +2557,16 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   // when hash tiles are expanded (expansion beats a sparse dense tile), else
   // every tile that fits stays dense
   ctab.fill_log2 = opt.dense_fill_log2 > 0 ? opt.dense_fill_log2 : (opt.dense_fill_log2 == 0 && esc && esc_mode == 2) ? 2 : 0;
-  ctab.override_log2 = 0.32f;  // the model must predict at least 25% cheaper to leave the rule
+  ctab.override_log2 = 0.32f;     // the model must predict at least 25% cheaper to leave the rule
+  ctab.dense_switch_log2 = 0.074f;  // ... or 5% cheaper for the other dense class
+  // Without a dense class and with every hash tile expanded, the class of a
+  // tile changes nothing: the rule runs alone (no features, no predictions).
+  if (learned && !hc[FCC_CLASS_DENSE].enabled && esc && esc_mode == 2) learned = false;
   const u32 *lb_or_null = dense ? tile_lb : nullptr;
   float *feat = nullptr, *pred = nullptr;
   if (learned || want_record) {
     feat = ar.get_n<float>(size_t(NT) * FCC_SCHED_FEATURES);
-    tile_features(st, sc32(S_NTILES), u32(NT), tile_abeg, P, tile_nrows, lb_or_null, LB, feat);
+    tile_features(st, sc32(S_NTILES), u32(NT), tile_abeg, P, tile_nrows, lb_or_null, LB, feat, ctx->num_sms);
   }
   if (learned) {
     pred = ar.get_n<float>(size_t(NT) * FCC_NUM_CLASSES);
@@ -2828,35 +2847,38 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     if (opt.wait_polls > 0) da.wait_polls = opt.wait_polls;
     da.fault_wait = opt.fault_wait ? 1u : 0u;
     const int dmode = opt.dense_kernel == 0 ? kDefaultDenseMode : opt.dense_kernel;
-    const bool flat = dmode == 2;
     // Items of class c in wave w: a contiguous slice of the class's items.
     auto wave_items = [&](int c, int w, u32 &lo, u32 &n) {
       lo = u32(u64(ccount[c]) * u64(w) / u64(waves));
       n = u32(u64(ccount[c]) * u64(w + 1) / u64(waves)) - lo;
     };
-    auto run_dense = [&](int w) {
+    // The items of dense class c (FCC_CLASS_DENSE: dense_kernel's items;
+    // FCC_CLASS_DENSE_FLAT: flat items) in wave w.
+    auto run_dense = [&](int c, int w) {
       u32 lo = 0, n = 0;
-      wave_items(FCC_CLASS_DENSE, w, lo, n);
+      wave_items(c, w, lo, n);
       if (!n) return;
-      da.items = items + cbeg[FCC_CLASS_DENSE] + lo;
+      const int mode = c == FCC_CLASS_DENSE_FLAT ? 2 : dmode;
+      da.items = items + cbeg[c] + lo;
       da.nitems = n;
-      da.counter = counters + w * FCC_NUM_CLASSES + FCC_CLASS_DENSE;
-      da.item_cyc = item_cyc ? item_cyc + cbeg[FCC_CLASS_DENSE] + lo : nullptr;
-      const int threads = hc[FCC_CLASS_DENSE].threads;
-      size_t smem = class_smem(FCC_CLASS_DENSE, hot);
+      da.counter = counters + w * FCC_NUM_CLASSES + c;
+      da.item_cyc = item_cyc ? item_cyc + cbeg[c] + lo : nullptr;
+      da.stage_off = 0;
+      const int threads = hc[c].threads;
+      size_t smem = class_smem(c, hot);
       // phase 1's staging ring, when it fits beside the tile
       const size_t soff = (smem + 15) & ~size_t(15);
-      if (!flat && opt.dense_staging >= 0 && soff + kStageBytes <= dense_dyn_cap) {
+      if (mode != 2 && opt.dense_staging >= 0 && soff + kStageBytes <= dense_dyn_cap) {
         da.stage_off = u32(soff);
         smem = soff + kStageBytes;
       }
-      const DenseKernel kern = dmode == 2   ? dense_kernel_for<2>(sentinel, threads)
-                               : dmode == 3 ? dense_kernel_for<3>(sentinel, threads)
-                                            : dense_kernel_for<1>(sentinel, threads);
+      const DenseKernel kern = mode == 2   ? dense_kernel_for<2>(sentinel, threads)
+                               : mode == 3 ? dense_kernel_for<3>(sentinel, threads)
+                                           : dense_kernel_for<1>(sentinel, threads);
       FCC_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void *>(kern), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     int(smem)));
       const int grid = grid_tiles(ctx, reinterpret_cast<const void *>(kern), threads, smem, da.nitems,
-                                  &ctas_per_sm[FCC_CLASS_DENSE]);
+                                  &ctas_per_sm[c]);
       kern<<<grid, threads, smem, st>>>(da);
       FCC_LAUNCH_CHECK();
     };
@@ -2868,7 +2890,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
                         nsplit_h, src, colptr, LB, u32(grouped ? std::max<u64>(TL, 2) : TL), 0u, hot, hoff_t,
                         hsz_t, gkeys, gvals, o, dec,
                         ctx->d_err, nullptr, merge_cyc};
-      for (int c = FCC_CLASS_HASH_L; c < FCC_NUM_CLASSES && w >= 0; c++) {
+      for (int c = FCC_CLASS_HASH_L; c <= FCC_CLASS_HASH_S && w >= 0; c++) {
         u32 lo = 0, n = 0;
         wave_items(c, w, lo, n);
         if (!n) continue;
@@ -2930,7 +2952,8 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       FCC_CUDA(cudaEventRecord(ctx->wave_ev[w], st));
     };
     for (int w = 0; w < waves; w++) {
-      run_dense(w);
+      run_dense(FCC_CLASS_DENSE, w);
+      run_dense(FCC_CLASS_DENSE_FLAT, w);
       if (colb32) run_hash(static_cast<const u32 *>(colB), w);
       else run_hash(static_cast<const u64 *>(colB), w);
       if (stream_out) snapshot(w);

@@ -144,7 +144,7 @@ struct SchedIo {
 
 // fcc_sched.cu: per-tile features, predicted class costs, measured tile costs.
 void tile_features(cudaStream_t st, const u32 *ntiles_p, u32 nmax, const u32 *abeg, const u64 *P, const u32 *nrows,
-                   const u32 *lb, u64 LB, float *feat);
+                   const u32 *lb, u64 LB, float *feat, int num_sms);
 void predict_costs(cudaStream_t st, const u32 *ntiles_p, u32 nmax, const float *feat, const float *model,
                    float *pred);
 void tile_costs(cudaStream_t st, u32 ntiles, const u32 *corder, const u32 *cls, const u32 *item_off,

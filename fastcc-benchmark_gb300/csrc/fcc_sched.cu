@@ -5,7 +5,8 @@
 // tile, and every class computes the same sums.
 //
 // Model layout (include/fastcc_gpu.h): mean[12] scale[12] W1[12][64] b1[64]
-// W2[64][64] b2[64] W3[64][4] b3[4], row-major (input index first).
+// W2[64][64] b2[64] W3[64][FCC_NUM_CLASSES] b3[FCC_NUM_CLASSES], row-major
+// (input index first).
 
 #include <algorithm>
 #include <cmath>
@@ -20,56 +21,112 @@ namespace {
 
 constexpr int kF = FCC_SCHED_FEATURES;  // 12
 constexpr int kH = FCC_SCHED_HIDDEN;    // 64
-constexpr int kO = FCC_NUM_CLASSES;     // 4
+constexpr int kO = FCC_NUM_CLASSES;
 constexpr int kMean = 0, kScale = kF, kW1 = 2 * kF, kB1 = kW1 + kF * kH, kW2 = kB1 + kH, kB2 = kW2 + kH * kH,
               kW3 = kB2 + kH, kB3 = kW3 + kH * kO, kTotal = kB3 + kO;
 static_assert(kTotal == FCC_SCHED_MODEL_FLOATS, "model layout");
 constexpr int kTrain0 = kW1;  // trainable parameters start after mean and scale
 
-// ---- per-tile features (one warp per tile) ----
-__global__ void k_tile_features(const u32 *__restrict__ ntiles_p, u32 nmax, const u32 *__restrict__ abeg,
-                                const u64 *__restrict__ P, const u32 *__restrict__ nrows, const u32 *__restrict__ lb,
-                                u64 LB, float *__restrict__ feat) {
+// ---- per-tile features ----
+//
+// Two passes. k_tile_sums: warps take contiguous runs of A entries (tiles are
+// contiguous runs of entries, so a warp sees few tiles), sum per tile the
+// multiply-adds of entries whose B segment is short (< 64), medium or long
+// (>= 1024) and the longest segment, in registers while the tile lasts, and
+// add them into the tile's row of `feat` (its first 32 bytes, as four u64)
+// with one set of atomics per tile and warp. A tile of a million entries is
+// shared by many warps instead of one. k_tile_features then turns each row
+// into the 12 FP32 features in place. Integer sums and FP32 logarithms: FP64
+// issues at 1/64 of FP32 on this GPU.
+constexpr int kRowU64 = kF / 2;  // a feature row holds 12 floats = 6 u64
+
+__device__ __forceinline__ u32 tile_of(const u32 *__restrict__ abeg, u32 ntiles, u32 e) {
+  u32 lo = 0, hi = ntiles;  // last tile t with abeg[t] <= e
+  while (hi - lo > 1) {
+    const u32 mid = (lo + hi) >> 1;
+    if (abeg[mid] <= e) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_tile_sums(const u32 *__restrict__ ntiles_p, u32 nmax, const u32 *__restrict__ abeg,
+                            const u64 *__restrict__ P, unsigned long long *__restrict__ acc) {
   const u32 ntiles = min(*ntiles_p, nmax);
+  if (ntiles == 0) return;
   const u32 lane = threadIdx.x & 31;
-  const u32 wstride = (gridDim.x * blockDim.x) >> 5;
-  for (u32 t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntiles; t += wstride) {
-    const u32 e0 = abeg[t], e1 = abeg[t + 1];
-    // integer sums and FP32 logarithms: FP64 issues at 1/64 of FP32 on this
-    // GPU, and a lane-0 FP64 tail per tile cost more than the whole plan
-    u64 sl = 0, sw = 0, sc = 0, mx = 0;
-    for (u32 e = e0 + lane; e < e1; e += 32) {
-      const u64 len = P[e + 1] - P[e];
-      if (len < 64) sl += len;
-      else if (len < 1024) sw += len;
-      else sc += len;
-      mx = max(mx, len);
-    }
+  const u64 nw = (u64(gridDim.x) * blockDim.x) >> 5, w = (u64(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const u32 e_first = abeg[0], e_last = abeg[ntiles];
+  const u64 per = (u64(e_last - e_first) + nw - 1) / nw;
+  const u64 lo64 = u64(e_first) + w * per;
+  if (lo64 >= e_last) return;
+  const u32 lo = u32(lo64), hi = u32(lo64 + per < u64(e_last) ? lo64 + per : u64(e_last));
+  u32 t = tile_of(abeg, ntiles, lo), tend = abeg[t + 1];
+  u64 sl = 0, sw = 0, sc = 0, mx = 0;  // this lane's part of tile t
+  auto flush = [&]() {
     for (int o = 16; o; o >>= 1) {
       sl += __shfl_xor_sync(kFull, (unsigned long long)sl, o);
       sw += __shfl_xor_sync(kFull, (unsigned long long)sw, o);
       sc += __shfl_xor_sync(kFull, (unsigned long long)sc, o);
       mx = max(mx, (u64)__shfl_xor_sync(kFull, (unsigned long long)mx, o));
     }
-    if (lane == 0) {
-      const u64 prodi = P[e1] - P[e0];
-      const float prod = float(prodi), nent = float(e1 - e0), rows = float(nrows[t]);
-      const float span = float(lb ? u64(lb[t]) : LB), area = rows * span;
-      const float pd = prodi > 0 ? prod : 1.f;
-      float *f = feat + size_t(t) * kF;
-      f[0] = log2f(1.f + prod);
-      f[1] = log2f(1.f + nent);
-      f[2] = log2f(rows);
-      f[3] = log2f(span);
-      f[4] = log2f(area);
-      f[5] = fminf(prod, area) / area;
-      f[6] = float(sl) / pd;
-      f[7] = float(sw) / pd;
-      f[8] = float(sc) / pd;
-      f[9] = log2f(1.f + prod / fmaxf(nent, 1.f));
-      f[10] = log2f(1.f + float(mx));
-      f[11] = log2f(1.f + prod / rows);
+    if (lane == 0 && (sl | sw | sc | mx)) {
+      unsigned long long *a = acc + size_t(t) * kRowU64;
+      if (sl) atomicAdd(&a[0], (unsigned long long)sl);
+      if (sw) atomicAdd(&a[1], (unsigned long long)sw);
+      if (sc) atomicAdd(&a[2], (unsigned long long)sc);
+      atomicMax(&a[3], (unsigned long long)mx);
     }
+    sl = sw = sc = mx = 0;
+  };
+  for (u32 base = lo; base < hi; base += 32) {
+    const u32 e = base + lane;
+    const bool in = e < hi;
+    const u64 len = in ? P[e + 1] - P[e] : 0;
+    bool left = in;  // not yet added to a tile
+    for (;;) {
+      if (left && e < tend) {
+        if (len < 64) sl += len;
+        else if (len < 1024) sw += len;
+        else sc += len;
+        mx = max(mx, len);
+        left = false;
+      }
+      const u32 rest = __ballot_sync(kFull, left);
+      if (!rest) break;
+      flush();  // tile t ends inside this round: move on to the next lane's tile
+      const u32 enext = __shfl_sync(kFull, e, __ffs(rest) - 1);
+      t = tile_of(abeg, ntiles, enext);
+      tend = abeg[t + 1];
+    }
+  }
+  flush();
+}
+
+__global__ void k_tile_features(const u32 *__restrict__ ntiles_p, u32 nmax, const u32 *__restrict__ abeg,
+                                const u64 *__restrict__ P, const u32 *__restrict__ nrows, const u32 *__restrict__ lb,
+                                u64 LB, float *__restrict__ feat) {
+  const u32 ntiles = min(*ntiles_p, nmax);
+  for (u32 t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
+    float *f = feat + size_t(t) * kF;
+    const unsigned long long *a = reinterpret_cast<const unsigned long long *>(f);
+    const u64 sl = a[0], sw = a[1], sc = a[2], mx = a[3];
+    const u32 e0 = abeg[t], e1 = abeg[t + 1];
+    const u64 prodi = P[e1] - P[e0];
+    const float prod = float(prodi), nent = float(e1 - e0), rows = float(nrows[t]);
+    const float span = float(lb ? u64(lb[t]) : LB), area = rows * span;
+    const float pd = prodi > 0 ? prod : 1.f;
+    f[0] = log2f(1.f + prod);
+    f[1] = log2f(1.f + nent);
+    f[2] = log2f(rows);
+    f[3] = log2f(span);
+    f[4] = log2f(area);
+    f[5] = fminf(prod, area) / area;
+    f[6] = float(sl) / pd;
+    f[7] = float(sw) / pd;
+    f[8] = float(sc) / pd;
+    f[9] = log2f(1.f + prod / fmaxf(nent, 1.f));
+    f[10] = log2f(1.f + float(mx));
+    f[11] = log2f(1.f + prod / rows);
   }
 }
 
@@ -290,10 +347,13 @@ void check_rows(const void *X, int64_t n) {
 }  // namespace
 
 void tile_features(cudaStream_t st, const u32 *ntiles_p, u32 nmax, const u32 *abeg, const u64 *P, const u32 *nrows,
-                   const u32 *lb, u64 LB, float *feat) {
+                   const u32 *lb, u64 LB, float *feat, int num_sms) {
   if (nmax == 0) return;
-  const u32 blocks = std::min<u32>((nmax + 7) / 8, 65535u);  // 8 warps per block, a warp per tile
-  k_tile_features<<<blocks, 256, 0, st>>>(ntiles_p, nmax, abeg, P, nrows, lb, LB, feat);
+  FCC_CUDA(cudaMemsetAsync(feat, 0, sizeof(float) * size_t(nmax) * kF, st));
+  k_tile_sums<<<std::max(num_sms, 1) * 8, 256, 0, st>>>(ntiles_p, nmax, abeg, P,
+                                                         reinterpret_cast<unsigned long long *>(feat));
+  FCC_LAUNCH_CHECK();
+  k_tile_features<<<grid_rows(nmax, 256), 256, 0, st>>>(ntiles_p, nmax, abeg, P, nrows, lb, LB, feat);
   FCC_LAUNCH_CHECK();
 }
 

@@ -22,11 +22,11 @@ ACC_AUTO, ACC_DENSE, ACC_HASH = 0, 1, 2
 RADIX_PER_OPERAND, RADIX_SHARED = 0, 1
 DENSE_AUTO, DENSE_BITMASK, DENSE_SENTINEL = 0, 1, 2
 PHASES = ["upload", "index", "plan", "contract", "merge", "total"]
-CLASS_DENSE, CLASS_HASH_L, CLASS_HASH_M, CLASS_HASH_S = 0, 1, 2, 3
-NUM_CLASSES = 4
+CLASS_DENSE, CLASS_HASH_L, CLASS_HASH_M, CLASS_HASH_S, CLASS_DENSE_FLAT = 0, 1, 2, 3, 4
+NUM_CLASSES = 5
 SCHED_RULE, SCHED_LEARNED, SCHED_FORCE = 0, 1, 2
 SCHED_FEATURES, SCHED_HIDDEN = 12, 64
-SCHED_MODEL_FLOATS = 2 * 12 + 12 * 64 + 64 + 64 * 64 + 64 + 64 * 4 + 4
+SCHED_MODEL_FLOATS = 2 * 12 + 12 * 64 + 64 + 64 * 64 + 64 + 64 * NUM_CLASSES + NUM_CLASSES
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "hash accumulator full",
           4: "bounded device wait timed out", 5: "CUDA error", 6: "index space exceeds 64 bits",
           7: "no usable sm_103 device", 8: "output buffer too small"}

@@ -6,7 +6,7 @@ benchmark workloads, at reduced sizes) every enabled tile class is forced in
 turn with opts.timing = 2. The tile structure does not depend on the class,
 so the runs give, for each tile, its features and its measured cost in every
 class: one record (x = 12 features, y = log2 cost per class, m = 1 where the
-class ran the tile). The MLP (12 -> 64 -> 64 -> 4) is trained with the
+class ran the tile). The MLP (12 -> 64 -> 64 -> 5) is trained with the
 library's own FP32 kernels (fcc_mlp_train) and written as a flat float32
 file of FCC_SCHED_MODEL_FLOATS values.
 
@@ -113,13 +113,28 @@ def regrets(pred, costs, mask):
     """Over the tiles where every hash class was measured: the measured cost
     of the classes the model picks, and of each single class run on every
     tile, relative to the per-tile best."""
-    sel = mask[:, 1:].sum(axis=1) == mask.shape[1] - 1
+    hash_cls = [F.CLASS_HASH_L, F.CLASS_HASH_M, F.CLASS_HASH_S]
+    sel = mask[:, hash_cls].sum(axis=1) == len(hash_cls)
     p = np.where(mask > 0, pred, np.inf)[sel]
     c = np.where(mask > 0, costs, np.inf)[sel]
     best = c.min(axis=1).sum()
     learned = float(c[np.arange(len(c)), p.argmin(axis=1)].sum() / best)
     uniform = {int(k): float(c[:, k].sum() / best) for k in range(c.shape[1]) if np.isfinite(c[:, k]).all()}
     return learned, uniform
+
+
+def dense_regrets(pred, costs, mask):
+    """Over the tiles where both dense classes were measured: the measured
+    cost of the model's pick between them, and of each alone, relative to the
+    per-tile best of the two."""
+    d = [F.CLASS_DENSE, F.CLASS_DENSE_FLAT]
+    sel = mask[:, d].sum(axis=1) == len(d)
+    if not sel.any():
+        return None
+    p, c = pred[sel][:, d], costs[sel][:, d]
+    best = c.min(axis=1).sum()
+    return {"learned": float(c[np.arange(len(c)), p.argmin(axis=1)].sum() / best),
+            "two_phase": float(c[:, 0].sum() / best), "flat": float(c[:, 1].sum() / best), "tiles": int(sel.sum())}
 
 
 def main():
@@ -164,7 +179,8 @@ def main():
     summary = {"records": int(X.shape[0]), "train": int(len(tr)), "val": int(len(val)),
                "loss_init": loss0, "loss_train": loss, "loss_val": vloss,
                "val_cost_vs_per_tile_best": {"learned": regrets(pv, C, M[val])[0],
-                                              "single_class": regrets(pv, C, M[val])[1]},
+                                              "single_class": regrets(pv, C, M[val])[1],
+                                              "dense_classes": dense_regrets(pv, C, M[val])},
                "record_s": t1 - t0, "train_s": t2 - t1, "contractions": names}
     model.astype(np.float32).tofile(args.out)
     print(json.dumps(summary), flush=True)

@@ -147,21 +147,28 @@ typedef struct fcc_options {
 
 /* Tile classes: every output tile runs in one of them. The hash classes
  * differ in table size and CTA shape: the small ones run several CTAs per SM
- * so that small tiles overlap their barriers and memory latency. */
+ * so that small tiles overlap their barriers and memory latency. The two
+ * dense classes share the tile; they differ in how the CTA runs its
+ * multiply-adds (dense_kernel): the rule uses FCC_CLASS_DENSE only, the
+ * learned schedule picks between the two per tile. */
 enum {
-  FCC_CLASS_DENSE = 0,   /* shared-memory dense tile, 640 threads (tile_threads) */
-  FCC_CLASS_HASH_L = 1,  /* hash, 8192 slots, 1024 threads (tile_threads), one CTA per SM */
-  FCC_CLASS_HASH_M = 2,  /* hash, 4096 slots, 256 threads */
-  FCC_CLASS_HASH_S = 3,  /* hash, 2048 slots, 128 threads */
-  FCC_NUM_CLASSES = 4
+  FCC_CLASS_DENSE = 0,       /* shared-memory dense tile, 640 threads (tile_threads), dense_kernel */
+  FCC_CLASS_HASH_L = 1,      /* hash, 8192 slots, 1024 threads (tile_threads), one CTA per SM */
+  FCC_CLASS_HASH_M = 2,      /* hash, 4096 slots, 256 threads */
+  FCC_CLASS_HASH_S = 3,      /* hash, 2048 slots, 128 threads */
+  FCC_CLASS_DENSE_FLAT = 4,  /* the dense tile with flat items (dense_kernel 2) */
+  FCC_NUM_CLASSES = 5
 };
 
 typedef enum fcc_schedule {
   FCC_SCHED_RULE = 0,     /* dense when the tile fits it (see dense_fill_log2), else the smallest
                              hash table that holds the tile without splitting it */
   FCC_SCHED_LEARNED = 1,  /* the rule's class, overridden per tile where the context's cost model
-                             (fcc_sched_set_model) predicts another class at least 25% cheaper;
-                             FCC_SCHED_RULE when no model is set */
+                             (fcc_sched_set_model) predicts another class at least 25% cheaper
+                             (between the two dense classes: at least 5% cheaper); the rule
+                             alone, without features or predictions, when no model is set or
+                             no tile has a choice (no dense class and every hash tile
+                             expanded) */
   FCC_SCHED_FORCE = 2     /* FCC_SCHED_FORCE + class: one class for every tile */
 } fcc_schedule;
 
@@ -347,7 +354,8 @@ int fcc_autotune_batch(fcc_ctx *ctx, int32_t n, const fcc_tensor *A, const fcc_t
  * in each class (log2 of SM cycles); a tile takes the class of lowest
  * prediction. Model layout (FCC_SCHED_MODEL_FLOATS floats): mean[12],
  * scale[12] (inputs are standardised as (x - mean) * scale), W1[12][64],
- * b1[64], W2[64][64], b2[64], W3[64][4], b3[4]. Features of a tile, in
+ * b1[64], W2[64][64], b2[64], W3[64][FCC_NUM_CLASSES], b3[FCC_NUM_CLASSES].
+ * Features of a tile, in
  * order: log2(1 + multiply-adds), log2(1 + A entries), log2(rows),
  * log2(column span), log2(area = rows x span), estimated fill
  * min(multiply-adds, area) / area, the fractions of its multiply-adds whose
@@ -357,7 +365,7 @@ int fcc_autotune_batch(fcc_ctx *ctx, int32_t n, const fcc_tensor *A, const fcc_t
  */
 #define FCC_SCHED_FEATURES 12
 #define FCC_SCHED_HIDDEN 64
-#define FCC_SCHED_MODEL_FLOATS (2 * 12 + 12 * 64 + 64 + 64 * 64 + 64 + 64 * 4 + 4)
+#define FCC_SCHED_MODEL_FLOATS (2 * 12 + 12 * 64 + 64 + 64 * 64 + 64 + 64 * 5 + 5)
 /* Installs (copies to the device) or, with model NULL, removes the model. */
 int fcc_sched_set_model(fcc_ctx *ctx, const float *model, int64_t n);
 /* Per-tile record of the last contraction on ctx: features (ntiles x 12;

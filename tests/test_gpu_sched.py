@@ -177,8 +177,8 @@ def test_learned_schedule_mixes_classes_and_records_tiles(ctx):
     scale[:] = 1.0
     W1[0, 0] = 1.0            # h1_0 = log2(1 + multiply-adds)
     W2[0, 0] = 1.0            # h2_0 = h1_0
-    W3[0, 1:] = 1.0           # predicted log2 cost of every hash class: log2(1 + multiply-adds)
-    b3[:] = [9.0, 0.0, 0.0, 0.0]  # dense: 9
+    W3[0, 1:4] = 1.0          # predicted log2 cost of every hash class: log2(1 + multiply-adds)
+    b3[:] = [9.0, 0.0, 0.0, 0.0, 20.0]  # dense: 9; flat dense items: never
     ctx.sched_set_model(m)
     try:
         r = ctx.contract(w["a"], w["b"], w["ctr_a"], w["ctr_b"], F.Options(schedule=F.SCHED_LEARNED, timing=2))
@@ -248,7 +248,7 @@ def test_learned_schedule_picks_one_class_when_mixing_does_not_pay(ctx):
     m = np.zeros(F.SCHED_MODEL_FLOATS, np.float32)
     mean, scale, W1, b1, W2, b2, W3, b3 = _split(m)
     scale[:] = 1.0
-    b3[:] = [3.0, 2.0, 1.0, 1.05]  # constant predictions: the medium hash class is cheapest everywhere
+    b3[:] = [3.0, 2.0, 1.0, 1.05, 3.5]  # constant predictions: the medium hash class is cheapest everywhere
     ctx.sched_set_model(m)
     try:
         r = ctx.contract(w["a"], w["b"], w["ctr_a"], w["ctr_b"],
@@ -258,3 +258,30 @@ def test_learned_schedule_picks_one_class_when_mixing_does_not_pay(ctx):
     finally:
         ctx.sched_set_model(None)
     assert np.all(cls == F.CLASS_HASH_M)
+
+
+def test_learned_schedule_switches_dense_tiles_to_flat_items_past_the_margin(ctx):
+    """Between the two dense classes (same tile, two kernels) the model needs
+    a 5% lower prediction (log2 0.074); a 3.4% lower one keeps the rule's
+    class. Either way the result is the oracle's."""
+    w = workloads.zipf3(seed=25, nnz=80_000, dims=(2_000, 2_000, 50_000))
+    a, b = w["a"], w["b"]
+    o = oracle.fastcc_multiply(a.coords, a.values, a.max_index, b.coords, b.values, b.max_index, w["ctr_a"],
+                               w["ctr_b"], want_abs=True)
+    for flat_cost, want_cls in ((4.95, F.CLASS_DENSE), (4.9, F.CLASS_DENSE_FLAT)):
+        m = np.zeros(F.SCHED_MODEL_FLOATS, np.float32)
+        mean, scale, W1, b1, W2, b2, W3, b3 = _split(m)
+        scale[:] = 1.0
+        b3[:] = [5.0, 9.0, 9.0, 9.0, flat_cost]
+        ctx.sched_set_model(m)
+        try:
+            r = ctx.contract(a, b, w["ctr_a"], w["ctr_b"], F.Options(schedule=F.SCHED_LEARNED, dense_fill_log2=-1))
+            try:
+                c, v = r.to_numpy()
+            finally:
+                r.free()
+            cls = ctx.sched_last_tiles(features=False, cost=False)["cls"]
+        finally:
+            ctx.sched_set_model(None)
+        assert np.all(cls == want_cls), np.bincount(cls, minlength=F.NUM_CLASSES)
+        check_parity(c, v, o["coords"], o["values"], o["abs_sum"])
