@@ -378,7 +378,7 @@ def run_sweep_batched(variants, reps):
 
     import fastcc_gpu as F
     import workloads
-    inst = workloads.batched(seed=1, count=256)
+    inst = workloads.batched(seed=int(os.environ.get("FCC_SWEEP_BATCH_SEED", "1")), count=256)
     cuda = lambda t: F.Tensor(torch.from_numpy(t.coords).cuda(), torch.from_numpy(t.values).cuda(), t.max_index)
     As = [cuda(w["a"]) for w in inst]
     Bs = [cuda(w["b"]) for w in inst]

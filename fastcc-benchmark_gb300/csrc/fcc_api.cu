@@ -341,6 +341,8 @@ void autotune(fcc_ctx *ctx, const std::string &sig, const fcc_options &base, int
       best_o = o;
     }
   }
+  // the trials' workspace (the largest of every candidate's) stays out of later calls
+  ctx->arena.shrink(ctx->stream);
   if (best_t == 1e300) throw fcc::Error{FCC_ERR_ARG, "no schedule can run this problem"};
   best_o.timing = base.timing;
   ctx->tuned[sig] = {best_o, best_t};

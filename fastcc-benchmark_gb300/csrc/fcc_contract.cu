@@ -590,7 +590,7 @@ __global__ void k_apply_colmap(ColT *__restrict__ col, i64 n, const u32 *__restr
 //  * shorter entries go one per lane, up to 32 at once, so rows made of many
 //    rare keys (hub rows of Zipf tensors) keep every lane busy.
 
-constexpr int kDefaultDenseMode = 1;  // fcc_options.dense_kernel 0 means this
+constexpr int kDefaultDenseMode = 3;  // fcc_options.dense_kernel 0 means this
 constexpr int kTileThreads = 640;   // dense tiles by default (20 warps in 96 registers); 512, 768, 1024 on request
 constexpr int kMergeThreads = 512;  // merges of split tiles
 constexpr int kBatch = 4;
@@ -1000,7 +1000,7 @@ __device__ __forceinline__ u32 window_count_le(u64 endk, u64 x) {  // window end
 // two-phase item ran them); kNoSkip runs every entry.
 template <class Add>
 __device__ void flat_chunks(const ProdSrc &s, const u32 *__restrict__ colB, u32 ahi, u64 p0, u64 p1, u32 LB,
-                            ItemPlan &pl, Add &add, u64 skip) {
+                            ItemPlan &pl, Add &add, u64 skip, bool add_tile) {
   const u32 lane = threadIdx.x & 31;
   const u64 chunk = pl.chunk;
   const u32 nch = pl.nchunk;
@@ -1058,7 +1058,7 @@ __device__ void flat_chunks(const ProdSrc &s, const u32 *__restrict__ colB, u32 
               valid |= 1u << r;
             }
           }
-          add.batch(key, m, x, valid, true, true);
+          add.batch(key, m, x, valid, true, true, add_tile);
           q = bend;
           if (q == ec) jc++;
         } else {  // the batch crosses entries: each lane finds its own
@@ -1086,7 +1086,7 @@ __device__ void flat_chunks(const ProdSrc &s, const u32 *__restrict__ colB, u32 
           for (int r = 0; r < kBatch; r++)
             if (((valid >> r) & 1u) && !aggregate_lanes(key[r], &m[r], &x[r])) valid &= ~(1u << r);
           __syncwarp();
-          add.batch(key, m, x, valid, false, true);
+          add.batch(key, m, x, valid, false, true, add_tile);
           q = bend;
           if (q < wend) jc = window_count_le(endk, q);
         }
@@ -1100,7 +1100,7 @@ template <class Add>
 __device__ void dense_item_flat(const ProdSrc &s, const u32 *__restrict__ colB, u32 ahi, u64 p0, u64 p1, u32 ea,
                                 u32 eb, u32 LB, ItemPlan &pl, Add &add) {
   build_item_plan(s.P, ea, eb, p0, p1, 256, pl);
-  flat_chunks(s, colB, ahi, p0, p1, LB, pl, add, kNoSkip);
+  flat_chunks(s, colB, ahi, p0, p1, LB, pl, add, kNoSkip, false);
 }
 
 // kFlat2: phase 2 runs flat (flat_chunks, the phase-1 entries left out)
@@ -1143,7 +1143,7 @@ __device__ void dense_item(const ProdSrc &s, const u32 *__restrict__ colB, u32 a
   }
   // phase 2
   if (kFlat2) {
-    flat_chunks(s, colB, ahi, p0, p1, LB, pl, add, u64(kCtaRun));
+    flat_chunks(s, colB, ahi, p0, p1, LB, pl, add, u64(kCtaRun), true);
     return;
   }
   const u64 chunk = pl.chunk;
@@ -1335,10 +1335,14 @@ struct DenseAdd {
   // (combined beforehand). plain_priv: the whole warp calls converged, so
   // its private hot-column copy, which no other warp touches, takes plain
   // read-modify-writes (rounds of different keys ordered by __syncwarp);
-  // otherwise it takes compare-and-swap like the shared tile.
+  // otherwise it takes compare-and-swap like the shared tile. add_tile: the
+  // shared tile takes the built-in FP64 atomic add of the product (a multiply
+  // and an atomic, no retry loop) instead of a compare-and-swap loop around
+  // one FMA; measured faster for the short entries of two-phase items (phase
+  // 2 run flat), slower for whole flat items.
   __device__ __forceinline__ void batch(const u32 (&key)[kBatch], const double (&m)[kBatch],
                                         const double (&x)[kBatch], u32 valid, bool distinct,
-                                        bool plain_priv) const {
+                                        bool plain_priv, bool add_tile = false) const {
 #pragma unroll
     for (int k = 0; k < kBatch; k++) {
       if ((valid >> k) & 1u) {
@@ -1348,7 +1352,8 @@ struct DenseAdd {
           else fma_shared(&priv[q], m[k], x[k]);
           if (!kSentinel) atomicOr(&pmask[q >> 5], 1u << (q & 31));
         } else {
-          fma_shared(&acc[q], m[k], x[k]);
+          if (add_tile) atomicAdd(&acc[q], m[k] * x[k]);
+          else fma_shared(&acc[q], m[k], x[k]);
           if (!kSentinel) atomicOr(&mask[q >> 5], 1u << (q & 31));
         }
       }
@@ -1594,7 +1599,7 @@ struct HashAdd {
   }
   __device__ __forceinline__ void batch(const u64 (&key)[kBatch], const double (&m)[kBatch],
                                         const double (&x)[kBatch], u32 valid, bool /*distinct*/,
-                                        bool /*plain_priv*/) const {
+                                        bool /*plain_priv*/, bool /*add_tile*/ = false) const {
 #pragma unroll
     for (int k = 0; k < kBatch; k++)
       if ((valid >> k) & 1u) (*this)(key[k], m[k], x[k]);
@@ -2539,8 +2544,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   const bool esc_wanted = esc_mode > 0;
   // (not while recording per-tile costs: expanded tiles have no work items to time)
   if (esc_wanted && !want_record) {
-    size_t fb = 0, tb = 0;
-    FCC_CUDA(cudaMemGetInfo(&fb, &tb));
+    const size_t fb = ar.available();
     const unsigned __int128 keyspace = (unsigned __int128)NT * esc_rows * LB;
     esc = ptotal <= 0xFFFFFFFFull && (unsigned __int128)ptotal * 56 <= fb / 2 && keyspace < ((unsigned __int128)1 << 64);
   }
@@ -2760,10 +2764,10 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   dec.narrow = (sa.span <= 0xFFFFFFFFull && sb.span <= 0xFFFFFFFFull) ? 1 : 0;
 
   // Output capacity: the planner's upper bound, limited to half of the free
-  // device memory; an overflow is detected on the device and retried once
-  // with the exact count (the cursor counts every reservation).
-  size_t free_b = 0, total_b = 0;
-  FCC_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  // device memory (the pool's unused memory included); an overflow is
+  // detected on the device and retried once with the exact count (the cursor
+  // counts every reservation).
+  const size_t free_b = ctx->arena.available();
   const u64 per_out = 8 + 4 * u64(out_order);
   const u64 budget = std::max<u64>(u64(free_b / 2) / per_out, 1 << 20);
   u64 cap = std::max<u64>(std::min(cap_total, budget), 1);
@@ -2846,7 +2850,11 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
                  item_cyc ? item_cyc + cbeg[FCC_CLASS_DENSE] : nullptr, 0u, merge_cyc};
     if (opt.wait_polls > 0) da.wait_polls = opt.wait_polls;
     da.fault_wait = opt.fault_wait ? 1u : 0u;
-    const int dmode = opt.dense_kernel == 0 ? kDefaultDenseMode : opt.dense_kernel;
+    // The rule's dense tiles run one kernel for every tile: dense_kernel, by
+    // default the two-phase items with a flat second phase. The learned
+    // schedule instead picks per tile between the two pure kernels, two-phase
+    // items (FCC_CLASS_DENSE) and flat items (FCC_CLASS_DENSE_FLAT).
+    const int dmode = opt.dense_kernel != 0 ? opt.dense_kernel : learned ? 1 : kDefaultDenseMode;
     // Items of class c in wave w: a contiguous slice of the class's items.
     auto wave_items = [&](int c, int w, u32 &lo, u32 &n) {
       lo = u32(u64(ccount[c]) * u64(w) / u64(waves));

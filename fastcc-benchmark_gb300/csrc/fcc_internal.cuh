@@ -115,6 +115,13 @@ class Arena {
   void *get(size_t bytes);     // 256-byte aligned, valid until the next begin()
   template <class T> T *get_n(size_t n) { return static_cast<T *>(get(sizeof(T) * (n ? n : 1))); }
   void release_all(cudaStream_t s);
+  // release_all, forget the high-water size and return the pool's unused
+  // memory to the device (after runs whose workspace says nothing of the
+  // next calls', such as the autotuner's trials)
+  void shrink(cudaStream_t s);
+  // Device memory a call can still allocate: free on the device plus what the
+  // pool holds unused.
+  size_t available() const;
   size_t high_water() const { return high_; }
   bool is_fixed() const { return fixed_; }
 

@@ -88,6 +88,26 @@ void Arena::release_all(cudaStream_t s) {
   used_ = total_used_ = 0;
 }
 
+void Arena::shrink(cudaStream_t s) {
+  if (fixed_) return;
+  release_all(s);
+  high_ = 0;
+  FCC_CUDA(cudaStreamSynchronize(s));
+  if (pool_) FCC_CUDA(cudaMemPoolTrimTo(pool_, 0));
+}
+
+size_t Arena::available() const {
+  size_t fb = 0, tb = 0;
+  FCC_CUDA(cudaMemGetInfo(&fb, &tb));
+  if (pool_) {
+    uint64_t reserved = 0, used = 0;
+    FCC_CUDA(cudaMemPoolGetAttribute(pool_, cudaMemPoolAttrReservedMemCurrent, &reserved));
+    FCC_CUDA(cudaMemPoolGetAttribute(pool_, cudaMemPoolAttrUsedMemCurrent, &used));
+    if (reserved > used) fb += size_t(reserved - used);
+  }
+  return fb;
+}
+
 // ----------------------------------------------------------------- scan ----
 
 namespace {

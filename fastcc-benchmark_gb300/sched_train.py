@@ -73,7 +73,8 @@ def record(ctx, pairs, ctr_a, ctr_b, batched, reps=2):
     split tiles)."""
     feats, costs, mask = None, None, None
     for c in range(F.NUM_CLASSES):
-        opts = F.Options(timing=2, schedule=F.SCHED_FORCE + c)
+        # the learned schedule's dense class runs two-phase items (dense_kernel 1)
+        opts = F.Options(timing=2, schedule=F.SCHED_FORCE + c, dense_kernel=1)
         acc = None
         try:
             for _ in range(reps):

@@ -138,10 +138,13 @@ typedef struct fcc_options {
                                  0 (default): off */
   int32_t dense_kernel;       /* how a dense tile runs its multiply-adds. 1: two phases (A entries
                                  with long B segments by the whole CTA through a bulk-copy ring
-                                 with plain read-modify-writes, the rest by warps with
-                                 compare-and-swap); 2: flat (warps take runs of consecutive
-                                 multiply-adds, one per lane, compare-and-swap updates).
-                                 0 (default): 1 */
+                                 with plain read-modify-writes, the rest by warps, windows of one
+                                 entry per lane, compare-and-swap updates); 2: flat (warps take
+                                 runs of consecutive multiply-adds, one per lane,
+                                 compare-and-swap updates); 3: two phases, the second run flat
+                                 with atomic adds. 0 (default): 3, except under the learned
+                                 schedule, whose FCC_CLASS_DENSE tiles run 1 (and whose
+                                 FCC_CLASS_DENSE_FLAT tiles run 2) */
   int32_t pad1;
 } fcc_options;
 

@@ -285,3 +285,75 @@ def test_learned_schedule_switches_dense_tiles_to_flat_items_past_the_margin(ctx
             ctx.sched_set_model(None)
         assert np.all(cls == want_cls), np.bincount(cls, minlength=F.NUM_CLASSES)
         check_parity(c, v, o["coords"], o["values"], o["abs_sum"])
+
+
+class _DevBuf:
+    def __init__(self, ptr, n, typestr):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False),
+                                         "version": 3, "strides": None}
+
+
+def _digest(r):
+    """Order-independent digest of a device result: entries, a hash sum of the
+    coordinates (mod 2^64) and the sum of the values."""
+    import torch
+    cptr, stride, vptr = r.device_pointers()
+    n = r.nnz
+    v = torch.as_tensor(_DevBuf(vptr, n, "<f8"), device="cuda")
+    h = torch.zeros(n, dtype=torch.int64, device="cuda")
+    for m in range(r.order):
+        c = torch.as_tensor(_DevBuf(cptr + 4 * m * stride, n, "<i4"), device="cuda").long()
+        h = h * 1000003 + c + 1
+    return n, int(h.sum().item()), float(v.sum().item()), float(v.abs().sum().item())
+
+
+def test_learned_schedule_gain_on_held_out_shapes(ctx):
+    """What the shipped cost model gains on seeds it was not trained on, in the
+    shapes of the two-mode and batched workloads: median total time of the
+    rule, of the autotuner's pick and of the learned schedule, identical
+    outputs required. Two-mode has no dense tile and expands every hash tile,
+    so the learned schedule runs the rule there; on the batch the model picks,
+    per dense tile, between two-phase and flat items (measured on seed 1:
+    105.9 ms against the rule's 109.8 ms). The bound asserted is loose
+    (timings on a shared machine); the times are printed (pytest -s)."""
+    import statistics
+
+    import torch
+    assert ctx.load_default_model()
+    ctx.sched_set_model(None)
+    dev = lambda t: F.Tensor(torch.from_numpy(t.coords).cuda(), torch.from_numpy(t.values).cuda(), t.max_index)
+    w = workloads.twomode(seed=101)
+    A = dev(w["a"])
+    inst = workloads.batched(seed=101, count=256)
+    As, Bs = [dev(x["a"]) for x in inst], [dev(x["b"]) for x in inst]
+    cases = [("twomode seed 101", lambda o: ctx.contract(A, A, w["ctr_a"], w["ctr_b"], o),
+              lambda: ctx.autotune(A, A, w["ctr_a"], w["ctr_b"], F.Options(), 1)[0]),
+             ("batched seed 101", lambda o: ctx.contract_batch(As, Bs, [1, 3], [1, 2], o)[0],
+              lambda: ctx.autotune_batch(As, Bs, [1, 3], [1, 2], F.Options(), 1)[0])]
+    for name, call, tune in cases:
+        def timed(opts, learned=False):
+            if learned:
+                ctx.load_default_model()
+            try:
+                ts, dg = [], None
+                for rep in range(4):
+                    o = F.Options(**{k: getattr(opts, k) for k, _ in F.Options._fields_})
+                    o.timing = 1
+                    r = call(o)
+                    if rep == 0:
+                        dg = _digest(r)
+                    r.free()
+                    if rep:
+                        ts.append(ctx.timings()["total"])
+                return statistics.median(ts), dg
+            finally:
+                ctx.sched_set_model(None)
+        t_rule, d_rule = timed(F.Options())
+        t_tuned, d_tuned = timed(tune())
+        t_learned, d_learned = timed(F.Options(schedule=F.SCHED_LEARNED), learned=True)
+        print(f"{name}: rule {t_rule:.2f} ms, autotuned {t_tuned:.2f} ms, learned {t_learned:.2f} ms "
+              f"(learned / rule {t_learned / t_rule:.3f})")
+        for d in (d_tuned, d_learned):
+            assert d[0] == d_rule[0] and d[1] == d_rule[1]
+            assert abs(d[2] - d_rule[2]) <= 1e-9 * max(d_rule[3], 1e-300)
+        assert t_learned <= 1.10 * t_rule
