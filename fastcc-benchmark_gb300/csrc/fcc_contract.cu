@@ -1719,6 +1719,7 @@ struct EscArgs {
   u64 span, LB;         // key = s * span + slot * LB + col, span = rows * LB
   u64 rows;
   u64 lbm;              // magic_for(LB) (used with 32-bit keys)
+  u64 rowsm;            // magic_for(rows) (used with 32-bit keys)
   u64 pair0;            // base[0]: this group's first pair
   void *keys;           // u32 when every key fits 32 bits, else u64
   u64 *vals;            // the products' bits (double), sorted along with the keys
@@ -1918,7 +1919,7 @@ __device__ __forceinline__ void esc_emit(const EscArgs &a, const u32 *__restrict
   else q = key / a.LB;
   const u64 col = key - q * a.LB;
   if (q != rc.q) {
-    const u64 s = q / a.rows, slot = q - s * a.rows;
+    const u64 s = sizeof(KeyT) == 4 ? u64(div_magic(u32(q), a.rowsm)) : q / a.rows, slot = q - s * a.rows;
     rc.q = q;
     rc.row = __ldg(&urow[tile_rank0[a.tiles[s]] + slot]);
   }
@@ -2058,6 +2059,533 @@ __global__ void __launch_bounds__(256) k_esc_reduce(EscArgs a, const u32 *__rest
     const u64 first = base + chunk_off[c];
     for (u32 r = lane; r < nruns; r += 32) esc_emit<KeyT>(a, tile_rank0, urow, out, dec, rc, first + r, sk[r], sv[r]);
     __syncwarp();
+  }
+}
+
+// ------------------------------- expanded pairs reduced in shared memory ----
+//
+// Instead of sorting a group's pairs, the expansion writes them tile by tile
+// into two regions of the group's buffer, every tile padded to a multiple of
+// eight pairs (padding keys are kBinEmpty):
+//  * small tiles (at most small_max pairs) first: windows of kBinWindow
+//    positions over this region, each taking the tiles that start in it
+//    (fewer than kBinWindow + small_max positions, one contiguous range), are
+//    reduced in shared-memory hash tables;
+//  * then the large tiles (hub rows): each is partitioned by blocks of
+//    kBinWidth consecutive local keys (slot x LB + column). Every chunk of
+//    kBinChunk positions counts its pairs per block, one exclusive scan over
+//    (tile, block, chunk) gives every chunk its positions, and the chunk
+//    scatters its pairs there. A block with more than kBinDenseMin pairs is
+//    reduced in a dense kBinWidth-entry accumulator with a bitmap of touched
+//    keys, runs of consecutive sparser blocks together in one hash table.
+// Every reduced window or block reserves its outputs with one atomic and
+// writes them in key order (dense) or table order (hash). After the
+// expansion a small tile's pair is read once, a large tile's twice (the
+// partition) and written once more.
+
+constexpr u32 kBinBits = 13;
+constexpr u32 kBinWidth = 1u << kBinBits;  // local keys per block: 8192 doubles, 64 KB
+constexpr u32 kBinMaxBlocks = 256;         // blocks per tile: spans up to 2^21 keys
+constexpr u32 kBinChunk = 4096;            // positions per partition chunk (a multiple of 8)
+constexpr u32 kBinWindow = 2048;           // small-tile positions per window
+constexpr u32 kBinSmallMax = 4096;         // default (and largest) small tile; a multiple of 8
+constexpr u32 kBinDenseMin = 2048;         // a block with more pairs is reduced densely
+constexpr u32 kBinHashPairs = 4096;        // sparse blocks merged up to this many pairs
+constexpr u32 kBinSlots = 8192;            // hash slots: > 4/3 x (kBinWindow + kBinSmallMax - 1)
+constexpr int kBinThreads = 512;
+constexpr u32 kBinEmpty = 0xFFFFFFFFu;     // padding / free slot: keys are below n x span <= 2^32 - 1
+constexpr size_t kBinSmem = size_t(kBinSlots) * (sizeof(double) + sizeof(u32));
+constexpr u32 kBinPer = 8;                 // pairs per expansion lane, the tiles' padding unit
+constexpr int kBinIlp = 4;                 // pairs per thread in flight in the reductions
+
+struct BinJob {  // a dense block, or a run of sparse blocks, of one large tile
+  u32 s;         // esc index within the group
+  uint16_t b0, b1;  // blocks [b0, b1)
+};
+
+struct BinArgs {
+  u32 small_max;  // tiles with more pairs are large
+  u32 nb;         // blocks per tile: ceil(span / kBinWidth)
+  u32 *lsz, *nch;                  // per esc tile: padded pairs if large (else 0); chunks if large
+  u32 *pp, *spp, *lpp, *chpre;     // exclusive scans over the tiles (n + 1 entries each) of the padded
+                                   // pairs, of those of the small tiles, of the large tiles, and of nch
+  u32 *chunk_tile;  // chunk -> esc index
+  u32 *first;       // window -> first esc index s with spp[s] >= window start
+  u64 max_windows;
+  u32 *hist;        // pairs per (tile, block, chunk), at nb * chpre[s] + b * nch[s] + c
+  u32 *hpre;        // exclusive scan of hist, hist_len + 1 entries
+  u64 hist_len;
+  u32 *bkeys;       // the large tiles' pairs, partitioned
+  u64 *bvals;
+  BinJob *jobs;
+  u32 *njobs;       // large-tile jobs
+  u32 *work;        // the reduction's job counter
+};
+
+// Pairs [t0, t1) of esc tile s, relative to the group's first pair.
+__device__ __forceinline__ void esc_tile_range(const EscArgs &a, u32 s, u64 &t0, u64 &t1) {
+  t0 = __ldg(&a.base[s]) - a.pair0;
+  t1 = s + 1 < a.n ? __ldg(&a.base[s + 1]) - a.pair0 : a.total;
+}
+
+// One CTA: every esc tile's padded size (pp), its place in the small or the
+// large region (spp, lpp) and its partition chunks (chpre), as exclusive
+// scans over the group's tiles, 1024 tiles per step.
+constexpr int kPrepThreads = 1024;
+__global__ void __launch_bounds__(kPrepThreads) k_bin_prep(EscArgs a, BinArgs b) {
+  __shared__ u32 wsum[4][kPrepThreads / 32];
+  __shared__ u32 carry[4];
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x < 4) carry[threadIdx.x] = 0;
+  __syncthreads();
+  for (u32 c0 = 0; c0 < a.n; c0 += kPrepThreads) {
+    const u32 s = c0 + threadIdx.x;
+    u32 v[4] = {0, 0, 0, 0};  // padded pairs; the same if small / large; chunks if large
+    if (s < a.n) {
+      u64 t0, t1;
+      esc_tile_range(a, s, t0, t1);
+      const u32 p = u32(t1 - t0);
+      const u32 pad = (p + kBinPer - 1) / kBinPer * kBinPer;
+      const bool large = p > b.small_max;
+      v[0] = pad;
+      v[1] = large ? 0u : pad;
+      v[2] = large ? pad : 0u;
+      v[3] = large ? (pad + kBinChunk - 1) / kBinChunk : 0u;
+      b.lsz[s] = v[2];
+      b.nch[s] = v[3];
+    }
+    u32 incl[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      incl[k] = warp_incl_u32(v[k]);
+      if (lane == 31) wsum[k][warp] = incl[k];
+    }
+    __syncthreads();
+    if (warp < 4) {  // warp k scans the 32 warp sums of value k
+      const u32 x = wsum[warp][lane], xi = warp_incl_u32(x);
+      wsum[warp][lane] = xi - x;
+    }
+    __syncthreads();
+    u32 *dst[4] = {b.pp, b.spp, b.lpp, b.chpre};
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (s < a.n) dst[k][s] = carry[k] + wsum[k][warp] + incl[k] - v[k];
+    __syncthreads();
+    if (threadIdx.x == kPrepThreads - 1) {
+#pragma unroll
+      for (int k = 0; k < 4; k++) carry[k] += wsum[k][warp] + incl[k];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    b.pp[a.n] = carry[0];
+    b.spp[a.n] = carry[1];
+    b.lpp[a.n] = carry[2];
+    b.chpre[a.n] = carry[3];
+  }
+}
+
+// Expansion into the two padded regions. A warp takes 256 consecutive
+// positions of the padded order, lane l the positions l, l + 32, ...: lanes
+// next to each other read B entries next to each other (one A entry's
+// segment) and store next to each other. Each lane finds its tile and A
+// entry by binary search once and then walks forward.
+template <class ColT>
+__global__ void __launch_bounds__(256) k_bin_expand(EscArgs a, BinArgs b, const ProdSrc src,
+                                                    const ColT *__restrict__ colB, const u32 *__restrict__ tile_abeg) {
+  u32 *keys = static_cast<u32 *>(a.keys);
+  const u64 ptot = b.pp[a.n], sfull = b.spp[a.n];
+  const u32 lane = threadIdx.x & 31;
+  const u64 nwarps = (u64(gridDim.x) * blockDim.x) >> 5;
+  for (u64 c = (u64(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; c * 256 < ptot; c += nwarps) {
+    const u64 q0 = c * 256 + lane;
+    u32 s;
+    {
+      u32 lo = 0, hi = a.n;  // pp[lo] <= q0 < pp[hi] (pp[n] = ptot)
+      while (hi - lo > 1) {
+        const u32 m = (lo + hi) >> 1;
+        if (u64(__ldg(&b.pp[m])) <= q0) lo = m;
+        else hi = m;
+      }
+      s = lo;
+    }
+    u64 tb = 0, te = 0, cnt = 0, d0 = 0, p0 = 0;  // the tile: padded [tb, te), pairs, destination, first product
+    u32 ea = 0, eb = 0;
+    u32 e = kNoEntry, sb = 0;
+    u64 pe = 0, pn = 0;
+    double va = 0.0;
+    u32 kb = 0;
+    bool fresh = true;
+#pragma unroll 1
+    for (u32 i = 0; i < 8; i++) {
+      const u64 q = q0 + 32 * i;
+      if (q >= ptot) break;
+      if (fresh || q >= te) {  // this lane's next tile
+        if (!fresh)
+          while (u64(__ldg(&b.pp[s + 1])) <= q) s++;
+        fresh = false;
+        tb = __ldg(&b.pp[s]);
+        te = __ldg(&b.pp[s + 1]);
+        u64 t0, t1;
+        esc_tile_range(a, s, t0, t1);
+        cnt = t1 - t0;
+        d0 = __ldg(&b.nch[s]) == 0 ? u64(__ldg(&b.spp[s])) : sfull + __ldg(&b.lpp[s]);
+        const u32 t = a.tiles[s];
+        ea = tile_abeg[t];
+        eb = tile_abeg[t + 1];
+        p0 = __ldg(&src.P[ea]);
+        e = kNoEntry;
+      }
+      const u64 o = q - tb;
+      u32 key = kBinEmpty;
+      double v = 0.0;
+      if (o < cnt) {
+        const u64 p = p0 + o;
+        if (e == kNoEntry) {
+          u32 l = ea, h = eb;  // the A entry holding p: P[l] <= p < P[h]
+          while (h - l > 1) {
+            const u32 m = (l + h) >> 1;
+            if (__ldg(&src.P[m]) <= p) l = m;
+            else h = m;
+          }
+          e = l;
+          pe = __ldg(&src.P[e]);
+          pn = __ldg(&src.P[e + 1]);
+          sb = __ldg(&src.sbA[e]);
+          va = __ldg(&src.valA[e]);
+          kb = s * u32(a.span) + __ldg(&src.slotA[e]) * u32(a.LB);
+        }
+        while (p >= pn) {  // the next A entries of the tile
+          e++;
+          pe = pn;
+          pn = __ldg(&src.P[e + 1]);
+          sb = __ldg(&src.sbA[e]);
+          va = __ldg(&src.valA[e]);
+          kb = s * u32(a.span) + __ldg(&src.slotA[e]) * u32(a.LB);
+        }
+        const u32 j = sb + u32(p - pe);
+        key = kb + u32(__ldg(&colB[j]));
+        v = va * __ldg(&src.valB[j]);
+      }
+      keys[d0 + o] = key;
+      a.vals[d0 + o] = u64(__double_as_longlong(v));
+    }
+  }
+}
+
+// chunk_tile for the large tiles' chunks; first[w] = the first esc index s
+// with spp[s] >= w * kBinWindow (n when none), for every window and one past.
+__global__ void k_bin_index(EscArgs a, BinArgs b) {
+  const u64 i0 = u64(blockIdx.x) * blockDim.x + threadIdx.x, nth = u64(gridDim.x) * blockDim.x;
+  for (u64 s = i0; s < a.n; s += nth) {
+    const u32 c0 = b.chpre[s], nc = b.nch[s];
+    for (u32 c = 0; c < nc; c++) b.chunk_tile[c0 + c] = u32(s);
+  }
+  const u64 nwin = (u64(b.spp[a.n]) + kBinWindow - 1) / kBinWindow;
+  for (u64 w = i0; w <= nwin && w < b.max_windows; w += nth) {
+    const u64 x = w * kBinWindow;
+    u32 lo = 0, hi = a.n;  // the first s in [lo, hi] with spp[s] >= x (spp[n] = the region's size)
+    while (lo < hi) {
+      const u32 m = (lo + hi) >> 1;
+      if (u64(b.spp[m]) >= x) hi = m;
+      else lo = m + 1;
+    }
+    b.first[w] = lo;
+  }
+}
+
+// Positions [q0, q1) of chunk g (tile s, chunk c) in the group's buffer.
+__device__ __forceinline__ void bin_chunk(const EscArgs &a, const BinArgs &b, u32 g, u32 &s, u32 &c, u64 &q0,
+                                          u64 &q1) {
+  s = b.chunk_tile[g];
+  c = g - b.chpre[s];
+  const u64 l0 = u64(b.spp[a.n]) + b.lpp[s];
+  q0 = l0 + u64(c) * kBinChunk;
+  q1 = min(l0 + b.lsz[s], q0 + kBinChunk);
+}
+
+// Pairs per block of each chunk of the large tiles.
+__global__ void __launch_bounds__(256) k_bin_hist(EscArgs a, BinArgs b) {
+  __shared__ u32 h[kBinMaxBlocks];
+  const u32 nchunks = b.chpre[a.n];
+  const u32 *keys = static_cast<const u32 *>(a.keys);
+  for (u32 g = blockIdx.x; g < nchunks; g += gridDim.x) {
+    for (u32 i = threadIdx.x; i < b.nb; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    u32 s, c;
+    u64 q0, q1;
+    bin_chunk(a, b, g, s, c, q0, q1);
+    const u32 kb = s * u32(a.span);  // keys (s x span + local key) fit 32 bits
+    for (u64 q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+      const u32 k = keys[q];
+      if (k != kBinEmpty) atomicAdd(&h[(k - kb) >> kBinBits], 1u);
+    }
+    __syncthreads();
+    const u64 r = u64(b.nb) * b.chpre[s] + c;
+    const u32 nc = b.nch[s];
+    for (u32 i = threadIdx.x; i < b.nb; i += blockDim.x) b.hist[r + u64(i) * nc] = h[i];
+    __syncthreads();
+  }
+}
+
+// Each chunk's pairs to their block's positions (within a block, in the
+// order the threads reach their shared counter).
+__global__ void __launch_bounds__(256) k_bin_scatter(EscArgs a, BinArgs b) {
+  __shared__ u32 cur[kBinMaxBlocks];
+  const u32 nchunks = b.chpre[a.n];
+  const u32 *keys = static_cast<const u32 *>(a.keys);
+  for (u32 g = blockIdx.x; g < nchunks; g += gridDim.x) {
+    u32 s, c;
+    u64 q0, q1;
+    bin_chunk(a, b, g, s, c, q0, q1);
+    const u64 r = u64(b.nb) * b.chpre[s] + c;
+    const u32 nc = b.nch[s];
+    for (u32 i = threadIdx.x; i < b.nb; i += blockDim.x) cur[i] = b.hpre[r + u64(i) * nc];
+    __syncthreads();
+    const u32 kb = s * u32(a.span);
+    const u32 lane = threadIdx.x & 31;
+    for (u64 qw = q0; qw < q1; qw += blockDim.x) {  // the same trip count in every lane
+      const u64 q = qw + threadIdx.x;
+      const u32 k = q < q1 ? keys[q] : kBinEmpty;
+      const u32 bin = k != kBinEmpty ? (k - kb) >> kBinBits : kBinMaxBlocks;
+      // lanes of one block take consecutive positions with one shared atomic
+      const u32 peers = __match_any_sync(kFull, bin);
+      const u32 leader = __ffs(peers) - 1;
+      u32 pos = 0;
+      if (lane == leader && bin < kBinMaxBlocks) pos = atomicAdd(&cur[bin], u32(__popc(peers)));
+      pos = __shfl_sync(kFull, pos, leader) + __popc(peers & ((1u << lane) - 1u));
+      if (bin < kBinMaxBlocks) {
+        b.bkeys[pos] = k;
+        b.bvals[pos] = a.vals[q];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Jobs of each large tile: every block with more than kBinDenseMin pairs
+// alone (dense), runs of consecutive sparser blocks up to kBinHashPairs pairs
+// together (hash).
+__global__ void k_bin_jobs(EscArgs a, BinArgs b) {
+  for (u32 s = blockIdx.x * blockDim.x + threadIdx.x; s < a.n; s += gridDim.x * blockDim.x) {
+    const u32 nc = b.nch[s];
+    if (nc == 0) continue;
+    const u64 r = u64(b.nb) * b.chpre[s];
+    u32 run0 = 0, runp = 0;
+    auto push = [&](u32 b0, u32 b1) {
+      const u32 j = atomicAdd(b.njobs, 1u);
+      b.jobs[j] = BinJob{s, uint16_t(b0), uint16_t(b1)};
+    };
+    u32 prev = b.hpre[r];
+    for (u32 blk = 0; blk < b.nb; blk++) {
+      const u32 next = b.hpre[r + u64(blk + 1) * nc];  // blk + 1 == nb: the next tile's (or the end's) start
+      const u32 cnt = next - prev;
+      prev = next;
+      if (cnt > kBinDenseMin) {
+        if (runp > 0) push(run0, blk);
+        push(blk, blk + 1);
+        run0 = blk + 1;
+        runp = 0;
+      } else if (runp + cnt > kBinHashPairs) {
+        push(run0, blk);
+        run0 = blk;
+        runp = cnt;
+      } else {
+        runp += cnt;
+      }
+    }
+    if (runp > 0) push(run0, b.nb);
+  }
+}
+
+// Lanes holding the same key (hub columns reach a block or a window from
+// many A entries at once) are summed first; returns true for the lane that
+// keeps the key with the group's sum in *v. Every lane of the warp calls it
+// (kBinEmpty for no pair).
+__device__ __forceinline__ bool bin_aggregate(u32 key, double *v) {
+  const u32 lane = threadIdx.x & 31;
+  const u32 peers = __match_any_sync(kFull, key);
+  if (key == kBinEmpty) return false;
+  if (peers == (1u << lane)) return true;
+  const u32 leader = __ffs(peers) - 1;
+  double sum = *v;
+  for (u32 rest = peers & (peers - 1); rest; rest &= rest - 1) {
+    const double y = __shfl_sync(peers, *v, __ffs(rest) - 1);
+    if (lane == leader) sum += y;
+  }
+  *v = sum;
+  return lane == leader;
+}
+
+// Shared-memory hash insert: linear probing from a multiplicative hash, the
+// table never full (slots > pairs); a slot's key is read before it is claimed.
+__device__ __forceinline__ void bin_insert(u32 *tk, double *tv, u32 mask, u32 lg, u32 key, double v) {
+  u32 h = (key * 2654435761u) >> (32 - lg);
+  for (;;) {
+    u32 cur = reinterpret_cast<volatile u32 *>(tk)[h];
+    if (cur == kBinEmpty) cur = atomicCAS(&tk[h], kBinEmpty, key);
+    if (cur == kBinEmpty || cur == key) break;
+    h = (h + 1) & mask;
+  }
+  atomicAdd(&tv[h], v);  // under contention the built-in add beats a compare-and-swap loop
+}
+
+// Emits the table's occupied slots (hash: tk[i] != empty; dense: bit i of
+// bitmap tk) with one reservation for the CTA; slots [0, n), n a multiple of
+// 32. Each warp packs the occupied slots of its words into a 64-entry ring
+// and writes full warps of outputs from it (the decode and the stores then
+// run on all 32 lanes instead of on the occupied ones only).
+struct BinRing {
+  u32 k[kBinThreads / 32][64];
+  double v[kBinThreads / 32][64];
+};
+
+template <bool kDense>
+__device__ void bin_emit(const EscArgs &a, const u32 *__restrict__ tile_rank0, const u64 *__restrict__ urow,
+                         const Out &out, const Decode &dec, u32 *err, const u32 *tk, const double *tv, u32 n,
+                         u32 dkey0, u32 *s_wcnt, u64 *s_base, BinRing &ring) {
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  u32 cnt = 0;
+  for (u32 w = warp; w < n / 32; w += nw) {
+    const u32 m = kDense ? tk[w] : __ballot_sync(kFull, tk[w * 32 + lane] != kBinEmpty);
+    cnt += __popc(m);
+  }
+  if (lane == 0) s_wcnt[warp] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    u32 tot = 0;
+    for (u32 i = 0; i < nw; i++) {
+      const u32 c = s_wcnt[i];
+      s_wcnt[i] = tot;
+      tot += c;
+    }
+    *s_base = reserve(out, tot, err);
+  }
+  __syncthreads();
+  const u64 base = *s_base;
+  if (base != ~0ull) {  // else over capacity: counted by the cursor, retried by the host
+    u64 idx = base + s_wcnt[warp];
+    u32 *rk = ring.k[warp];
+    double *rv = ring.v[warp];
+    u32 head = 0, tail = 0;  // entries queued / written
+    EscRowCache rc;
+    for (u32 w = warp; w < n / 32; w += nw) {
+      const u32 i = w * 32 + lane;
+      const u32 m = kDense ? tk[w] : __ballot_sync(kFull, tk[i] != kBinEmpty);
+      if ((m >> lane) & 1u) {
+        const u32 e = (head + __popc(m & ((1u << lane) - 1u))) & 63u;
+        rk[e] = kDense ? dkey0 + i : tk[i];
+        rv[e] = tv[i];
+      }
+      head += __popc(m);
+      __syncwarp();
+      if (head - tail >= 32) {
+        const u32 e = (tail + lane) & 63u;
+        esc_emit<u32>(a, tile_rank0, urow, out, dec, rc, idx + lane, rk[e], rv[e]);
+        idx += 32;
+        tail += 32;
+        __syncwarp();
+      }
+    }
+    if (lane < head - tail) {
+      const u32 e = (tail + lane) & 63u;
+      esc_emit<u32>(a, tile_rank0, urow, out, dec, rc, idx + lane, rk[e], rv[e]);
+    }
+  }
+  __syncthreads();
+}
+
+// Hash-reduces positions [lo, hi) of (keys, vals), padding skipped.
+__device__ __forceinline__ void bin_hash(const u32 *__restrict__ keys, const u64 *__restrict__ vals, u64 lo, u64 hi,
+                                         u32 *tk, double *tv, u32 &slots) {
+  const u32 np = u32(hi - lo);
+  u32 lg = 5;
+  while ((1u << lg) < np + np / 3 + 1) lg++;
+  slots = 1u << lg;
+  for (u32 i = threadIdx.x; i < slots; i += blockDim.x) {
+    tk[i] = kBinEmpty;
+    tv[i] = 0.0;
+  }
+  __syncthreads();
+  for (u64 q0 = lo; q0 < hi; q0 += u64(blockDim.x) * kBinIlp) {  // the same trip count in every lane
+    u32 k[kBinIlp];
+    double v[kBinIlp];
+#pragma unroll
+    for (int i = 0; i < kBinIlp; i++) {  // every load in flight first
+      const u64 q = q0 + u64(i) * blockDim.x + threadIdx.x;
+      k[i] = q < hi ? keys[q] : kBinEmpty;
+      v[i] = q < hi ? __longlong_as_double((long long)vals[q]) : 0.0;
+    }
+#pragma unroll
+    for (int i = 0; i < kBinIlp; i++)
+      if (bin_aggregate(k[i], &v[i])) bin_insert(tk, tv, slots - 1, lg, k[i], v[i]);
+  }
+  __syncthreads();
+}
+
+// Persistent CTAs take jobs from a counter: first the large tiles' jobs
+// (dense blocks and runs of sparse blocks, from the partitioned pairs), then
+// the windows of small tiles.
+__global__ void __launch_bounds__(kBinThreads) k_bin_reduce(EscArgs a, BinArgs b, const u32 *__restrict__ tile_rank0,
+                                                            const u64 *__restrict__ urow, const Out out,
+                                                            const Decode dec, u32 *err) {
+  extern __shared__ __align__(16) unsigned char bin_smem[];
+  double *tv = reinterpret_cast<double *>(bin_smem);  // kBinSlots values (dense: the block)
+  u32 *tk = reinterpret_cast<u32 *>(tv + kBinSlots);   // kBinSlots keys (dense: the bitmap)
+  __shared__ u32 s_job, s_wcnt[kBinThreads / 32];
+  __shared__ u64 s_base;
+  __shared__ BinRing ring;
+  const u32 nbig = *b.njobs;
+  const u64 nwin = (u64(b.spp[a.n]) + kBinWindow - 1) / kBinWindow;
+  const u64 njobs = u64(nbig) + nwin;
+  const u32 *keys = static_cast<const u32 *>(a.keys);
+  for (;;) {
+    if (threadIdx.x == 0) s_job = atomicAdd(b.work, 1u);
+    __syncthreads();
+    const u64 j = s_job;
+    __syncthreads();
+    if (j >= njobs) break;
+    if (j < nbig) {
+      const BinJob jb = b.jobs[j];
+      const u32 nc = b.nch[jb.s];
+      const u64 r = u64(b.nb) * b.chpre[jb.s];
+      const u32 lo = b.hpre[r + u64(jb.b0) * nc], hi = b.hpre[r + u64(jb.b1) * nc];
+      if (jb.b1 == jb.b0 + 1 && hi - lo > kBinDenseMin) {  // dense block
+        const u32 k0 = jb.s * u32(a.span) + u32(jb.b0) * kBinWidth;
+        for (u32 i = threadIdx.x; i < kBinWidth; i += blockDim.x) tv[i] = 0.0;
+        for (u32 i = threadIdx.x; i < kBinWidth / 32; i += blockDim.x) tk[i] = 0u;
+        __syncthreads();
+        for (u32 q0 = lo; q0 < hi; q0 += blockDim.x * kBinIlp) {  // the same trip count in every lane
+          u32 loc[kBinIlp];
+          double v[kBinIlp];
+#pragma unroll
+          for (int i = 0; i < kBinIlp; i++) {
+            const u32 q = q0 + u32(i) * blockDim.x + threadIdx.x;
+            loc[i] = q < hi ? b.bkeys[q] - k0 : kBinEmpty;
+            v[i] = q < hi ? __longlong_as_double((long long)b.bvals[q]) : 0.0;
+          }
+#pragma unroll
+          for (int i = 0; i < kBinIlp; i++) {
+            if (bin_aggregate(loc[i], &v[i])) {
+              atomicAdd(&tv[loc[i]], v[i]);
+              atomicOr(&tk[loc[i] >> 5], 1u << (loc[i] & 31));
+            }
+          }
+        }
+        __syncthreads();
+        bin_emit<true>(a, tile_rank0, urow, out, dec, err, tk, tv, kBinWidth, k0, s_wcnt, &s_base, ring);
+      } else {  // sparse blocks: at most kBinHashPairs pairs
+        u32 slots;
+        bin_hash(b.bkeys, b.bvals, lo, hi, tk, tv, slots);
+        bin_emit<false>(a, tile_rank0, urow, out, dec, err, tk, tv, slots, 0, s_wcnt, &s_base, ring);
+      }
+    } else {  // a window of small tiles: fewer than kBinWindow + small_max positions
+      const u64 w = j - nbig;
+      const u32 lo = b.spp[b.first[w]], hi = b.spp[b.first[w + 1]];
+      u32 slots;
+      bin_hash(keys, a.vals, lo, hi, tk, tv, slots);
+      bin_emit<false>(a, tile_rank0, urow, out, dec, err, tk, tv, slots, 0, s_wcnt, &s_base, ring);
+    }
   }
 }
 
@@ -2448,6 +2976,9 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   if (opt.fault_wait != 0 && opt.fault_wait != 1) throw Error{FCC_ERR_ARG, "fault_wait must be 0 or 1"};
   if (opt.dense_kernel < 0 || opt.dense_kernel > 3) throw Error{FCC_ERR_ARG, "dense_kernel must be 0, 1, 2 or 3"};
   if (opt.esc_group < 0) throw Error{FCC_ERR_ARG, "esc_group must be >= 0"};
+  if (opt.esc_reduce < 0 || opt.esc_reduce > 2) throw Error{FCC_ERR_ARG, "esc_reduce must be 0, 1 or 2"};
+  if (opt.esc_small < 0 || opt.esc_small > int(kBinSmallMax))
+    throw Error{FCC_ERR_ARG, "esc_small must be in [0, " + std::to_string(kBinSmallMax) + "]"};
   bool learned = forced < 0 && opt.schedule == FCC_SCHED_LEARNED && ctx->sched && ctx->sched->model;
   const bool want_record = opt.timing == 2 && ctx->sched;
   // Row groups (batched contractions): dense tiles hold rows of one group,
@@ -2675,6 +3206,13 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   std::vector<EscGroup> escg;
   const u64 esc_span = esc_rows * LB;
   const bool esc_k32 = esc_span <= 0xFFFFFFFFull;
+  // Groups reduced in shared memory (32-bit keys, a span of at most
+  // kBinMaxBlocks blocks) share one set of scratch buffers, sized for the
+  // largest group; the rest are sorted.
+  const u32 bin_nb = u32((esc_span + kBinWidth - 1) / kBinWidth);
+  const bool binned = esc_k32 && esc_span <= u64(kBinMaxBlocks) * kBinWidth && opt.esc_reduce != 2;
+  const u32 bin_small = opt.esc_small > 0 ? u32(opt.esc_small) : kBinSmallMax;
+  BinArgs bins{};
   if (nesc > 0) {
     u64 G = esc_k32 ? std::max<u64>(1, 0xFFFFFFFFull / esc_span) : u64(nesc);
     if (opt.esc_group > 0) G = std::min<u64>(G, u64(opt.esc_group));
@@ -2691,17 +3229,49 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     for (u32 g = 0; g < ng; g++) {
       const u32 s0 = u32(u64(g) * G), n = u32(std::min<u64>(G, u64(nesc) - s0));
       const u64 pairs = start[g + 1] - start[g];
-      EscGroup e{EscArgs{esc_tiles + s0, esc_base + s0, n, esc_span, LB, esc_rows, magic_for(LB), start[g], nullptr,
-                         nullptr, pairs},
+      EscGroup e{EscArgs{esc_tiles + s0, esc_base + s0, n, esc_span, LB, esc_rows, magic_for(LB), magic_for(esc_rows),
+                         start[g], nullptr, nullptr, pairs},
                  nullptr, nullptr, 0, 1, 0};
-      e.a.keys = esc_k32 ? static_cast<void *>(ar.get_n<u32>(pairs)) : static_cast<void *>(ar.get_n<u64>(pairs));
-      e.a.vals = ar.get_n<u64>(pairs);
+      const u64 cap = binned ? pairs + u64(kBinPer) * n : pairs;  // binned: every tile padded to 8 pairs
+      e.a.keys = esc_k32 ? static_cast<void *>(ar.get_n<u32>(cap)) : static_cast<void *>(ar.get_n<u64>(cap));
+      e.a.vals = ar.get_n<u64>(cap);
       e.chunks = (pairs + kEscChunk - 1) / kEscChunk;
       e.heads = ar.get_n<u32>(e.chunks);
       e.offc = ar.get_n<u32>(e.chunks);
       e.grid = int(std::max<u64>(1, std::min<u64>((e.chunks + 7) / 8, u64(ctx->num_sms) * 8)));
       e.bits = bits_for(u64(n) * esc_span - 1);
       escg.push_back(e);
+    }
+    if (binned) {
+      u64 maxn = 0, maxp = 0, maxch = 0, maxjobs = 0;
+      for (const EscGroup &e : escg) {
+        const u64 cap = e.a.total + u64(kBinPer) * e.a.n;  // with every tile's padding
+        maxn = std::max<u64>(maxn, e.a.n);
+        maxp = std::max<u64>(maxp, cap);
+        maxch = std::max<u64>(maxch, cap / kBinChunk + e.a.n);
+        maxjobs = std::max<u64>(maxjobs, u64(bin_nb) * std::min<u64>(e.a.n, e.a.total / (u64(bin_small) + 1) + 1));
+      }
+      bins.small_max = bin_small;
+      bins.nb = bin_nb;
+      u32 *per = ar.get_n<u32>(2 * maxn);
+      bins.lsz = per;
+      bins.nch = per + maxn;
+      u32 *pre = ar.get_n<u32>(4 * (maxn + 1));
+      bins.pp = pre;
+      bins.spp = pre + (maxn + 1);
+      bins.lpp = pre + 2 * (maxn + 1);
+      bins.chpre = pre + 3 * (maxn + 1);
+      bins.chunk_tile = ar.get_n<u32>(maxch);
+      bins.max_windows = maxp / kBinWindow + 2;
+      bins.first = ar.get_n<u32>(bins.max_windows);
+      bins.hist_len = u64(bin_nb) * maxch;
+      bins.hist = ar.get_n<u32>(bins.hist_len);
+      bins.hpre = ar.get_n<u32>(bins.hist_len + 1);
+      bins.bkeys = ar.get_n<u32>(maxp);
+      bins.bvals = ar.get_n<u64>(maxp);
+      bins.jobs = ar.get_n<BinJob>(std::max<u64>(maxjobs, 1));
+      bins.njobs = ar.get_n<u32>(2);
+      bins.work = bins.njobs + 1;
     }
   }
   const u64 words = dense ? (area + 31) / 32 : 0;
@@ -2932,6 +3502,37 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       }
       for (const EscGroup &e : escg) {  // expanded tiles: expand, sort, reduce, group by group
         const EscArgs &ea = e.a;
+        if (binned) {  // plan, expand (the pairs stay for a retry), partition the large tiles, reduce
+          const int tgrid = grid_for(ea.n, 256);
+          BinArgs bg = bins;
+          const u64 cap = ea.total + u64(kBinPer) * ea.n;
+          bg.max_windows = cap / kBinWindow + 2;
+          bg.hist_len = u64(bin_nb) * (cap / kBinChunk + ea.n);
+          // (a retry repeats all but the expansion: the scratch is shared by the groups)
+          k_bin_prep<<<1, kPrepThreads, 0, st>>>(ea, bg);
+          FCC_LAUNCH_CHECK();
+          if (attempt == 0) {
+            const u32 xgrid = u32(std::max<u64>(1, std::min<u64>((cap + 2047) / 2048, u64(ctx->num_sms) * 16)));
+            k_bin_expand<ColT><<<xgrid, 256, 0, st>>>(ea, bg, src, colptr, tile_abeg);
+            FCC_LAUNCH_CHECK();
+          }
+          k_bin_index<<<grid_for(i64(std::max<u64>(ea.n, bg.max_windows)), 256), 256, 0, st>>>(ea, bg);
+          FCC_LAUNCH_CHECK();
+          FCC_CUDA(cudaMemsetAsync(bg.hist, 0, sizeof(u32) * bg.hist_len, st));
+          const int cgrid = ctx->num_sms * 8;
+          k_bin_hist<<<cgrid, 256, 0, st>>>(ea, bg);
+          FCC_LAUNCH_CHECK();
+          scan_exclusive(bg.hist, bg.hpre, i64(bg.hist_len), bg.hpre + bg.hist_len, ar, st);
+          k_bin_scatter<<<cgrid, 256, 0, st>>>(ea, bg);
+          FCC_LAUNCH_CHECK();
+          FCC_CUDA(cudaMemsetAsync(bg.njobs, 0, 2 * sizeof(u32), st));
+          k_bin_jobs<<<tgrid, 256, 0, st>>>(ea, bg);
+          FCC_LAUNCH_CHECK();
+          FCC_CUDA(cudaFuncSetAttribute(k_bin_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kBinSmem)));
+          k_bin_reduce<<<ctx->num_sms * 2, kBinThreads, kBinSmem, st>>>(ea, bg, tile_rank0, urow, o, dec, ctx->d_err);
+          FCC_LAUNCH_CHECK();
+          continue;
+        }
         if (attempt == 0) {  // the sorted pairs stay for a retry
           const u32 xgrid = u32(std::max<u64>(1, std::min<u64>((ea.total + 2047) / 2048, u64(ctx->num_sms) * 8)));
           if (esc_k32) {

@@ -50,14 +50,14 @@ class Options(ctypes.Structure):
                 ("radix_mode", ctypes.c_int32), ("rows_per_tile", ctypes.c_int32),
                 ("products_per_item", ctypes.c_int64), ("dense_cap", ctypes.c_int32),
                 ("hash_slots", ctypes.c_int32), ("timing", ctypes.c_int32),
-                ("pad0", ctypes.c_int32), ("capacity_hint", ctypes.c_int64),
+                ("esc_small", ctypes.c_int32), ("capacity_hint", ctypes.c_int64),
                 ("dense_mode", ctypes.c_int32), ("tile_threads", ctypes.c_int32),
                 ("hot_columns", ctypes.c_int32), ("schedule", ctypes.c_int32),
                 ("dense_fill_log2", ctypes.c_int32), ("dense_staging", ctypes.c_int32),
                 ("sched_mix_margin", ctypes.c_int32), ("hash_esc", ctypes.c_int32),
                 ("out_waves", ctypes.c_int32), ("esc_group", ctypes.c_int32),
                 ("wait_polls", ctypes.c_int32), ("fault_wait", ctypes.c_int32),
-                ("dense_kernel", ctypes.c_int32), ("pad1", ctypes.c_int32)]
+                ("dense_kernel", ctypes.c_int32), ("esc_reduce", ctypes.c_int32)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -368,7 +368,7 @@ class Context:
 
     @staticmethod
     def options_dict(o):
-        return {name: getattr(o, name) for name, _ in Options._fields_ if name not in ("pad0", "pad1", "reserved")}
+        return {name: getattr(o, name) for name, _ in Options._fields_ if name not in ("reserved",)}
 
     def load_default_model(self):
         """Installs the cost model shipped with the package (sched_model.f32); False when absent."""

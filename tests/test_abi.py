@@ -37,7 +37,7 @@ def test_synth_library_exports_every_declared_symbol():
 
 def test_library_loads_and_reports_status_strings():
     L = F.lib()
-    assert L.fcc_abi_version() == 4
+    assert L.fcc_abi_version() == 5
     assert L.fcc_status_string(0) == b"ok"
     assert L.fcc_status_string(3) == b"hash accumulator full"
     o = F.Options()

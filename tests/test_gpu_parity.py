@@ -65,6 +65,11 @@ VARIANTS = [
     {"dense_kernel": 3, "hot_columns": 32, "rows_per_tile": 1},             # private hot columns, plain updates
     {"dense_kernel": 2, "hot_columns": 64, "rows_per_tile": 1, "dense_mode": F.DENSE_BITMASK,
      "products_per_item": 9},
+    {"accumulator": F.ACC_HASH, "esc_reduce": 2},                             # expanded pairs radix-sorted
+    {"accumulator": F.ACC_HASH, "products_per_item": 5, "esc_reduce": 2, "esc_group": 2},
+    {"accumulator": F.ACC_HASH, "esc_small": 1},                              # every tile partitioned by key blocks
+    {"accumulator": F.ACC_HASH, "esc_small": 24, "esc_group": 3},
+    {"accumulator": F.ACC_HASH, "esc_small": 7, "capacity_hint": 5},          # ... and the exact-count retry
 ]
 
 
@@ -300,7 +305,25 @@ def test_long_runs_of_equal_outputs(ctx, rows, cols, k):
     for opts in ({"accumulator": F.ACC_HASH, "hash_slots": 64},
                  {"accumulator": F.ACC_HASH, "hash_slots": 64, "esc_group": 2},
                  {"accumulator": F.ACC_HASH, "hash_slots": 64, "hash_esc": -1},
-                 {"accumulator": F.ACC_HASH, "products_per_item": 100}):
+                 {"accumulator": F.ACC_HASH, "products_per_item": 100},
+                 {"accumulator": F.ACC_HASH, "esc_reduce": 2},
+                 {"accumulator": F.ACC_HASH, "esc_small": 1}):
         c, v, prods = run_gpu(ctx, *args, **opts)
         assert prods == o["products"] == rows * cols * k
         check_parity(c, v, o["coords"], o["values"], o["abs_sum"])
+
+
+@pytest.mark.parametrize("opts", [{}, {"esc_small": 1}, {"esc_small": 300}, {"esc_small": 4096, "esc_group": 7},
+                                  {"esc_reduce": 2}])
+def test_expanded_pairs_reduced_by_key_blocks(ctx, opts):
+    # two-mode shape with a 40,000-column B span (5 key blocks of 8192): hub
+    # rows hold dense blocks (over 2048 pairs) and runs of sparse ones, the
+    # other rows go through the windows of small tiles
+    w = workloads.twomode(seed=3, nnz=400_000, dims=(800, 800, 300, 50))
+    a = w["a"]
+    args = (a.coords, a.values, a.max_index, a.coords, a.values, a.max_index, w["ctr_a"], w["ctr_b"])
+    o = run_oracle(*args)
+    c, v, prods = run_gpu(ctx, *args, **opts)
+    assert prods == o["products"]
+    n, _, _ = check_parity(c, v, o["coords"], o["values"], o["abs_sum"])
+    assert n == len(o["values"])
