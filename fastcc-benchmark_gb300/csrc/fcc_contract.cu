@@ -2064,24 +2064,26 @@ __global__ void __launch_bounds__(256) k_esc_reduce(EscArgs a, const u32 *__rest
 
 // ------------------------------- expanded pairs reduced in shared memory ----
 //
-// Instead of sorting a group's pairs, the expansion writes them tile by tile
-// into two regions of the group's buffer, every tile padded to a multiple of
-// eight pairs (padding keys are kBinEmpty):
-//  * small tiles (at most small_max pairs) first: windows of kBinWindow
+// Instead of being sorted, the expanded pairs are written tile by tile into
+// two regions of one buffer, every tile padded to a multiple of eight pairs
+// (padding keys are kBinEmpty):
+//  * small tiles (at most small_max pairs) first. Windows of kBinWindow
 //    positions over this region, each taking the tiles that start in it
-//    (fewer than kBinWindow + small_max positions, one contiguous range), are
-//    reduced in shared-memory hash tables;
-//  * then the large tiles (hub rows): each is partitioned by blocks of
-//    kBinWidth consecutive local keys (slot x LB + column). Every chunk of
-//    kBinChunk positions counts its pairs per block, one exclusive scan over
-//    (tile, block, chunk) gives every chunk its positions, and the chunk
+//    (fewer than kBinWindow + small_max positions and at most
+//    kBinWindow / 8 + 1 tiles, one contiguous range), are reduced in
+//    shared-memory hash tables; a small tile's key is its rank among the
+//    window's tiles x span + its local key (slot x LB + column);
+//  * then the large tiles (hub rows), keyed by the local key alone. Each is
+//    partitioned by blocks of kBinWidth consecutive local keys: every chunk
+//    of kBinChunk positions counts its pairs per block, one exclusive scan
+//    over (tile, block, chunk) gives every chunk its positions, and the chunk
 //    scatters its pairs there. A block with more than kBinDenseMin pairs is
 //    reduced in a dense kBinWidth-entry accumulator with a bitmap of touched
 //    keys, runs of consecutive sparser blocks together in one hash table.
 // Every reduced window or block reserves its outputs with one atomic and
-// writes them in key order (dense) or table order (hash). After the
-// expansion a small tile's pair is read once, a large tile's twice (the
-// partition) and written once more.
+// writes them. After the expansion a small tile's pair is read once, a large
+// tile's twice and written once more; keys never need more than 32 bits, so
+// every expanded tile goes through one set of launches.
 
 constexpr u32 kBinBits = 13;
 constexpr u32 kBinWidth = 1u << kBinBits;  // local keys per block: 8192 doubles, 64 KB
@@ -2093,95 +2095,151 @@ constexpr u32 kBinDenseMin = 2048;         // a block with more pairs is reduced
 constexpr u32 kBinHashPairs = 4096;        // sparse blocks merged up to this many pairs
 constexpr u32 kBinSlots = 8192;            // hash slots: > 4/3 x (kBinWindow + kBinSmallMax - 1)
 constexpr int kBinThreads = 512;
-constexpr u32 kBinEmpty = 0xFFFFFFFFu;     // padding / free slot: keys are below n x span <= 2^32 - 1
+constexpr u32 kBinEmpty = 0xFFFFFFFFu;     // padding / free slot (keys stay below 257 x 2^21)
 constexpr size_t kBinSmem = size_t(kBinSlots) * (sizeof(double) + sizeof(u32));
-constexpr u32 kBinPer = 8;                 // pairs per expansion lane, the tiles' padding unit
+constexpr u32 kBinPer = 8;                 // the tiles' padding unit
 constexpr int kBinIlp = 4;                 // pairs per thread in flight in the reductions
 
 struct BinJob {  // a dense block, or a run of sparse blocks, of one large tile
-  u32 s;         // esc index within the group
+  u32 s;         // esc index
   uint16_t b0, b1;  // blocks [b0, b1)
 };
 
 struct BinArgs {
-  u32 small_max;  // tiles with more pairs are large
-  u32 nb;         // blocks per tile: ceil(span / kBinWidth)
-  u32 *lsz, *nch;                  // per esc tile: padded pairs if large (else 0); chunks if large
-  u32 *pp, *spp, *lpp, *chpre;     // exclusive scans over the tiles (n + 1 entries each) of the padded
-                                   // pairs, of those of the small tiles, of the large tiles, and of nch
-  u32 *chunk_tile;  // chunk -> esc index
-  u32 *first;       // window -> first esc index s with spp[s] >= window start
+  u32 n;                  // expanded tiles
+  u32 small_max;          // tiles with more pairs are large
+  u32 nb;                 // blocks per tile: ceil(span / kBinWidth)
+  u32 span, LB, rows;     // local key = slot x LB + column < span = rows x LB
+  u64 spanm, lbm;         // magic_for(span), magic_for(LB)
+  const u32 *tiles;       // esc index -> tile
+  const u64 *base;        // esc index -> first pair (base[0] = 0)
+  u64 total;              // pairs
+  u32 *keys;              // the padded regions
+  u64 *vals;
+  u32 *lsz, *nch;         // per esc tile: padded pairs if large (else 0); partition chunks if large
+  u32 *pp, *spp, *lpp, *chpre, *srk;  // exclusive scans over the tiles (n + 1 entries each) of the padded
+                                      // pairs, of those of the small tiles and of the large tiles, of nch,
+                                      // and of the small tiles' count
+  u32 *small_list;        // small tiles in esc order
+  u32 *chunk_tile;        // chunk -> esc index
+  u32 *first;             // window -> first esc index s with spp[s] >= window start
   u64 max_windows;
-  u32 *hist;        // pairs per (tile, block, chunk), at nb * chpre[s] + b * nch[s] + c
-  u32 *hpre;        // exclusive scan of hist, hist_len + 1 entries
+  u32 *hist;              // pairs per (tile, block, chunk), at nb * chpre[s] + b * nch[s] + c
+  u32 *hpre;              // exclusive scan of hist, hist_len + 1 entries
   u64 hist_len;
-  u32 *bkeys;       // the large tiles' pairs, partitioned
+  u32 *bkeys;             // the large tiles' pairs, partitioned
   u64 *bvals;
   BinJob *jobs;
-  u32 *njobs;       // large-tile jobs
-  u32 *work;        // the reduction's job counter
+  u32 *njobs;             // large-tile jobs
+  u32 *work;              // the reduction's job counter
 };
 
-// Pairs [t0, t1) of esc tile s, relative to the group's first pair.
-__device__ __forceinline__ void esc_tile_range(const EscArgs &a, u32 s, u64 &t0, u64 &t1) {
-  t0 = __ldg(&a.base[s]) - a.pair0;
-  t1 = s + 1 < a.n ? __ldg(&a.base[s + 1]) - a.pair0 : a.total;
+__device__ __forceinline__ u64 bin_tile_pairs(const BinArgs &b, u32 s) {
+  return (s + 1 < b.n ? __ldg(&b.base[s + 1]) : b.total) - __ldg(&b.base[s]);
 }
 
-// One CTA: every esc tile's padded size (pp), its place in the small or the
-// large region (spp, lpp) and its partition chunks (chpre), as exclusive
-// scans over the group's tiles, 1024 tiles per step.
+// Every tile's padded size (pp), its place in the small or the large region
+// (spp, lpp), its partition chunks (chpre) and the small tiles' ranks (srk),
+// as exclusive scans over the tiles: each CTA scans 1024 tiles and writes
+// its totals (k_bin_prep), one CTA scans the totals (k_bin_prep_totals), and
+// every tile adds its CTA's offset (k_bin_prep_add).
 constexpr int kPrepThreads = 1024;
-__global__ void __launch_bounds__(kPrepThreads) k_bin_prep(EscArgs a, BinArgs b) {
-  __shared__ u32 wsum[4][kPrepThreads / 32];
-  __shared__ u32 carry[4];
+constexpr int kPrepVals = 5;
+__global__ void __launch_bounds__(kPrepThreads) k_bin_prep(BinArgs b, u32 *__restrict__ bsum) {
+  __shared__ u32 wsum[kPrepVals][kPrepThreads / 32];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x < 4) carry[threadIdx.x] = 0;
+  const u32 s = blockIdx.x * kPrepThreads + threadIdx.x;
+  u32 v[kPrepVals] = {0, 0, 0, 0, 0};  // padded pairs; the same if small / large; chunks if large; 1 if small
+  if (s < b.n) {
+    const u32 p = u32(bin_tile_pairs(b, s));
+    const u32 pad = (p + kBinPer - 1) / kBinPer * kBinPer;
+    const bool large = p > b.small_max;
+    v[0] = pad;
+    v[1] = large ? 0u : pad;
+    v[2] = large ? pad : 0u;
+    v[3] = large ? (pad + kBinChunk - 1) / kBinChunk : 0u;
+    v[4] = large ? 0u : 1u;
+    b.lsz[s] = v[2];
+    b.nch[s] = v[3];
+  }
+  u32 incl[kPrepVals];
+#pragma unroll
+  for (int k = 0; k < kPrepVals; k++) {
+    incl[k] = warp_incl_u32(v[k]);
+    if (lane == 31) wsum[k][warp] = incl[k];
+  }
   __syncthreads();
-  for (u32 c0 = 0; c0 < a.n; c0 += kPrepThreads) {
-    const u32 s = c0 + threadIdx.x;
-    u32 v[4] = {0, 0, 0, 0};  // padded pairs; the same if small / large; chunks if large
-    if (s < a.n) {
-      u64 t0, t1;
-      esc_tile_range(a, s, t0, t1);
-      const u32 p = u32(t1 - t0);
-      const u32 pad = (p + kBinPer - 1) / kBinPer * kBinPer;
-      const bool large = p > b.small_max;
-      v[0] = pad;
-      v[1] = large ? 0u : pad;
-      v[2] = large ? pad : 0u;
-      v[3] = large ? (pad + kBinChunk - 1) / kBinChunk : 0u;
-      b.lsz[s] = v[2];
-      b.nch[s] = v[3];
-    }
-    u32 incl[4];
+  if (warp < kPrepVals) {  // warp k scans the warp sums of value k
+    const u32 x = wsum[warp][lane], xi = warp_incl_u32(x);
+    wsum[warp][lane] = xi - x;
+    if (lane == 31) bsum[u64(warp) * gridDim.x + blockIdx.x] = xi;
+  }
+  __syncthreads();
+  u32 *dst[kPrepVals] = {b.pp, b.spp, b.lpp, b.chpre, b.srk};
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      incl[k] = warp_incl_u32(v[k]);
-      if (lane == 31) wsum[k][warp] = incl[k];
-    }
+  for (int k = 0; k < kPrepVals; k++)
+    if (s < b.n) dst[k][s] = wsum[k][warp] + incl[k] - v[k];
+}
+
+// Exclusive scan of the CTA totals in place (nblk per value); the grand
+// totals go to entry n of each scan.
+__global__ void __launch_bounds__(kPrepThreads) k_bin_prep_totals(BinArgs b, u32 *__restrict__ bsum, u32 nblk) {
+  __shared__ u32 wsum[kPrepThreads / 32];
+  __shared__ u32 carry;
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  u32 *dst[kPrepVals] = {b.pp, b.spp, b.lpp, b.chpre, b.srk};
+  for (int k = 0; k < kPrepVals; k++) {
+    if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    if (warp < 4) {  // warp k scans the 32 warp sums of value k
-      const u32 x = wsum[warp][lane], xi = warp_incl_u32(x);
-      wsum[warp][lane] = xi - x;
+    u32 *t = bsum + u64(k) * nblk;
+    for (u32 c0 = 0; c0 < nblk; c0 += kPrepThreads) {
+      const u32 i = c0 + threadIdx.x;
+      const u32 v = i < nblk ? t[i] : 0u, incl = warp_incl_u32(v);
+      if (lane == 31) wsum[warp] = incl;
+      __syncthreads();
+      if (warp == 0) {
+        const u32 x = wsum[lane], xi = warp_incl_u32(x);
+        wsum[lane] = xi - x;
+      }
+      __syncthreads();
+      if (i < nblk) t[i] = carry + wsum[warp] + incl - v;
+      __syncthreads();
+      if (threadIdx.x == kPrepThreads - 1) carry += wsum[warp] + incl;
+      __syncthreads();
     }
-    __syncthreads();
-    u32 *dst[4] = {b.pp, b.spp, b.lpp, b.chpre};
-#pragma unroll
-    for (int k = 0; k < 4; k++)
-      if (s < a.n) dst[k][s] = carry[k] + wsum[k][warp] + incl[k] - v[k];
-    __syncthreads();
-    if (threadIdx.x == kPrepThreads - 1) {
-#pragma unroll
-      for (int k = 0; k < 4; k++) carry[k] += wsum[k][warp] + incl[k];
-    }
+    if (threadIdx.x == 0) dst[k][b.n] = carry;
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    b.pp[a.n] = carry[0];
-    b.spp[a.n] = carry[1];
-    b.lpp[a.n] = carry[2];
-    b.chpre[a.n] = carry[3];
+}
+
+__global__ void __launch_bounds__(kPrepThreads) k_bin_prep_add(BinArgs b, const u32 *__restrict__ bsum) {
+  const u32 s = blockIdx.x * kPrepThreads + threadIdx.x;
+  if (s >= b.n) return;
+  u32 *dst[kPrepVals] = {b.pp, b.spp, b.lpp, b.chpre, b.srk};
+#pragma unroll
+  for (int k = 0; k < kPrepVals; k++) dst[k][s] += bsum[u64(k) * gridDim.x + blockIdx.x];
+}
+
+// chunk_tile for the large tiles' chunks; small_list; first[w] = the first
+// esc index s with spp[s] >= w * kBinWindow (n when none), for every window
+// and one past.
+__global__ void k_bin_index(BinArgs b) {
+  const u64 i0 = u64(blockIdx.x) * blockDim.x + threadIdx.x, nth = u64(gridDim.x) * blockDim.x;
+  for (u64 s = i0; s < b.n; s += nth) {
+    const u32 c0 = b.chpre[s], nc = b.nch[s];
+    for (u32 c = 0; c < nc; c++) b.chunk_tile[c0 + c] = u32(s);
+    if (nc == 0) b.small_list[b.srk[s]] = u32(s);
+  }
+  const u64 nwin = (u64(b.spp[b.n]) + kBinWindow - 1) / kBinWindow;
+  for (u64 w = i0; w <= nwin && w < b.max_windows; w += nth) {
+    const u64 x = w * kBinWindow;
+    u32 lo = 0, hi = b.n;  // the first s in [lo, hi] with spp[s] >= x (spp[n] = the region's size)
+    while (lo < hi) {
+      const u32 m = (lo + hi) >> 1;
+      if (u64(b.spp[m]) >= x) hi = m;
+      else lo = m + 1;
+    }
+    b.first[w] = lo;
   }
 }
 
@@ -2191,17 +2249,16 @@ __global__ void __launch_bounds__(kPrepThreads) k_bin_prep(EscArgs a, BinArgs b)
 // segment) and store next to each other. Each lane finds its tile and A
 // entry by binary search once and then walks forward.
 template <class ColT>
-__global__ void __launch_bounds__(256) k_bin_expand(EscArgs a, BinArgs b, const ProdSrc src,
-                                                    const ColT *__restrict__ colB, const u32 *__restrict__ tile_abeg) {
-  u32 *keys = static_cast<u32 *>(a.keys);
-  const u64 ptot = b.pp[a.n], sfull = b.spp[a.n];
+__global__ void __launch_bounds__(256) k_bin_expand(BinArgs b, const ProdSrc src, const ColT *__restrict__ colB,
+                                                    const u32 *__restrict__ tile_abeg) {
+  const u64 ptot = b.pp[b.n], sfull = b.spp[b.n];
   const u32 lane = threadIdx.x & 31;
   const u64 nwarps = (u64(gridDim.x) * blockDim.x) >> 5;
   for (u64 c = (u64(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; c * 256 < ptot; c += nwarps) {
     const u64 q0 = c * 256 + lane;
     u32 s;
     {
-      u32 lo = 0, hi = a.n;  // pp[lo] <= q0 < pp[hi] (pp[n] = ptot)
+      u32 lo = 0, hi = b.n;  // pp[lo] <= q0 < pp[hi] (pp[n] = ptot)
       while (hi - lo > 1) {
         const u32 m = (lo + hi) >> 1;
         if (u64(__ldg(&b.pp[m])) <= q0) lo = m;
@@ -2210,7 +2267,7 @@ __global__ void __launch_bounds__(256) k_bin_expand(EscArgs a, BinArgs b, const 
       s = lo;
     }
     u64 tb = 0, te = 0, cnt = 0, d0 = 0, p0 = 0;  // the tile: padded [tb, te), pairs, destination, first product
-    u32 ea = 0, eb = 0;
+    u32 ea = 0, eb = 0, kt = 0;                   // its A entries; its key offset (rank in the window x span)
     u32 e = kNoEntry, sb = 0;
     u64 pe = 0, pn = 0;
     double va = 0.0;
@@ -2226,11 +2283,16 @@ __global__ void __launch_bounds__(256) k_bin_expand(EscArgs a, BinArgs b, const 
         fresh = false;
         tb = __ldg(&b.pp[s]);
         te = __ldg(&b.pp[s + 1]);
-        u64 t0, t1;
-        esc_tile_range(a, s, t0, t1);
-        cnt = t1 - t0;
-        d0 = __ldg(&b.nch[s]) == 0 ? u64(__ldg(&b.spp[s])) : sfull + __ldg(&b.lpp[s]);
-        const u32 t = a.tiles[s];
+        cnt = bin_tile_pairs(b, s);
+        if (__ldg(&b.nch[s]) == 0) {
+          const u32 sp = __ldg(&b.spp[s]);
+          d0 = sp;
+          kt = (__ldg(&b.srk[s]) - __ldg(&b.srk[__ldg(&b.first[sp / kBinWindow])])) * b.span;
+        } else {
+          d0 = sfull + __ldg(&b.lpp[s]);
+          kt = 0;
+        }
+        const u32 t = b.tiles[s];
         ea = tile_abeg[t];
         eb = tile_abeg[t + 1];
         p0 = __ldg(&src.P[ea]);
@@ -2253,7 +2315,7 @@ __global__ void __launch_bounds__(256) k_bin_expand(EscArgs a, BinArgs b, const 
           pn = __ldg(&src.P[e + 1]);
           sb = __ldg(&src.sbA[e]);
           va = __ldg(&src.valA[e]);
-          kb = s * u32(a.span) + __ldg(&src.slotA[e]) * u32(a.LB);
+          kb = kt + __ldg(&src.slotA[e]) * b.LB;
         }
         while (p >= pn) {  // the next A entries of the tile
           e++;
@@ -2261,64 +2323,40 @@ __global__ void __launch_bounds__(256) k_bin_expand(EscArgs a, BinArgs b, const 
           pn = __ldg(&src.P[e + 1]);
           sb = __ldg(&src.sbA[e]);
           va = __ldg(&src.valA[e]);
-          kb = s * u32(a.span) + __ldg(&src.slotA[e]) * u32(a.LB);
+          kb = kt + __ldg(&src.slotA[e]) * b.LB;
         }
         const u32 j = sb + u32(p - pe);
         key = kb + u32(__ldg(&colB[j]));
         v = va * __ldg(&src.valB[j]);
       }
-      keys[d0 + o] = key;
-      a.vals[d0 + o] = u64(__double_as_longlong(v));
+      b.keys[d0 + o] = key;
+      b.vals[d0 + o] = u64(__double_as_longlong(v));
     }
   }
 }
 
-// chunk_tile for the large tiles' chunks; first[w] = the first esc index s
-// with spp[s] >= w * kBinWindow (n when none), for every window and one past.
-__global__ void k_bin_index(EscArgs a, BinArgs b) {
-  const u64 i0 = u64(blockIdx.x) * blockDim.x + threadIdx.x, nth = u64(gridDim.x) * blockDim.x;
-  for (u64 s = i0; s < a.n; s += nth) {
-    const u32 c0 = b.chpre[s], nc = b.nch[s];
-    for (u32 c = 0; c < nc; c++) b.chunk_tile[c0 + c] = u32(s);
-  }
-  const u64 nwin = (u64(b.spp[a.n]) + kBinWindow - 1) / kBinWindow;
-  for (u64 w = i0; w <= nwin && w < b.max_windows; w += nth) {
-    const u64 x = w * kBinWindow;
-    u32 lo = 0, hi = a.n;  // the first s in [lo, hi] with spp[s] >= x (spp[n] = the region's size)
-    while (lo < hi) {
-      const u32 m = (lo + hi) >> 1;
-      if (u64(b.spp[m]) >= x) hi = m;
-      else lo = m + 1;
-    }
-    b.first[w] = lo;
-  }
-}
-
-// Positions [q0, q1) of chunk g (tile s, chunk c) in the group's buffer.
-__device__ __forceinline__ void bin_chunk(const EscArgs &a, const BinArgs &b, u32 g, u32 &s, u32 &c, u64 &q0,
-                                          u64 &q1) {
+// Positions [q0, q1) of chunk g (tile s, chunk c) in the buffer.
+__device__ __forceinline__ void bin_chunk(const BinArgs &b, u32 g, u32 &s, u32 &c, u64 &q0, u64 &q1) {
   s = b.chunk_tile[g];
   c = g - b.chpre[s];
-  const u64 l0 = u64(b.spp[a.n]) + b.lpp[s];
+  const u64 l0 = u64(b.spp[b.n]) + b.lpp[s];
   q0 = l0 + u64(c) * kBinChunk;
   q1 = min(l0 + b.lsz[s], q0 + kBinChunk);
 }
 
 // Pairs per block of each chunk of the large tiles.
-__global__ void __launch_bounds__(256) k_bin_hist(EscArgs a, BinArgs b) {
+__global__ void __launch_bounds__(256) k_bin_hist(BinArgs b) {
   __shared__ u32 h[kBinMaxBlocks];
-  const u32 nchunks = b.chpre[a.n];
-  const u32 *keys = static_cast<const u32 *>(a.keys);
+  const u32 nchunks = b.chpre[b.n];
   for (u32 g = blockIdx.x; g < nchunks; g += gridDim.x) {
     for (u32 i = threadIdx.x; i < b.nb; i += blockDim.x) h[i] = 0;
     __syncthreads();
     u32 s, c;
     u64 q0, q1;
-    bin_chunk(a, b, g, s, c, q0, q1);
-    const u32 kb = s * u32(a.span);  // keys (s x span + local key) fit 32 bits
+    bin_chunk(b, g, s, c, q0, q1);
     for (u64 q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
-      const u32 k = keys[q];
-      if (k != kBinEmpty) atomicAdd(&h[(k - kb) >> kBinBits], 1u);
+      const u32 k = b.keys[q];
+      if (k != kBinEmpty) atomicAdd(&h[k >> kBinBits], 1u);
     }
     __syncthreads();
     const u64 r = u64(b.nb) * b.chpre[s] + c;
@@ -2328,27 +2366,24 @@ __global__ void __launch_bounds__(256) k_bin_hist(EscArgs a, BinArgs b) {
   }
 }
 
-// Each chunk's pairs to their block's positions (within a block, in the
-// order the threads reach their shared counter).
-__global__ void __launch_bounds__(256) k_bin_scatter(EscArgs a, BinArgs b) {
+// Each chunk's pairs to their block's positions; lanes of one block take
+// consecutive positions with one shared atomic.
+__global__ void __launch_bounds__(256) k_bin_scatter(BinArgs b) {
   __shared__ u32 cur[kBinMaxBlocks];
-  const u32 nchunks = b.chpre[a.n];
-  const u32 *keys = static_cast<const u32 *>(a.keys);
+  const u32 nchunks = b.chpre[b.n];
+  const u32 lane = threadIdx.x & 31;
   for (u32 g = blockIdx.x; g < nchunks; g += gridDim.x) {
     u32 s, c;
     u64 q0, q1;
-    bin_chunk(a, b, g, s, c, q0, q1);
+    bin_chunk(b, g, s, c, q0, q1);
     const u64 r = u64(b.nb) * b.chpre[s] + c;
     const u32 nc = b.nch[s];
     for (u32 i = threadIdx.x; i < b.nb; i += blockDim.x) cur[i] = b.hpre[r + u64(i) * nc];
     __syncthreads();
-    const u32 kb = s * u32(a.span);
-    const u32 lane = threadIdx.x & 31;
     for (u64 qw = q0; qw < q1; qw += blockDim.x) {  // the same trip count in every lane
       const u64 q = qw + threadIdx.x;
-      const u32 k = q < q1 ? keys[q] : kBinEmpty;
-      const u32 bin = k != kBinEmpty ? (k - kb) >> kBinBits : kBinMaxBlocks;
-      // lanes of one block take consecutive positions with one shared atomic
+      const u32 k = q < q1 ? b.keys[q] : kBinEmpty;
+      const u32 bin = k != kBinEmpty ? k >> kBinBits : kBinMaxBlocks;
       const u32 peers = __match_any_sync(kFull, bin);
       const u32 leader = __ffs(peers) - 1;
       u32 pos = 0;
@@ -2356,7 +2391,7 @@ __global__ void __launch_bounds__(256) k_bin_scatter(EscArgs a, BinArgs b) {
       pos = __shfl_sync(kFull, pos, leader) + __popc(peers & ((1u << lane) - 1u));
       if (bin < kBinMaxBlocks) {
         b.bkeys[pos] = k;
-        b.bvals[pos] = a.vals[q];
+        b.bvals[pos] = b.vals[q];
       }
     }
     __syncthreads();
@@ -2366,8 +2401,8 @@ __global__ void __launch_bounds__(256) k_bin_scatter(EscArgs a, BinArgs b) {
 // Jobs of each large tile: every block with more than kBinDenseMin pairs
 // alone (dense), runs of consecutive sparser blocks up to kBinHashPairs pairs
 // together (hash).
-__global__ void k_bin_jobs(EscArgs a, BinArgs b) {
-  for (u32 s = blockIdx.x * blockDim.x + threadIdx.x; s < a.n; s += gridDim.x * blockDim.x) {
+__global__ void k_bin_jobs(BinArgs b) {
+  for (u32 s = blockIdx.x * blockDim.x + threadIdx.x; s < b.n; s += gridDim.x * blockDim.x) {
     const u32 nc = b.nch[s];
     if (nc == 0) continue;
     const u64 r = u64(b.nb) * b.chpre[s];
@@ -2430,6 +2465,38 @@ __device__ __forceinline__ void bin_insert(u32 *tk, double *tv, u32 mask, u32 lg
   atomicAdd(&tv[h], v);  // under contention the built-in add beats a compare-and-swap loop
 }
 
+// Output row and column of a reduced key: a window's key is the tile's rank
+// in the window x span + the local key, a large tile's key the local key.
+struct BinWho {
+  bool window;
+  u32 s;      // large tile: its esc index
+  u32 rank0;  // window: the rank of its first small tile
+};
+
+struct BinRowCache {
+  u32 s = kBinEmpty, slot = 0;
+  u64 row = 0;
+};
+
+__device__ __forceinline__ void bin_emit_one(const BinArgs &b, const u32 *__restrict__ tile_rank0,
+                                             const u64 *__restrict__ urow, const Out &out, const Decode &dec,
+                                             const BinWho &who, BinRowCache &rc, u64 idx, u32 key, double v) {
+  u32 s = who.s, loc = key;
+  if (who.window) {
+    const u32 r = div_magic(key, b.spanm);
+    loc = key - r * b.span;
+    s = __ldg(&b.small_list[who.rank0 + r]);
+  }
+  const u32 slot = b.rows > 1 ? div_magic(loc, b.lbm) : 0u;
+  const u32 col = loc - slot * b.LB;
+  if (s != rc.s || slot != rc.slot) {
+    rc.s = s;
+    rc.slot = slot;
+    rc.row = __ldg(&urow[tile_rank0[b.tiles[s]] + slot]);
+  }
+  emit(out, dec, idx, rc.row, col, v);
+}
+
 // Emits the table's occupied slots (hash: tk[i] != empty; dense: bit i of
 // bitmap tk) with one reservation for the CTA; slots [0, n), n a multiple of
 // 32. Each warp packs the occupied slots of its words into a 64-entry ring
@@ -2441,9 +2508,9 @@ struct BinRing {
 };
 
 template <bool kDense>
-__device__ void bin_emit(const EscArgs &a, const u32 *__restrict__ tile_rank0, const u64 *__restrict__ urow,
-                         const Out &out, const Decode &dec, u32 *err, const u32 *tk, const double *tv, u32 n,
-                         u32 dkey0, u32 *s_wcnt, u64 *s_base, BinRing &ring) {
+__device__ void bin_emit(const BinArgs &b, const u32 *__restrict__ tile_rank0, const u64 *__restrict__ urow,
+                         const Out &out, const Decode &dec, u32 *err, const BinWho &who, const u32 *tk,
+                         const double *tv, u32 n, u32 dkey0, u32 *s_wcnt, u64 *s_base, BinRing &ring) {
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   u32 cnt = 0;
   for (u32 w = warp; w < n / 32; w += nw) {
@@ -2468,7 +2535,7 @@ __device__ void bin_emit(const EscArgs &a, const u32 *__restrict__ tile_rank0, c
     u32 *rk = ring.k[warp];
     double *rv = ring.v[warp];
     u32 head = 0, tail = 0;  // entries queued / written
-    EscRowCache rc;
+    BinRowCache rc;
     for (u32 w = warp; w < n / 32; w += nw) {
       const u32 i = w * 32 + lane;
       const u32 m = kDense ? tk[w] : __ballot_sync(kFull, tk[i] != kBinEmpty);
@@ -2481,7 +2548,7 @@ __device__ void bin_emit(const EscArgs &a, const u32 *__restrict__ tile_rank0, c
       __syncwarp();
       if (head - tail >= 32) {
         const u32 e = (tail + lane) & 63u;
-        esc_emit<u32>(a, tile_rank0, urow, out, dec, rc, idx + lane, rk[e], rv[e]);
+        bin_emit_one(b, tile_rank0, urow, out, dec, who, rc, idx + lane, rk[e], rv[e]);
         idx += 32;
         tail += 32;
         __syncwarp();
@@ -2489,7 +2556,7 @@ __device__ void bin_emit(const EscArgs &a, const u32 *__restrict__ tile_rank0, c
     }
     if (lane < head - tail) {
       const u32 e = (tail + lane) & 63u;
-      esc_emit<u32>(a, tile_rank0, urow, out, dec, rc, idx + lane, rk[e], rv[e]);
+      bin_emit_one(b, tile_rank0, urow, out, dec, who, rc, idx + lane, rk[e], rv[e]);
     }
   }
   __syncthreads();
@@ -2523,10 +2590,10 @@ __device__ __forceinline__ void bin_hash(const u32 *__restrict__ keys, const u64
   __syncthreads();
 }
 
-// Persistent CTAs take jobs from a counter: first the large tiles' jobs
-// (dense blocks and runs of sparse blocks, from the partitioned pairs), then
-// the windows of small tiles.
-__global__ void __launch_bounds__(kBinThreads) k_bin_reduce(EscArgs a, BinArgs b, const u32 *__restrict__ tile_rank0,
+// Persistent CTAs take jobs from a counter (the next one fetched while the
+// current one runs): first the large tiles' jobs (dense blocks and runs of
+// sparse blocks, from the partitioned pairs), then the windows of small tiles.
+__global__ void __launch_bounds__(kBinThreads) k_bin_reduce(BinArgs b, const u32 *__restrict__ tile_rank0,
                                                             const u64 *__restrict__ urow, const Out out,
                                                             const Decode dec, u32 *err) {
   extern __shared__ __align__(16) unsigned char bin_smem[];
@@ -2536,22 +2603,24 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_reduce(EscArgs a, BinArgs b
   __shared__ u64 s_base;
   __shared__ BinRing ring;
   const u32 nbig = *b.njobs;
-  const u64 nwin = (u64(b.spp[a.n]) + kBinWindow - 1) / kBinWindow;
+  const u64 nwin = (u64(b.spp[b.n]) + kBinWindow - 1) / kBinWindow;
   const u64 njobs = u64(nbig) + nwin;
-  const u32 *keys = static_cast<const u32 *>(a.keys);
+  if (threadIdx.x == 0) s_job = atomicAdd(b.work, 1u);
+  __syncthreads();
   for (;;) {
-    if (threadIdx.x == 0) s_job = atomicAdd(b.work, 1u);
-    __syncthreads();
     const u64 j = s_job;
     __syncthreads();
     if (j >= njobs) break;
+    u32 next = 0;
+    if (threadIdx.x == 0) next = atomicAdd(b.work, 1u);  // consumed after this job
     if (j < nbig) {
       const BinJob jb = b.jobs[j];
+      const BinWho who{false, jb.s, 0};
       const u32 nc = b.nch[jb.s];
       const u64 r = u64(b.nb) * b.chpre[jb.s];
       const u32 lo = b.hpre[r + u64(jb.b0) * nc], hi = b.hpre[r + u64(jb.b1) * nc];
       if (jb.b1 == jb.b0 + 1 && hi - lo > kBinDenseMin) {  // dense block
-        const u32 k0 = jb.s * u32(a.span) + u32(jb.b0) * kBinWidth;
+        const u32 k0 = u32(jb.b0) * kBinWidth;
         for (u32 i = threadIdx.x; i < kBinWidth; i += blockDim.x) tv[i] = 0.0;
         for (u32 i = threadIdx.x; i < kBinWidth / 32; i += blockDim.x) tk[i] = 0u;
         __syncthreads();
@@ -2573,19 +2642,22 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_reduce(EscArgs a, BinArgs b
           }
         }
         __syncthreads();
-        bin_emit<true>(a, tile_rank0, urow, out, dec, err, tk, tv, kBinWidth, k0, s_wcnt, &s_base, ring);
+        bin_emit<true>(b, tile_rank0, urow, out, dec, err, who, tk, tv, kBinWidth, k0, s_wcnt, &s_base, ring);
       } else {  // sparse blocks: at most kBinHashPairs pairs
         u32 slots;
         bin_hash(b.bkeys, b.bvals, lo, hi, tk, tv, slots);
-        bin_emit<false>(a, tile_rank0, urow, out, dec, err, tk, tv, slots, 0, s_wcnt, &s_base, ring);
+        bin_emit<false>(b, tile_rank0, urow, out, dec, err, who, tk, tv, slots, 0, s_wcnt, &s_base, ring);
       }
     } else {  // a window of small tiles: fewer than kBinWindow + small_max positions
       const u64 w = j - nbig;
-      const u32 lo = b.spp[b.first[w]], hi = b.spp[b.first[w + 1]];
+      const u32 f0 = b.first[w], f1 = b.first[w + 1];
+      const BinWho who{true, 0, b.srk[f0]};
       u32 slots;
-      bin_hash(keys, a.vals, lo, hi, tk, tv, slots);
-      bin_emit<false>(a, tile_rank0, urow, out, dec, err, tk, tv, slots, 0, s_wcnt, &s_base, ring);
+      bin_hash(b.keys, b.vals, b.spp[f0], b.spp[f1], tk, tv, slots);
+      bin_emit<false>(b, tile_rank0, urow, out, dec, err, who, tk, tv, slots, 0, s_wcnt, &s_base, ring);
     }
+    if (threadIdx.x == 0) s_job = next;
+    __syncthreads();
   }
 }
 
@@ -3206,14 +3278,58 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   std::vector<EscGroup> escg;
   const u64 esc_span = esc_rows * LB;
   const bool esc_k32 = esc_span <= 0xFFFFFFFFull;
-  // Groups reduced in shared memory (32-bit keys, a span of at most
-  // kBinMaxBlocks blocks) share one set of scratch buffers, sized for the
-  // largest group; the rest are sorted.
+  // Expanded tiles are reduced in shared memory (one set of launches, keys
+  // local to a window or a tile) when a tile spans at most kBinMaxBlocks key
+  // blocks and the padded pairs count in 32 bits; otherwise they are sorted
+  // in groups whose keys fit 32 bits.
   const u32 bin_nb = u32((esc_span + kBinWidth - 1) / kBinWidth);
-  const bool binned = esc_k32 && esc_span <= u64(kBinMaxBlocks) * kBinWidth && opt.esc_reduce != 2;
   const u32 bin_small = opt.esc_small > 0 ? u32(opt.esc_small) : kBinSmallMax;
+  const bool binned = nesc > 0 && opt.esc_reduce != 2 && esc_span <= u64(kBinMaxBlocks) * kBinWidth &&
+                      esc_pairs + u64(kBinPer) * nesc < 0xFFFFFFFFull;
   BinArgs bins{};
-  if (nesc > 0) {
+  u32 *bin_bsum = nullptr;
+  u32 bin_nblk = 0;
+  if (binned) {
+    const u64 cap = esc_pairs + u64(kBinPer) * nesc;  // with every tile's padding
+    const u64 maxch = cap / kBinChunk + esc_pairs / (u64(bin_small) + 1) + 1;  // a large tile has > small_max pairs
+    bins.n = nesc;
+    bins.small_max = bin_small;
+    bins.nb = bin_nb;
+    bins.span = u32(esc_span);
+    bins.LB = u32(LB);
+    bins.rows = u32(esc_rows);
+    bins.spanm = magic_for(esc_span);
+    bins.lbm = magic_for(LB);
+    bins.tiles = esc_tiles;
+    bins.base = esc_base;
+    bins.total = esc_pairs;
+    bins.keys = ar.get_n<u32>(cap);
+    bins.vals = ar.get_n<u64>(cap);
+    u32 *per = ar.get_n<u32>(3 * u64(nesc));
+    bins.lsz = per;
+    bins.nch = per + nesc;
+    bins.small_list = per + 2 * u64(nesc);
+    u32 *pre = ar.get_n<u32>(5 * (u64(nesc) + 1));
+    bins.pp = pre;
+    bins.spp = pre + (nesc + 1);
+    bins.lpp = pre + 2 * (u64(nesc) + 1);
+    bins.chpre = pre + 3 * (u64(nesc) + 1);
+    bins.srk = pre + 4 * (u64(nesc) + 1);
+    bin_nblk = (nesc + kPrepThreads - 1) / kPrepThreads;
+    bin_bsum = ar.get_n<u32>(u64(kPrepVals) * bin_nblk);
+    bins.chunk_tile = ar.get_n<u32>(maxch);
+    bins.max_windows = cap / kBinWindow + 2;
+    bins.first = ar.get_n<u32>(bins.max_windows);
+    bins.hist_len = u64(bin_nb) * maxch;
+    bins.hist = ar.get_n<u32>(bins.hist_len);
+    bins.hpre = ar.get_n<u32>(bins.hist_len + 1);
+    bins.bkeys = ar.get_n<u32>(esc_pairs);
+    bins.bvals = ar.get_n<u64>(esc_pairs);
+    bins.jobs = ar.get_n<BinJob>(u64(bin_nb) * std::min<u64>(nesc, esc_pairs / (u64(bin_small) + 1) + 1));
+    bins.njobs = ar.get_n<u32>(2);
+    bins.work = bins.njobs + 1;
+  }
+  if (nesc > 0 && !binned) {
     u64 G = esc_k32 ? std::max<u64>(1, 0xFFFFFFFFull / esc_span) : u64(nesc);
     if (opt.esc_group > 0) G = std::min<u64>(G, u64(opt.esc_group));
     const u32 ng = u32((u64(nesc) + G - 1) / G);
@@ -3232,46 +3348,14 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       EscGroup e{EscArgs{esc_tiles + s0, esc_base + s0, n, esc_span, LB, esc_rows, magic_for(LB), magic_for(esc_rows),
                          start[g], nullptr, nullptr, pairs},
                  nullptr, nullptr, 0, 1, 0};
-      const u64 cap = binned ? pairs + u64(kBinPer) * n : pairs;  // binned: every tile padded to 8 pairs
-      e.a.keys = esc_k32 ? static_cast<void *>(ar.get_n<u32>(cap)) : static_cast<void *>(ar.get_n<u64>(cap));
-      e.a.vals = ar.get_n<u64>(cap);
+      e.a.keys = esc_k32 ? static_cast<void *>(ar.get_n<u32>(pairs)) : static_cast<void *>(ar.get_n<u64>(pairs));
+      e.a.vals = ar.get_n<u64>(pairs);
       e.chunks = (pairs + kEscChunk - 1) / kEscChunk;
       e.heads = ar.get_n<u32>(e.chunks);
       e.offc = ar.get_n<u32>(e.chunks);
       e.grid = int(std::max<u64>(1, std::min<u64>((e.chunks + 7) / 8, u64(ctx->num_sms) * 8)));
       e.bits = bits_for(u64(n) * esc_span - 1);
       escg.push_back(e);
-    }
-    if (binned) {
-      u64 maxn = 0, maxp = 0, maxch = 0, maxjobs = 0;
-      for (const EscGroup &e : escg) {
-        const u64 cap = e.a.total + u64(kBinPer) * e.a.n;  // with every tile's padding
-        maxn = std::max<u64>(maxn, e.a.n);
-        maxp = std::max<u64>(maxp, cap);
-        maxch = std::max<u64>(maxch, cap / kBinChunk + e.a.n);
-        maxjobs = std::max<u64>(maxjobs, u64(bin_nb) * std::min<u64>(e.a.n, e.a.total / (u64(bin_small) + 1) + 1));
-      }
-      bins.small_max = bin_small;
-      bins.nb = bin_nb;
-      u32 *per = ar.get_n<u32>(2 * maxn);
-      bins.lsz = per;
-      bins.nch = per + maxn;
-      u32 *pre = ar.get_n<u32>(4 * (maxn + 1));
-      bins.pp = pre;
-      bins.spp = pre + (maxn + 1);
-      bins.lpp = pre + 2 * (maxn + 1);
-      bins.chpre = pre + 3 * (maxn + 1);
-      bins.chunk_tile = ar.get_n<u32>(maxch);
-      bins.max_windows = maxp / kBinWindow + 2;
-      bins.first = ar.get_n<u32>(bins.max_windows);
-      bins.hist_len = u64(bin_nb) * maxch;
-      bins.hist = ar.get_n<u32>(bins.hist_len);
-      bins.hpre = ar.get_n<u32>(bins.hist_len + 1);
-      bins.bkeys = ar.get_n<u32>(maxp);
-      bins.bvals = ar.get_n<u64>(maxp);
-      bins.jobs = ar.get_n<BinJob>(std::max<u64>(maxjobs, 1));
-      bins.njobs = ar.get_n<u32>(2);
-      bins.work = bins.njobs + 1;
     }
   }
   const u64 words = dense ? (area + 31) / 32 : 0;
@@ -3500,39 +3584,39 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
         k_merge_hash<ColT><<<std::min<u32>(nsplit_h, u32(ctx->num_sms) * 2), kMergeThreads, 0, st>>>(ha);
         FCC_LAUNCH_CHECK();
       }
+      if (binned) {  // expand (the pairs stay for a retry), partition the large tiles, reduce
+        if (attempt == 0) {
+          const u32 pgrid = bin_nblk;
+          k_bin_prep<<<pgrid, kPrepThreads, 0, st>>>(bins, bin_bsum);
+          FCC_LAUNCH_CHECK();
+          k_bin_prep_totals<<<1, kPrepThreads, 0, st>>>(bins, bin_bsum, pgrid);
+          FCC_LAUNCH_CHECK();
+          k_bin_prep_add<<<pgrid, kPrepThreads, 0, st>>>(bins, bin_bsum);
+          FCC_LAUNCH_CHECK();
+          k_bin_index<<<grid_for(i64(std::max<u64>(nesc, bins.max_windows)), 256), 256, 0, st>>>(bins);
+          FCC_LAUNCH_CHECK();
+          const u64 cap = esc_pairs + u64(kBinPer) * nesc;
+          const u32 xgrid = u32(std::max<u64>(1, std::min<u64>((cap + 2047) / 2048, u64(ctx->num_sms) * 16)));
+          k_bin_expand<ColT><<<xgrid, 256, 0, st>>>(bins, src, colptr, tile_abeg);
+          FCC_LAUNCH_CHECK();
+          FCC_CUDA(cudaMemsetAsync(bins.hist, 0, sizeof(u32) * bins.hist_len, st));
+          const int cgrid = ctx->num_sms * 8;
+          k_bin_hist<<<cgrid, 256, 0, st>>>(bins);
+          FCC_LAUNCH_CHECK();
+          scan_exclusive(bins.hist, bins.hpre, i64(bins.hist_len), bins.hpre + bins.hist_len, ar, st);
+          k_bin_scatter<<<cgrid, 256, 0, st>>>(bins);
+          FCC_LAUNCH_CHECK();
+          FCC_CUDA(cudaMemsetAsync(bins.njobs, 0, sizeof(u32), st));
+          k_bin_jobs<<<grid_for(nesc, 256), 256, 0, st>>>(bins);
+          FCC_LAUNCH_CHECK();
+        }
+        FCC_CUDA(cudaMemsetAsync(bins.work, 0, sizeof(u32), st));  // (a retry runs the reduction again)
+        FCC_CUDA(cudaFuncSetAttribute(k_bin_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kBinSmem)));
+        k_bin_reduce<<<ctx->num_sms * 2, kBinThreads, kBinSmem, st>>>(bins, tile_rank0, urow, o, dec, ctx->d_err);
+        FCC_LAUNCH_CHECK();
+      }
       for (const EscGroup &e : escg) {  // expanded tiles: expand, sort, reduce, group by group
         const EscArgs &ea = e.a;
-        if (binned) {  // plan, expand (the pairs stay for a retry), partition the large tiles, reduce
-          const int tgrid = grid_for(ea.n, 256);
-          BinArgs bg = bins;
-          const u64 cap = ea.total + u64(kBinPer) * ea.n;
-          bg.max_windows = cap / kBinWindow + 2;
-          bg.hist_len = u64(bin_nb) * (cap / kBinChunk + ea.n);
-          // (a retry repeats all but the expansion: the scratch is shared by the groups)
-          k_bin_prep<<<1, kPrepThreads, 0, st>>>(ea, bg);
-          FCC_LAUNCH_CHECK();
-          if (attempt == 0) {
-            const u32 xgrid = u32(std::max<u64>(1, std::min<u64>((cap + 2047) / 2048, u64(ctx->num_sms) * 16)));
-            k_bin_expand<ColT><<<xgrid, 256, 0, st>>>(ea, bg, src, colptr, tile_abeg);
-            FCC_LAUNCH_CHECK();
-          }
-          k_bin_index<<<grid_for(i64(std::max<u64>(ea.n, bg.max_windows)), 256), 256, 0, st>>>(ea, bg);
-          FCC_LAUNCH_CHECK();
-          FCC_CUDA(cudaMemsetAsync(bg.hist, 0, sizeof(u32) * bg.hist_len, st));
-          const int cgrid = ctx->num_sms * 8;
-          k_bin_hist<<<cgrid, 256, 0, st>>>(ea, bg);
-          FCC_LAUNCH_CHECK();
-          scan_exclusive(bg.hist, bg.hpre, i64(bg.hist_len), bg.hpre + bg.hist_len, ar, st);
-          k_bin_scatter<<<cgrid, 256, 0, st>>>(ea, bg);
-          FCC_LAUNCH_CHECK();
-          FCC_CUDA(cudaMemsetAsync(bg.njobs, 0, 2 * sizeof(u32), st));
-          k_bin_jobs<<<tgrid, 256, 0, st>>>(ea, bg);
-          FCC_LAUNCH_CHECK();
-          FCC_CUDA(cudaFuncSetAttribute(k_bin_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kBinSmem)));
-          k_bin_reduce<<<ctx->num_sms * 2, kBinThreads, kBinSmem, st>>>(ea, bg, tile_rank0, urow, o, dec, ctx->d_err);
-          FCC_LAUNCH_CHECK();
-          continue;
-        }
         if (attempt == 0) {  // the sorted pairs stay for a retry
           const u32 xgrid = u32(std::max<u64>(1, std::min<u64>((ea.total + 2047) / 2048, u64(ctx->num_sms) * 8)));
           if (esc_k32) {
