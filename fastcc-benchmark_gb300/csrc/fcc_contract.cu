@@ -2064,26 +2064,27 @@ __global__ void __launch_bounds__(256) k_esc_reduce(EscArgs a, const u32 *__rest
 
 // ------------------------------- expanded pairs reduced in shared memory ----
 //
-// Instead of being sorted, the expanded pairs are written tile by tile into
-// two regions of one buffer, every tile padded to a multiple of eight pairs
-// (padding keys are kBinEmpty):
-//  * small tiles (at most small_max pairs) first. Windows of kBinWindow
+// Instead of being sorted, the expanded pairs are reduced in shared memory:
+//  * small tiles (at most small_max pairs): windows of kBinWindow
 //    positions over this region, each taking the tiles that start in it
 //    (fewer than kBinWindow + small_max positions and at most
 //    kBinWindow / 8 + 1 tiles, one contiguous range), are reduced in
-//    shared-memory hash tables; a small tile's key is its rank among the
-//    window's tiles x span + its local key (slot x LB + column);
-//  * then the large tiles (hub rows), keyed by the local key alone. Each is
-//    partitioned by blocks of kBinWidth consecutive local keys: every chunk
-//    of kBinChunk positions counts its pairs per block, one exclusive scan
-//    over (tile, block, chunk) gives every chunk its positions, and the chunk
-//    scatters its pairs there. A block with more than kBinDenseMin pairs is
-//    reduced in a dense kBinWidth-entry accumulator with a bitmap of touched
-//    keys, runs of consecutive sparser blocks together in one hash table.
+//    shared-memory hash tables. Their pairs are written tile by tile, each
+//    tile padded to a multiple of eight pairs (padding keys are kBinEmpty);
+//    a small tile's key is its rank among the window's tiles x span + its
+//    local key (slot x LB + column);
+//  * the large tiles (hub rows) are expanded straight into blocks of
+//    kBinWidth consecutive local keys (slot x LB + column), keyed by the
+//    local key alone: every chunk of kBinChunk of a tile's products counts
+//    its pairs per block, one exclusive scan over (tile, block, chunk) gives
+//    every chunk its positions, and the chunk computes its products again
+//    and writes each pair there. A block with more than kBinDenseMin pairs
+//    is reduced in a dense kBinWidth-entry accumulator with a bitmap of
+//    touched keys, runs of consecutive sparser blocks together in one hash
+//    table.
 // Every reduced window or block reserves its outputs with one atomic and
-// writes them. After the expansion a small tile's pair is read once, a large
-// tile's twice and written once more; keys never need more than 32 bits, so
-// every expanded tile goes through one set of launches.
+// writes them. Every pair is written once and read once; keys never need
+// more than 32 bits, so every expanded tile goes through one set of launches.
 
 constexpr u32 kBinBits = 13;
 constexpr u32 kBinWidth = 1u << kBinBits;  // local keys per block: 8192 doubles, 64 KB
@@ -2114,12 +2115,11 @@ struct BinArgs {
   const u32 *tiles;       // esc index -> tile
   const u64 *base;        // esc index -> first pair (base[0] = 0)
   u64 total;              // pairs
-  u32 *keys;              // the padded regions
+  u32 *keys;              // the small tiles' pairs, padded
   u64 *vals;
-  u32 *lsz, *nch;         // per esc tile: padded pairs if large (else 0); partition chunks if large
-  u32 *pp, *spp, *lpp, *chpre, *srk;  // exclusive scans over the tiles (n + 1 entries each) of the padded
-                                      // pairs, of those of the small tiles and of the large tiles, of nch,
-                                      // and of the small tiles' count
+  u32 *nch;               // per esc tile: partition chunks if large, else 0
+  u32 *spp, *chpre, *srk; // exclusive scans over the tiles (n + 1 entries each) of the small tiles'
+                          // padded pairs, of nch, and of the small tiles' count
   u32 *small_list;        // small tiles in esc order
   u32 *chunk_tile;        // chunk -> esc index
   u32 *first;             // window -> first esc index s with spp[s] >= window start
@@ -2138,29 +2138,25 @@ __device__ __forceinline__ u64 bin_tile_pairs(const BinArgs &b, u32 s) {
   return (s + 1 < b.n ? __ldg(&b.base[s + 1]) : b.total) - __ldg(&b.base[s]);
 }
 
-// Every tile's padded size (pp), its place in the small or the large region
-// (spp, lpp), its partition chunks (chpre) and the small tiles' ranks (srk),
-// as exclusive scans over the tiles: each CTA scans 1024 tiles and writes
-// its totals (k_bin_prep), one CTA scans the totals (k_bin_prep_totals), and
-// every tile adds its CTA's offset (k_bin_prep_add).
+// Every tile's place in the small region (spp), its partition chunks
+// (chpre) and the small tiles' ranks (srk), as exclusive scans over the
+// tiles: each CTA scans 1024 tiles and writes its totals (k_bin_prep), one
+// CTA scans the totals (k_bin_prep_totals), and every tile adds its CTA's
+// offset (k_bin_prep_add).
 constexpr int kPrepThreads = 1024;
-constexpr int kPrepVals = 5;
+constexpr int kPrepVals = 3;
 __global__ void __launch_bounds__(kPrepThreads) k_bin_prep(BinArgs b, u32 *__restrict__ bsum) {
   __shared__ u32 wsum[kPrepVals][kPrepThreads / 32];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const u32 s = blockIdx.x * kPrepThreads + threadIdx.x;
-  u32 v[kPrepVals] = {0, 0, 0, 0, 0};  // padded pairs; the same if small / large; chunks if large; 1 if small
+  u32 v[kPrepVals] = {0, 0, 0};  // padded pairs if small; chunks if large; 1 if small
   if (s < b.n) {
     const u32 p = u32(bin_tile_pairs(b, s));
-    const u32 pad = (p + kBinPer - 1) / kBinPer * kBinPer;
     const bool large = p > b.small_max;
-    v[0] = pad;
-    v[1] = large ? 0u : pad;
-    v[2] = large ? pad : 0u;
-    v[3] = large ? (pad + kBinChunk - 1) / kBinChunk : 0u;
-    v[4] = large ? 0u : 1u;
-    b.lsz[s] = v[2];
-    b.nch[s] = v[3];
+    v[0] = large ? 0u : (p + kBinPer - 1) / kBinPer * kBinPer;
+    v[1] = large ? (p + kBinChunk - 1) / kBinChunk : 0u;
+    v[2] = large ? 0u : 1u;
+    b.nch[s] = v[1];
   }
   u32 incl[kPrepVals];
 #pragma unroll
@@ -2175,7 +2171,7 @@ __global__ void __launch_bounds__(kPrepThreads) k_bin_prep(BinArgs b, u32 *__res
     if (lane == 31) bsum[u64(warp) * gridDim.x + blockIdx.x] = xi;
   }
   __syncthreads();
-  u32 *dst[kPrepVals] = {b.pp, b.spp, b.lpp, b.chpre, b.srk};
+  u32 *dst[kPrepVals] = {b.spp, b.chpre, b.srk};
 #pragma unroll
   for (int k = 0; k < kPrepVals; k++)
     if (s < b.n) dst[k][s] = wsum[k][warp] + incl[k] - v[k];
@@ -2187,7 +2183,7 @@ __global__ void __launch_bounds__(kPrepThreads) k_bin_prep_totals(BinArgs b, u32
   __shared__ u32 wsum[kPrepThreads / 32];
   __shared__ u32 carry;
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  u32 *dst[kPrepVals] = {b.pp, b.spp, b.lpp, b.chpre, b.srk};
+  u32 *dst[kPrepVals] = {b.spp, b.chpre, b.srk};
   for (int k = 0; k < kPrepVals; k++) {
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
@@ -2215,7 +2211,7 @@ __global__ void __launch_bounds__(kPrepThreads) k_bin_prep_totals(BinArgs b, u32
 __global__ void __launch_bounds__(kPrepThreads) k_bin_prep_add(BinArgs b, const u32 *__restrict__ bsum) {
   const u32 s = blockIdx.x * kPrepThreads + threadIdx.x;
   if (s >= b.n) return;
-  u32 *dst[kPrepVals] = {b.pp, b.spp, b.lpp, b.chpre, b.srk};
+  u32 *dst[kPrepVals] = {b.spp, b.chpre, b.srk};
 #pragma unroll
   for (int k = 0; k < kPrepVals; k++) dst[k][s] += bsum[u64(k) * gridDim.x + blockIdx.x];
 }
@@ -2243,121 +2239,148 @@ __global__ void k_bin_index(BinArgs b) {
   }
 }
 
-// Expansion into the two padded regions. A warp takes 256 consecutive
-// positions of the padded order, lane l the positions l, l + 32, ...: lanes
-// next to each other read B entries next to each other (one A entry's
-// segment) and store next to each other. Each lane finds its tile and A
-// entry by binary search once and then walks forward.
+// The A entry holding product p of a tile whose entries are [ea, eb).
+__device__ __forceinline__ u32 bin_entry_of(const u64 *__restrict__ P, u32 ea, u32 eb, u64 p) {
+  u32 l = ea, h = eb;  // P[l] <= p < P[h]
+  while (h - l > 1) {
+    const u32 m = (l + h) >> 1;
+    if (__ldg(&P[m]) <= p) l = m;
+    else h = m;
+  }
+  return l;
+}
+
+// A lane's walk over the products of one tile, forward only.
+struct BinWalk {
+  u32 e = kNoEntry, sb = 0, kb = 0;
+  u64 pe = 0, pn = 0;
+  double va = 0.0;
+  __device__ __forceinline__ void load(const ProdSrc &src, u32 kt, u32 LB) {
+    pe = __ldg(&src.P[e]);
+    pn = __ldg(&src.P[e + 1]);
+    sb = __ldg(&src.sbA[e]);
+    va = __ldg(&src.valA[e]);
+    kb = kt + __ldg(&src.slotA[e]) * LB;
+  }
+  // key kb + column and value of product p (p at or after the current entry's first)
+  template <class ColT>
+  __device__ __forceinline__ void at(const ProdSrc &src, const ColT *__restrict__ colB, u32 kt, u32 LB, u64 p,
+                                     bool want_val, u32 &key, double &v) {
+    while (p >= pn) {
+      e++;
+      load(src, kt, LB);
+    }
+    const u32 j = sb + u32(p - pe);
+    key = kb + u32(__ldg(&colB[j]));
+    v = want_val ? va * __ldg(&src.valB[j]) : 0.0;
+  }
+};
+
+// Expansion of the small tiles into their padded region. A warp takes 256
+// consecutive positions, lane l the positions l, l + 32, ...: lanes next to
+// each other read B entries next to each other (one A entry's segment) and
+// store next to each other. The warp finds the tile of its first position
+// by binary search; lanes walk forward from there.
 template <class ColT>
 __global__ void __launch_bounds__(256) k_bin_expand(BinArgs b, const ProdSrc src, const ColT *__restrict__ colB,
                                                     const u32 *__restrict__ tile_abeg) {
-  const u64 ptot = b.pp[b.n], sfull = b.spp[b.n];
+  const u64 ptot = b.spp[b.n];
   const u32 lane = threadIdx.x & 31;
   const u64 nwarps = (u64(gridDim.x) * blockDim.x) >> 5;
   for (u64 c = (u64(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; c * 256 < ptot; c += nwarps) {
-    const u64 q0 = c * 256 + lane;
+    // the last s with spp[s] <= c * 256: a small tile (large tiles tie with the small tile after them)
     u32 s;
     {
-      u32 lo = 0, hi = b.n;  // pp[lo] <= q0 < pp[hi] (pp[n] = ptot)
+      u32 lo = 0, hi = b.n;  // spp[lo] <= x < spp[hi] (spp[n] = ptot)
+      const u64 x = c * 256;
       while (hi - lo > 1) {
         const u32 m = (lo + hi) >> 1;
-        if (u64(__ldg(&b.pp[m])) <= q0) lo = m;
+        if (u64(__ldg(&b.spp[m])) <= x) lo = m;
         else hi = m;
       }
       s = lo;
     }
-    u64 tb = 0, te = 0, cnt = 0, d0 = 0, p0 = 0;  // the tile: padded [tb, te), pairs, destination, first product
-    u32 ea = 0, eb = 0, kt = 0;                   // its A entries; its key offset (rank in the window x span)
-    u32 e = kNoEntry, sb = 0;
-    u64 pe = 0, pn = 0;
-    double va = 0.0;
-    u32 kb = 0;
+    u64 tb = 0, te = 0, cnt = 0, p0 = 0;  // the tile: padded [tb, te), pairs, first product
+    u32 ea = 0, eb = 0, kt = 0;           // its A entries; its key offset (rank in the window x span)
+    BinWalk wk;
     bool fresh = true;
 #pragma unroll 1
     for (u32 i = 0; i < 8; i++) {
-      const u64 q = q0 + 32 * i;
+      const u64 q = c * 256 + 32 * i + lane;
       if (q >= ptot) break;
       if (fresh || q >= te) {  // this lane's next tile
-        if (!fresh)
-          while (u64(__ldg(&b.pp[s + 1])) <= q) s++;
+        while (u64(__ldg(&b.spp[s + 1])) <= q) s++;
         fresh = false;
-        tb = __ldg(&b.pp[s]);
-        te = __ldg(&b.pp[s + 1]);
+        tb = __ldg(&b.spp[s]);
+        te = __ldg(&b.spp[s + 1]);
         cnt = bin_tile_pairs(b, s);
-        if (__ldg(&b.nch[s]) == 0) {
-          const u32 sp = __ldg(&b.spp[s]);
-          d0 = sp;
-          kt = (__ldg(&b.srk[s]) - __ldg(&b.srk[__ldg(&b.first[sp / kBinWindow])])) * b.span;
-        } else {
-          d0 = sfull + __ldg(&b.lpp[s]);
-          kt = 0;
-        }
+        kt = (__ldg(&b.srk[s]) - __ldg(&b.srk[__ldg(&b.first[u32(tb / kBinWindow)])])) * b.span;
         const u32 t = b.tiles[s];
         ea = tile_abeg[t];
         eb = tile_abeg[t + 1];
         p0 = __ldg(&src.P[ea]);
-        e = kNoEntry;
+        wk.e = kNoEntry;
       }
       const u64 o = q - tb;
       u32 key = kBinEmpty;
       double v = 0.0;
       if (o < cnt) {
         const u64 p = p0 + o;
-        if (e == kNoEntry) {
-          u32 l = ea, h = eb;  // the A entry holding p: P[l] <= p < P[h]
-          while (h - l > 1) {
-            const u32 m = (l + h) >> 1;
-            if (__ldg(&src.P[m]) <= p) l = m;
-            else h = m;
-          }
-          e = l;
-          pe = __ldg(&src.P[e]);
-          pn = __ldg(&src.P[e + 1]);
-          sb = __ldg(&src.sbA[e]);
-          va = __ldg(&src.valA[e]);
-          kb = kt + __ldg(&src.slotA[e]) * b.LB;
+        if (wk.e == kNoEntry) {
+          wk.e = bin_entry_of(src.P, ea, eb, p);
+          wk.load(src, kt, b.LB);
         }
-        while (p >= pn) {  // the next A entries of the tile
-          e++;
-          pe = pn;
-          pn = __ldg(&src.P[e + 1]);
-          sb = __ldg(&src.sbA[e]);
-          va = __ldg(&src.valA[e]);
-          kb = kt + __ldg(&src.slotA[e]) * b.LB;
-        }
-        const u32 j = sb + u32(p - pe);
-        key = kb + u32(__ldg(&colB[j]));
-        v = va * __ldg(&src.valB[j]);
+        wk.at(src, colB, kt, b.LB, p, true, key, v);
       }
-      b.keys[d0 + o] = key;
-      b.vals[d0 + o] = u64(__double_as_longlong(v));
+      b.keys[q] = key;
+      b.vals[q] = u64(__double_as_longlong(v));
     }
   }
 }
 
-// Positions [q0, q1) of chunk g (tile s, chunk c) in the buffer.
-__device__ __forceinline__ void bin_chunk(const BinArgs &b, u32 g, u32 &s, u32 &c, u64 &q0, u64 &q1) {
-  s = b.chunk_tile[g];
-  c = g - b.chpre[s];
-  const u64 l0 = u64(b.spp[b.n]) + b.lpp[s];
-  q0 = l0 + u64(c) * kBinChunk;
-  q1 = min(l0 + b.lsz[s], q0 + kBinChunk);
+// Chunk g of the large tiles: tile s, chunk c, its products [p0 + o0, p0 + o1)
+// (tile offsets). Warp w of the CTA takes offsets o0 + 512 w + [0, 512),
+// lane l every 32nd from l; f(valid, local key, value) is called by every
+// lane of the warp at each step.
+template <class ColT, bool kVal, class F>
+__device__ __forceinline__ void bin_chunk_pairs(const BinArgs &b, const ProdSrc &src, const ColT *__restrict__ colB,
+                                                const u32 *__restrict__ tile_abeg, u32 s, u32 c, F &&f) {
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const u64 cnt = bin_tile_pairs(b, s);
+  const u64 w0 = u64(c) * kBinChunk + u64(warp) * (kBinChunk / 8);
+  if (w0 >= cnt) return;  // warp-uniform
+  const u64 w1 = min(cnt, w0 + kBinChunk / 8);
+  const u32 t = b.tiles[s];
+  const u32 ea = tile_abeg[t], eb = tile_abeg[t + 1];
+  const u64 p0 = __ldg(&src.P[ea]);
+  BinWalk wk;
+  wk.e = bin_entry_of(src.P, ea, eb, p0 + w0);  // the warp's first product; lanes walk on from it
+  wk.load(src, 0u, b.LB);
+  for (u64 o = w0 + lane; o - lane < w1; o += 32) {
+    const bool valid = o < w1;
+    u32 key = kBinEmpty;
+    double v = 0.0;
+    if (valid) wk.at(src, colB, 0u, b.LB, p0 + o, kVal, key, v);
+    f(valid, key, v);
+  }
 }
 
 // Pairs per block of each chunk of the large tiles.
-__global__ void __launch_bounds__(256) k_bin_hist(BinArgs b) {
+template <class ColT>
+__global__ void __launch_bounds__(256) k_bin_count(BinArgs b, const ProdSrc src, const ColT *__restrict__ colB,
+                                                   const u32 *__restrict__ tile_abeg) {
   __shared__ u32 h[kBinMaxBlocks];
   const u32 nchunks = b.chpre[b.n];
+  const u32 lane = threadIdx.x & 31;
   for (u32 g = blockIdx.x; g < nchunks; g += gridDim.x) {
     for (u32 i = threadIdx.x; i < b.nb; i += blockDim.x) h[i] = 0;
     __syncthreads();
-    u32 s, c;
-    u64 q0, q1;
-    bin_chunk(b, g, s, c, q0, q1);
-    for (u64 q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
-      const u32 k = b.keys[q];
-      if (k != kBinEmpty) atomicAdd(&h[k >> kBinBits], 1u);
-    }
+    const u32 s = b.chunk_tile[g], c = g - b.chpre[s];
+    bin_chunk_pairs<ColT, false>(b, src, colB, tile_abeg, s, c, [&](bool valid, u32 key, double) {
+      const u32 bin = valid ? key >> kBinBits : kBinMaxBlocks;
+      const u32 peers = __match_any_sync(kFull, bin);
+      if (bin < kBinMaxBlocks && lane == __ffs(peers) - 1) atomicAdd(&h[bin], u32(__popc(peers)));
+    });
     __syncthreads();
     const u64 r = u64(b.nb) * b.chpre[s] + c;
     const u32 nc = b.nch[s];
@@ -2366,34 +2389,32 @@ __global__ void __launch_bounds__(256) k_bin_hist(BinArgs b) {
   }
 }
 
-// Each chunk's pairs to their block's positions; lanes of one block take
-// consecutive positions with one shared atomic.
-__global__ void __launch_bounds__(256) k_bin_scatter(BinArgs b) {
+// Each chunk's pairs, computed again, to their block's positions; lanes of
+// one block take consecutive positions with one shared atomic.
+template <class ColT>
+__global__ void __launch_bounds__(256) k_bin_place(BinArgs b, const ProdSrc src, const ColT *__restrict__ colB,
+                                                   const u32 *__restrict__ tile_abeg) {
   __shared__ u32 cur[kBinMaxBlocks];
   const u32 nchunks = b.chpre[b.n];
   const u32 lane = threadIdx.x & 31;
   for (u32 g = blockIdx.x; g < nchunks; g += gridDim.x) {
-    u32 s, c;
-    u64 q0, q1;
-    bin_chunk(b, g, s, c, q0, q1);
+    const u32 s = b.chunk_tile[g], c = g - b.chpre[s];
     const u64 r = u64(b.nb) * b.chpre[s] + c;
     const u32 nc = b.nch[s];
     for (u32 i = threadIdx.x; i < b.nb; i += blockDim.x) cur[i] = b.hpre[r + u64(i) * nc];
     __syncthreads();
-    for (u64 qw = q0; qw < q1; qw += blockDim.x) {  // the same trip count in every lane
-      const u64 q = qw + threadIdx.x;
-      const u32 k = q < q1 ? b.keys[q] : kBinEmpty;
-      const u32 bin = k != kBinEmpty ? k >> kBinBits : kBinMaxBlocks;
+    bin_chunk_pairs<ColT, true>(b, src, colB, tile_abeg, s, c, [&](bool valid, u32 key, double v) {
+      const u32 bin = valid ? key >> kBinBits : kBinMaxBlocks;
       const u32 peers = __match_any_sync(kFull, bin);
       const u32 leader = __ffs(peers) - 1;
       u32 pos = 0;
       if (lane == leader && bin < kBinMaxBlocks) pos = atomicAdd(&cur[bin], u32(__popc(peers)));
       pos = __shfl_sync(kFull, pos, leader) + __popc(peers & ((1u << lane) - 1u));
-      if (bin < kBinMaxBlocks) {
-        b.bkeys[pos] = k;
-        b.bvals[pos] = b.vals[q];
+      if (valid) {
+        b.bkeys[pos] = key;
+        b.bvals[pos] = u64(__double_as_longlong(v));
       }
-    }
+    });
     __syncthreads();
   }
 }
@@ -3291,7 +3312,7 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
   u32 bin_nblk = 0;
   if (binned) {
     const u64 cap = esc_pairs + u64(kBinPer) * nesc;  // with every tile's padding
-    const u64 maxch = cap / kBinChunk + esc_pairs / (u64(bin_small) + 1) + 1;  // a large tile has > small_max pairs
+    const u64 maxch = esc_pairs / kBinChunk + esc_pairs / (u64(bin_small) + 1) + 1;  // a large tile has > small_max pairs
     bins.n = nesc;
     bins.small_max = bin_small;
     bins.nb = bin_nb;
@@ -3305,16 +3326,13 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     bins.total = esc_pairs;
     bins.keys = ar.get_n<u32>(cap);
     bins.vals = ar.get_n<u64>(cap);
-    u32 *per = ar.get_n<u32>(3 * u64(nesc));
-    bins.lsz = per;
-    bins.nch = per + nesc;
-    bins.small_list = per + 2 * u64(nesc);
-    u32 *pre = ar.get_n<u32>(5 * (u64(nesc) + 1));
-    bins.pp = pre;
-    bins.spp = pre + (nesc + 1);
-    bins.lpp = pre + 2 * (u64(nesc) + 1);
-    bins.chpre = pre + 3 * (u64(nesc) + 1);
-    bins.srk = pre + 4 * (u64(nesc) + 1);
+    u32 *per = ar.get_n<u32>(2 * u64(nesc));
+    bins.nch = per;
+    bins.small_list = per + nesc;
+    u32 *pre = ar.get_n<u32>(3 * (u64(nesc) + 1));
+    bins.spp = pre;
+    bins.chpre = pre + (u64(nesc) + 1);
+    bins.srk = pre + 2 * (u64(nesc) + 1);
     bin_nblk = (nesc + kPrepThreads - 1) / kPrepThreads;
     bin_bsum = ar.get_n<u32>(u64(kPrepVals) * bin_nblk);
     bins.chunk_tile = ar.get_n<u32>(maxch);
@@ -3601,10 +3619,10 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
           FCC_LAUNCH_CHECK();
           FCC_CUDA(cudaMemsetAsync(bins.hist, 0, sizeof(u32) * bins.hist_len, st));
           const int cgrid = ctx->num_sms * 8;
-          k_bin_hist<<<cgrid, 256, 0, st>>>(bins);
+          k_bin_count<ColT><<<cgrid, 256, 0, st>>>(bins, src, colptr, tile_abeg);
           FCC_LAUNCH_CHECK();
           scan_exclusive(bins.hist, bins.hpre, i64(bins.hist_len), bins.hpre + bins.hist_len, ar, st);
-          k_bin_scatter<<<cgrid, 256, 0, st>>>(bins);
+          k_bin_place<ColT><<<cgrid, 256, 0, st>>>(bins, src, colptr, tile_abeg);
           FCC_LAUNCH_CHECK();
           FCC_CUDA(cudaMemsetAsync(bins.njobs, 0, sizeof(u32), st));
           k_bin_jobs<<<grid_for(nesc, 256), 256, 0, st>>>(bins);
