@@ -2079,9 +2079,10 @@ __global__ void __launch_bounds__(256) k_esc_reduce(EscArgs a, const u32 *__rest
 //    its pairs per block, one exclusive scan over (tile, block, chunk) gives
 //    every chunk its positions, and the chunk computes its products again
 //    and writes each pair there. A block with more than kBinDenseMin pairs
-//    is reduced in a dense kBinWidth-entry accumulator with a bitmap of
-//    touched keys, runs of consecutive sparser blocks together in one hash
-//    table.
+//    is reduced in a dense kBinWidth-entry accumulator (untouched entries
+//    hold -0.0), runs of consecutive sparser blocks together in one hash
+//    table. Every first update of a slot appends it to a list of occupied
+//    slots, from which the outputs are written.
 // Every reduced window or block reserves its outputs with one atomic and
 // writes them. Every pair is written once and read once; keys never need
 // more than 32 bits, so every expanded tile goes through one set of launches.
@@ -2097,7 +2098,8 @@ constexpr u32 kBinHashPairs = 4096;        // sparse blocks merged up to this ma
 constexpr u32 kBinSlots = 8192;            // hash slots: > 4/3 x (kBinWindow + kBinSmallMax - 1)
 constexpr int kBinThreads = 512;
 constexpr u32 kBinEmpty = 0xFFFFFFFFu;     // padding / free slot (keys stay below 257 x 2^21)
-constexpr size_t kBinSmem = size_t(kBinSlots) * (sizeof(double) + sizeof(u32));
+// values, keys, and the list of occupied slots
+constexpr size_t kBinSmem = size_t(kBinSlots) * (sizeof(double) + sizeof(u32) + sizeof(uint16_t));
 constexpr u32 kBinPer = 8;                 // the tiles' padding unit
 constexpr int kBinIlp = 4;                 // pairs per thread in flight in the reductions
 
@@ -2474,16 +2476,35 @@ __device__ __forceinline__ bool bin_aggregate(u32 key, double *v) {
 }
 
 // Shared-memory hash insert: linear probing from a multiplicative hash, the
-// table never full (slots > pairs); a slot's key is read before it is claimed.
-__device__ __forceinline__ void bin_insert(u32 *tk, double *tv, u32 mask, u32 lg, u32 key, double v) {
+// table never full (slots > pairs); a slot's key is read before it is
+// claimed. Returns true when this call claimed the slot (*slot).
+__device__ __forceinline__ bool bin_insert(u32 *tk, double *tv, u32 mask, u32 lg, u32 key, double v, u32 *slot) {
   u32 h = (key * 2654435761u) >> (32 - lg);
+  bool claimed = false;
   for (;;) {
     u32 cur = reinterpret_cast<volatile u32 *>(tk)[h];
-    if (cur == kBinEmpty) cur = atomicCAS(&tk[h], kBinEmpty, key);
+    if (cur == kBinEmpty) {
+      cur = atomicCAS(&tk[h], kBinEmpty, key);
+      claimed = cur == kBinEmpty;
+    }
     if (cur == kBinEmpty || cur == key) break;
     h = (h + 1) & mask;
   }
   atomicAdd(&tv[h], v);  // under contention the built-in add beats a compare-and-swap loop
+  *slot = h;
+  return claimed;
+}
+
+// Appends the slots this warp's lanes claimed to the CTA's list of occupied
+// slots (one shared atomic per warp). Every lane of the warp calls it.
+__device__ __forceinline__ void bin_list_append(bool claimed, u32 slot, uint16_t *list, u32 *nocc) {
+  const u32 m = __ballot_sync(kFull, claimed);
+  if (!m) return;
+  const u32 lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  u32 base = 0;
+  if (lane == leader) base = atomicAdd(nocc, u32(__popc(m)));
+  base = __shfl_sync(kFull, base, leader);
+  if (claimed) list[base + __popc(m & ((1u << lane) - 1u))] = uint16_t(slot);
 }
 
 // Output row and column of a reduced key: a window's key is the tile's rank
@@ -2518,66 +2539,21 @@ __device__ __forceinline__ void bin_emit_one(const BinArgs &b, const u32 *__rest
   emit(out, dec, idx, rc.row, col, v);
 }
 
-// Emits the table's occupied slots (hash: tk[i] != empty; dense: bit i of
-// bitmap tk) with one reservation for the CTA; slots [0, n), n a multiple of
-// 32. Each warp packs the occupied slots of its words into a 64-entry ring
-// and writes full warps of outputs from it (the decode and the stores then
-// run on all 32 lanes instead of on the occupied ones only).
-struct BinRing {
-  u32 k[kBinThreads / 32][64];
-  double v[kBinThreads / 32][64];
-};
-
-template <bool kDense>
-__device__ void bin_emit(const BinArgs &b, const u32 *__restrict__ tile_rank0, const u64 *__restrict__ urow,
-                         const Out &out, const Decode &dec, u32 *err, const BinWho &who, const u32 *tk,
-                         const double *tv, u32 n, u32 dkey0, u32 *s_wcnt, u64 *s_base, BinRing &ring) {
-  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  u32 cnt = 0;
-  for (u32 w = warp; w < n / 32; w += nw) {
-    const u32 m = kDense ? tk[w] : __ballot_sync(kFull, tk[w * 32 + lane] != kBinEmpty);
-    cnt += __popc(m);
-  }
-  if (lane == 0) s_wcnt[warp] = cnt;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    u32 tot = 0;
-    for (u32 i = 0; i < nw; i++) {
-      const u32 c = s_wcnt[i];
-      s_wcnt[i] = tot;
-      tot += c;
-    }
-    *s_base = reserve(out, tot, err);
-  }
+// Emits the nocc slots of the list (key tk[slot], or k0 + slot for a dense
+// block; value tv[slot]) with one reservation for the CTA: consecutive
+// threads write consecutive outputs.
+__device__ __forceinline__ void bin_emit(const BinArgs &b, const u32 *__restrict__ tile_rank0,
+                                         const u64 *__restrict__ urow, const Out &out, const Decode &dec, u32 *err,
+                                         const BinWho &who, const uint16_t *list, u32 nocc, const u32 *tk,
+                                         const double *tv, bool dense, u32 k0, u64 *s_base) {
+  if (threadIdx.x == 0) *s_base = reserve(out, nocc, err);
   __syncthreads();
   const u64 base = *s_base;
   if (base != ~0ull) {  // else over capacity: counted by the cursor, retried by the host
-    u64 idx = base + s_wcnt[warp];
-    u32 *rk = ring.k[warp];
-    double *rv = ring.v[warp];
-    u32 head = 0, tail = 0;  // entries queued / written
     BinRowCache rc;
-    for (u32 w = warp; w < n / 32; w += nw) {
-      const u32 i = w * 32 + lane;
-      const u32 m = kDense ? tk[w] : __ballot_sync(kFull, tk[i] != kBinEmpty);
-      if ((m >> lane) & 1u) {
-        const u32 e = (head + __popc(m & ((1u << lane) - 1u))) & 63u;
-        rk[e] = kDense ? dkey0 + i : tk[i];
-        rv[e] = tv[i];
-      }
-      head += __popc(m);
-      __syncwarp();
-      if (head - tail >= 32) {
-        const u32 e = (tail + lane) & 63u;
-        bin_emit_one(b, tile_rank0, urow, out, dec, who, rc, idx + lane, rk[e], rv[e]);
-        idx += 32;
-        tail += 32;
-        __syncwarp();
-      }
-    }
-    if (lane < head - tail) {
-      const u32 e = (tail + lane) & 63u;
-      bin_emit_one(b, tile_rank0, urow, out, dec, who, rc, idx + lane, rk[e], rv[e]);
+    for (u32 i = threadIdx.x; i < nocc; i += blockDim.x) {
+      const u32 slot = list[i];
+      bin_emit_one(b, tile_rank0, urow, out, dec, who, rc, base + i, dense ? k0 + slot : tk[slot], tv[slot]);
     }
   }
   __syncthreads();
@@ -2585,15 +2561,16 @@ __device__ void bin_emit(const BinArgs &b, const u32 *__restrict__ tile_rank0, c
 
 // Hash-reduces positions [lo, hi) of (keys, vals), padding skipped.
 __device__ __forceinline__ void bin_hash(const u32 *__restrict__ keys, const u64 *__restrict__ vals, u64 lo, u64 hi,
-                                         u32 *tk, double *tv, u32 &slots) {
+                                         u32 *tk, double *tv, uint16_t *list, u32 *nocc) {
   const u32 np = u32(hi - lo);
   u32 lg = 5;
   while ((1u << lg) < np + np / 3 + 1) lg++;
-  slots = 1u << lg;
+  const u32 slots = 1u << lg;
   for (u32 i = threadIdx.x; i < slots; i += blockDim.x) {
     tk[i] = kBinEmpty;
     tv[i] = 0.0;
   }
+  if (threadIdx.x == 0) *nocc = 0;
   __syncthreads();
   for (u64 q0 = lo; q0 < hi; q0 += u64(blockDim.x) * kBinIlp) {  // the same trip count in every lane
     u32 k[kBinIlp];
@@ -2605,8 +2582,11 @@ __device__ __forceinline__ void bin_hash(const u32 *__restrict__ keys, const u64
       v[i] = q < hi ? __longlong_as_double((long long)vals[q]) : 0.0;
     }
 #pragma unroll
-    for (int i = 0; i < kBinIlp; i++)
-      if (bin_aggregate(k[i], &v[i])) bin_insert(tk, tv, slots - 1, lg, k[i], v[i]);
+    for (int i = 0; i < kBinIlp; i++) {
+      u32 slot = 0;
+      const bool claimed = bin_aggregate(k[i], &v[i]) && bin_insert(tk, tv, slots - 1, lg, k[i], v[i], &slot);
+      bin_list_append(claimed, slot, list, nocc);
+    }
   }
   __syncthreads();
 }
@@ -2618,11 +2598,11 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_reduce(BinArgs b, const u32
                                                             const u64 *__restrict__ urow, const Out out,
                                                             const Decode dec, u32 *err) {
   extern __shared__ __align__(16) unsigned char bin_smem[];
-  double *tv = reinterpret_cast<double *>(bin_smem);  // kBinSlots values (dense: the block)
-  u32 *tk = reinterpret_cast<u32 *>(tv + kBinSlots);   // kBinSlots keys (dense: the bitmap)
-  __shared__ u32 s_job, s_wcnt[kBinThreads / 32];
+  double *tv = reinterpret_cast<double *>(bin_smem);               // kBinSlots values (dense: the block)
+  u32 *tk = reinterpret_cast<u32 *>(tv + kBinSlots);                // kBinSlots keys (hash)
+  uint16_t *list = reinterpret_cast<uint16_t *>(tk + kBinSlots);   // occupied slots
+  __shared__ u32 s_job, s_nocc;
   __shared__ u64 s_base;
-  __shared__ BinRing ring;
   const u32 nbig = *b.njobs;
   const u64 nwin = (u64(b.spp[b.n]) + kBinWindow - 1) / kBinWindow;
   const u64 njobs = u64(nbig) + nwin;
@@ -2641,9 +2621,13 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_reduce(BinArgs b, const u32
       const u64 r = u64(b.nb) * b.chpre[jb.s];
       const u32 lo = b.hpre[r + u64(jb.b0) * nc], hi = b.hpre[r + u64(jb.b1) * nc];
       if (jb.b1 == jb.b0 + 1 && hi - lo > kBinDenseMin) {  // dense block
+        // Untouched positions hold -0.0 and every update adds a value that is
+        // not -0.0 (a -0.0 product is added as +0.0): a sum never returns to
+        // -0.0 in round-to-nearest, so "touched" is "not -0.0", with no
+        // bitmap to maintain.
         const u32 k0 = u32(jb.b0) * kBinWidth;
-        for (u32 i = threadIdx.x; i < kBinWidth; i += blockDim.x) tv[i] = 0.0;
-        for (u32 i = threadIdx.x; i < kBinWidth / 32; i += blockDim.x) tk[i] = 0u;
+        for (u32 i = threadIdx.x; i < kBinWidth; i += blockDim.x) tv[i] = -0.0;
+        if (threadIdx.x == 0) s_nocc = 0;
         __syncthreads();
         for (u32 q0 = lo; q0 < hi; q0 += blockDim.x * kBinIlp) {  // the same trip count in every lane
           u32 loc[kBinIlp];
@@ -2656,26 +2640,24 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_reduce(BinArgs b, const u32
           }
 #pragma unroll
           for (int i = 0; i < kBinIlp; i++) {
-            if (bin_aggregate(loc[i], &v[i])) {
-              atomicAdd(&tv[loc[i]], v[i]);
-              atomicOr(&tk[loc[i] >> 5], 1u << (loc[i] & 31));
-            }
+            bool first = false;
+            if (bin_aggregate(loc[i], &v[i]))
+              first = __double_as_longlong(atomicAdd(&tv[loc[i]], v[i] + 0.0)) == (long long)0x8000000000000000ull;
+            bin_list_append(first, loc[i], list, &s_nocc);
           }
         }
         __syncthreads();
-        bin_emit<true>(b, tile_rank0, urow, out, dec, err, who, tk, tv, kBinWidth, k0, s_wcnt, &s_base, ring);
+        bin_emit(b, tile_rank0, urow, out, dec, err, who, list, s_nocc, tk, tv, true, k0, &s_base);
       } else {  // sparse blocks: at most kBinHashPairs pairs
-        u32 slots;
-        bin_hash(b.bkeys, b.bvals, lo, hi, tk, tv, slots);
-        bin_emit<false>(b, tile_rank0, urow, out, dec, err, who, tk, tv, slots, 0, s_wcnt, &s_base, ring);
+        bin_hash(b.bkeys, b.bvals, lo, hi, tk, tv, list, &s_nocc);
+        bin_emit(b, tile_rank0, urow, out, dec, err, who, list, s_nocc, tk, tv, false, 0, &s_base);
       }
     } else {  // a window of small tiles: fewer than kBinWindow + small_max positions
       const u64 w = j - nbig;
       const u32 f0 = b.first[w], f1 = b.first[w + 1];
       const BinWho who{true, 0, b.srk[f0]};
-      u32 slots;
-      bin_hash(b.keys, b.vals, b.spp[f0], b.spp[f1], tk, tv, slots);
-      bin_emit<false>(b, tile_rank0, urow, out, dec, err, who, tk, tv, slots, 0, s_wcnt, &s_base, ring);
+      bin_hash(b.keys, b.vals, b.spp[f0], b.spp[f1], tk, tv, list, &s_nocc);
+      bin_emit(b, tile_rank0, urow, out, dec, err, who, list, s_nocc, tk, tv, false, 0, &s_base);
     }
     if (threadIdx.x == 0) s_job = next;
     __syncthreads();
