@@ -492,8 +492,8 @@ def run_twomode(steps, stream, local, cpu=True):
     alg = 2 * coo_bytes(a.nnz, a.order) + coo_bytes(outs, order)
     out = {"workload": w["name"], "multiply_adds": prods, "outputs": outs, "gpu_ms": ms,
            "multiply_adds_per_s": prods / (ms / 1000.0), "phases_ms": med,
-           "roofline": hbm_roofline(alg, ms, "whole contraction (index, plan, expanded hash tiles: expand, "
-                                             "radix sort, reduce)")}
+           "roofline": hbm_roofline(alg, ms, "whole contraction (index, plan, expanded hash tiles: expanded, "
+                                             "hub rows partitioned by key blocks, reduced in shared memory)")}
     if cpu:
         p, _, dt = cpu_port(a, a, w["ctr_a"], w["ctr_b"])
         out["cpu_baseline"] = {"value": p / dt, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
