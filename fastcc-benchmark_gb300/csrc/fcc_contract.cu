@@ -2090,7 +2090,7 @@ __global__ void __launch_bounds__(256) k_esc_reduce(EscArgs a, const u32 *__rest
 constexpr u32 kBinBits = 13;
 constexpr u32 kBinWidth = 1u << kBinBits;  // local keys per block: 8192 doubles, 64 KB
 constexpr u32 kBinMaxBlocks = 256;         // blocks per tile: spans up to 2^21 keys
-constexpr u32 kBinChunk = 4096;            // positions per partition chunk (a multiple of 8)
+constexpr u32 kBinChunk = 4096;            // products per partition chunk (a multiple of 8)
 constexpr u32 kBinWindow = 2048;           // small-tile positions per window
 constexpr u32 kBinSmallMax = 4096;         // default (and largest) small tile; a multiple of 8
 constexpr u32 kBinDenseMin = 2048;         // a block with more pairs is reduced densely
@@ -2264,17 +2264,25 @@ struct BinWalk {
     va = __ldg(&src.valA[e]);
     kb = kt + __ldg(&src.slotA[e]) * LB;
   }
-  // key kb + column and value of product p (p at or after the current entry's first)
-  template <class ColT>
+  // key kb + column and value of product p (p at or after the current entry's
+  // first). Entries it passes over cost one load each (their ends); the
+  // entry it stops at loads the rest once.
+  template <bool kVal, class ColT>
   __device__ __forceinline__ void at(const ProdSrc &src, const ColT *__restrict__ colB, u32 kt, u32 LB, u64 p,
-                                     bool want_val, u32 &key, double &v) {
-    while (p >= pn) {
-      e++;
-      load(src, kt, LB);
+                                     u32 &key, double &v) {
+    if (p >= pn) {
+      do {
+        e++;
+        pe = pn;
+        pn = __ldg(&src.P[e + 1]);
+      } while (p >= pn);
+      sb = __ldg(&src.sbA[e]);
+      if (kVal) va = __ldg(&src.valA[e]);
+      kb = kt + __ldg(&src.slotA[e]) * LB;
     }
     const u32 j = sb + u32(p - pe);
     key = kb + u32(__ldg(&colB[j]));
-    v = want_val ? va * __ldg(&src.valB[j]) : 0.0;
+    v = kVal ? va * __ldg(&src.valB[j]) : 0.0;
   }
 };
 
@@ -2332,7 +2340,7 @@ __global__ void __launch_bounds__(256) k_bin_expand(BinArgs b, const ProdSrc src
           wk.e = bin_entry_of(src.P, ea, eb, p);
           wk.load(src, kt, b.LB);
         }
-        wk.at(src, colB, kt, b.LB, p, true, key, v);
+        wk.at<true>(src, colB, kt, b.LB, p, key, v);
       }
       b.keys[q] = key;
       b.vals[q] = u64(__double_as_longlong(v));
@@ -2362,7 +2370,7 @@ __device__ __forceinline__ void bin_chunk_pairs(const BinArgs &b, const ProdSrc 
     const bool valid = o < w1;
     u32 key = kBinEmpty;
     double v = 0.0;
-    if (valid) wk.at(src, colB, 0u, b.LB, p0 + o, kVal, key, v);
+    if (valid) wk.at<kVal>(src, colB, 0u, b.LB, p0 + o, key, v);
     f(valid, key, v);
   }
 }
