@@ -91,9 +91,10 @@ typedef struct fcc_options {
   int32_t dense_cap;          /* doubles per shared-memory dense tile; 0 = planner */
   int32_t hash_slots;         /* shared-memory hash slots (power of two); 0 = planner */
   int32_t timing;             /* 1: record per-phase CUDA-event times (fcc_last_timings) */
-  int32_t esc_small;          /* esc_reduce 1: expanded tiles with at most this many pairs are
-                                 reduced in windows, larger ones partitioned by key blocks
-                                 first; 0 (default): 4096, the largest allowed */
+  int32_t esc_small;          /* expanded pairs reduced in shared memory (esc_reduce): tiles
+                                 with at most this many pairs are small (reduced in windows of
+                                 consecutive small tiles), larger ones are partitioned by key
+                                 blocks first; 0 (default): 4096, the largest allowed */
   int64_t capacity_hint;      /* first output allocation in entries; 0 = planner bound. A
                                  smaller hint is not an error: the device counts every output
                                  and the call retries once with the exact count. */
@@ -147,14 +148,15 @@ typedef struct fcc_options {
                                  with atomic adds. 0 (default): 3, except under the learned
                                  schedule, whose FCC_CLASS_DENSE tiles run 1 (and whose
                                  FCC_CLASS_DENSE_FLAT tiles run 2) */
-  int32_t esc_reduce;         /* how expanded pairs (hash_esc) are reduced. 1: in shared memory:
-                                 a tile's pairs are contiguous after the expansion, so small
-                                 tiles are reduced in hash tables over windows of consecutive
-                                 tiles, and large ones are partitioned by blocks of 8192 keys,
-                                 each block reduced densely or, when sparse, with its sparse
-                                 neighbours in a hash table; 2: a radix sort of the group's keys,
-                                 then one pass over the runs of equal keys. 0 (default): 1 where
-                                 the keys fit 32 bits and a tile spans at most 2^21 keys, else 2 */
+  int32_t esc_reduce;         /* how expanded pairs (hash_esc) are reduced. 0 (default) or 1: in
+                                 shared memory, no sort: small tiles in hash tables over
+                                 windows of consecutive small tiles, large ones computed
+                                 straight into blocks of 8192 keys, each block reduced densely
+                                 or, when sparse, with its sparse neighbours in a hash table;
+                                 used where a tile spans at most 2^21 keys and the pairs (each
+                                 small tile padded to 8) count in 32 bits, else 2. 2: a radix
+                                 sort of groups of tiles whose keys fit 32 bits (64-bit keys
+                                 otherwise), then one pass over the runs of equal keys */
 } fcc_options;
 
 /* Tile classes: every output tile runs in one of them. The hash classes
