@@ -46,6 +46,7 @@ fcc::Runtime runtime_of(fcc_ctx *ctx) {
   rt.copy_stream = ctx->copy_stream;
   rt.wave_ev = ctx->wave_ev;
   rt.h_cursors = ctx->h_cursors;
+  rt.wave_tune = &ctx->wave_tune;
   return rt;
 }
 

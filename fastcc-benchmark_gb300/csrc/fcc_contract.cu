@@ -26,6 +26,7 @@
 //    and drained by k_merge_*.
 
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <memory>
 #include <type_traits>
@@ -3481,10 +3482,17 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
       stream_out = false;
     }
   }
-  // One wave (compute, then one copy) unless more are asked for: the copies
-  // of a wave slow the tile kernels running beside them, by a factor that
-  // differs from box to box (measured 1.9x to 6x on the contract phase).
-  const int waves = !stream_out || opt.out_waves <= 0 ? 1 : opt.out_waves;
+  // One wave (compute, then one copy) unless more are asked for, or, for a
+  // large output with out_waves 0, unless the context measured waves faster
+  // (WaveTune): the copies of a wave slow the tile kernels running beside
+  // them, by a factor that differs from box to box (measured 1.9x to 6x on
+  // the contract phase).
+  int waves = !stream_out || opt.out_waves <= 0 ? 1 : opt.out_waves;
+  const u64 out_bytes = cap * (8 + 4 * u64(out_order));
+  WaveTune *wt = stream_out && opt.out_waves == 0 && out_bytes >= kAutoWaveBytes ? ctx->wave_tune : nullptr;
+  const int wt_trial = wt && wt->trials < 2 ? wt->trials : -1;
+  if (wt) waves = wt_trial == 0 ? 1 : wt_trial == 1 ? kAutoWaves : wt->pick;
+  const auto wt_t0 = std::chrono::steady_clock::now();
   for (int attempt = 0;; attempt++) {
     i64 stride = i64(cap);
     if (!caller_out) {
@@ -3693,6 +3701,10 @@ void contract(Runtime *ctx, const fcc_tensor *A, const fcc_tensor *B, const int3
     const bool overflow = (u32(ctx->h_scalars[S_ERR]) & ERRB_OVERFLOW) != 0 || produced > cap;
     if (!overflow) {
       res->nnz = i64(produced);
+      if (wt_trial >= 0) {  // a measured trial of the wave choice
+        wt->ms[wt_trial] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wt_t0).count();
+        if (++wt->trials == 2) wt->pick = wt->ms[1] < wt->ms[0] ? kAutoWaves : 1;
+      }
       break;
     }
     if (caller_out) {

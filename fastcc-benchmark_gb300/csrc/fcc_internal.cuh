@@ -158,6 +158,8 @@ void tile_costs(cudaStream_t st, u32 ntiles, const u32 *corder, const u32 *cls, 
                 const u32 *t_items, const u64 *item_cyc, const double *occ, const u64 *merge_cyc,
                 double merge_occ, double *cost);
 
+struct WaveTune;  // below
+
 struct Runtime {
   explicit Runtime(Arena &a) : arena(a) {}
   Arena &arena;
@@ -179,10 +181,24 @@ struct Runtime {
   cudaStream_t copy_stream = nullptr;  // device-to-host copies of finished output ranges
   cudaEvent_t *wave_ev = nullptr;      // kMaxWaves + 1 events, one per wave and one after the merges
   u64 *h_cursors = nullptr;            // pinned, kMaxWaves + 1 output cursor snapshots
+  WaveTune *wave_tune = nullptr;       // the context's choice between one copy and waves (NULL: one copy)
 };
 
 // A pinned host output is produced in at most this many waves of tiles.
 constexpr int kMaxWaves = 16;
+
+// out_waves 0 with a large pinned host output: the first such call copies
+// the output once after the contraction, the second runs kAutoWaves waves
+// (copies overlapping the contraction), and later calls take whichever was
+// faster. Which one wins depends on the host link: the copies slow the tile
+// kernels beside them by a factor that differs from box to box.
+constexpr int kAutoWaves = 12;
+constexpr unsigned long long kAutoWaveBytes = 1ull << 30;  // outputs below this: one copy
+struct WaveTune {
+  int trials = 0;    // calls measured so far (0, 1 or 2)
+  double ms[2] = {}; // their wall times: one copy, waves
+  int pick = 1;      // waves after the trials
+};
 
 void set_thread_error(const std::string &msg);
 void *pool_alloc(cudaMemPool_t pool, size_t bytes, cudaStream_t st);  // fcc_prims.cu
@@ -205,6 +221,7 @@ struct fcc_ctx {
   cudaEvent_t wave_ev[fcc::kMaxWaves + 1] = {};
   fcc::u64 *h_cursors = nullptr;               // pinned
   fcc::SchedIo sched;
+  fcc::WaveTune wave_tune;
   std::map<std::string, std::pair<fcc_options, double>> tuned;  // autotuner cache: signature -> best
   std::string last_error;
 };

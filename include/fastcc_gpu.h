@@ -124,8 +124,10 @@ typedef struct fcc_options {
   int32_t out_waves;          /* fcc_contract_into with pinned host output buffers: the output is
                                  produced in device memory in this many waves of tiles (1..16),
                                  each wave's outputs copied to the host while the next computes.
-                                 0 (default): one wave, i.e. the whole output computed, then
-                                 copied once */
+                                 0 (default): one wave (the whole output computed, then copied
+                                 once), except for outputs of 1 GiB or more: the context's first
+                                 such call copies once, its second runs 12 waves, and later calls
+                                 take whichever of the two was faster */
   int32_t esc_group;          /* expanded hash tiles are sorted in groups whose keys fit 32 bits;
                                  0 (default): as many tiles per group as that allows; > 0: at
                                  most this many */
