@@ -5,6 +5,7 @@ import os
 import re
 import subprocess
 
+import numpy as np
 import pytest
 
 import fastcc_gpu as F
@@ -80,3 +81,19 @@ def test_python_options_mirror_the_c_layout():
     assert [width[t] for t, _ in c] == [w for _, w in py]
     for (t, name), (pname, _) in zip(c, py):
         assert getattr(F.Options, pname).offset % width[t] == 0
+
+
+def test_shipped_cost_model_matches_the_header_layout():
+    # FCC_SCHED_MODEL_FLOATS as the header computes it, the Python constant and
+    # the shipped model file agree (a model trained for another output count
+    # would be rejected at fcc_sched_set_model)
+    txt = open(os.path.join(ROOT, "include", "fastcc_gpu.h")).read()
+    m = re.search(r"#define FCC_SCHED_MODEL_FLOATS \(([^)]*)\)", txt)
+    assert m
+    n = eval(m.group(1), {})  # integer arithmetic only
+    assert n == F.SCHED_MODEL_FLOATS
+    k = int(re.search(r"FCC_NUM_CLASSES = (\d+)", txt).group(1))
+    assert k == F.NUM_CLASSES and n == 2 * 12 + 12 * 64 + 64 + 64 * 64 + 64 + 64 * k + k
+    path = os.path.join(ROOT, "fastcc-benchmark_gb300", "sched_model.f32")
+    model = np.fromfile(path, np.float32)
+    assert model.size == n and np.all(np.isfinite(model))
